@@ -1,0 +1,461 @@
+"""Benchmark: lattice-Boltzmann step throughput (MLUPS) and HBM bandwidth.
+
+Workload (default): the 256x192x512 Y-bifurcation (parent r=24 lu, daughters
+r=17 lu at +/-30 deg, seed 0), D3Q19 BGK, FP32 storage, tau=0.55, parabolic
+pulsatile velocity inlet u(t)=0.03(1+0.5 sin(2 pi t/4000)+0.2 sin(4 pi t/4000))
+on the z-min face, density outlet rho=1 on the z-max face, half-way
+bounce-back walls, wall shear stress on every next-to-wall node each step.
+
+One bench "step" is one LBM time step over the whole lattice.  Each timed
+step is bracketed by CUDA events on the solver's own stream, and the L2 is
+flushed (a 512 MB device memset) between timed steps, outside the events.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With --gpus N > 1 (launched by torchrun) every rank advances an independent
+replica of the lattice (the single-domain solver has no inter-GPU exchange);
+value = total lattice updates of all ranks / max rank time.
+--impl reference times the CPU oracle (the reference's algorithm restated in
+C, FP64, parity semantics) on this host's cores on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_LU = {(19, "f32"): 152, (19, "f16"): 76, (19, "bf16"): 76, (19, "f64"): 304,
+                (27, "f32"): 216, (27, "f16"): 108, (27, "bf16"): 108, (27, "f64"): 432}
+L2_FLUSH_BYTES = 512 << 20
+TAU = 0.55
+U_MEAN = 0.03
+PERIOD = 4000.0
+
+
+# --------------------------------------------------------------------------- cudart via ctypes
+
+class Cudart:
+    def __init__(self):
+        self.L = C.CDLL("libcudart.so.13")
+        for name in ("cudaEventCreate", "cudaEventRecord", "cudaEventSynchronize", "cudaEventElapsedTime",
+                     "cudaEventDestroy", "cudaMalloc", "cudaFree", "cudaMemsetAsync", "cudaHostAlloc",
+                     "cudaFreeHost", "cudaStreamSynchronize", "cudaSetDevice", "cudaGetDeviceProperties"):
+            getattr(self.L, name).restype = C.c_int
+
+    def ck(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} failed: cuda error {rc}")
+
+    def event(self):
+        e = C.c_void_p()
+        self.ck(self.L.cudaEventCreate(C.byref(e)), "cudaEventCreate")
+        return e
+
+    def record(self, e, stream):
+        self.ck(self.L.cudaEventRecord(e, C.c_void_p(stream)), "cudaEventRecord")
+
+    def elapsed_ms(self, a, b):
+        self.ck(self.L.cudaEventSynchronize(b), "cudaEventSynchronize")
+        ms = C.c_float()
+        self.ck(self.L.cudaEventElapsedTime(C.byref(ms), a, b), "cudaEventElapsedTime")
+        return ms.value
+
+    def malloc(self, n):
+        p = C.c_void_p()
+        self.ck(self.L.cudaMalloc(C.byref(p), C.c_size_t(n)), "cudaMalloc")
+        return p
+
+    def memset_async(self, p, v, n, stream):
+        self.ck(self.L.cudaMemsetAsync(p, C.c_int(v), C.c_size_t(n), C.c_void_p(stream)), "cudaMemsetAsync")
+
+    def host_alloc(self, n):
+        p = C.c_void_p()
+        self.ck(self.L.cudaHostAlloc(C.byref(p), C.c_size_t(n), C.c_uint(0)), "cudaHostAlloc")
+        return p
+
+
+def pinned_array(cr, n, dtype):
+    p = cr.host_alloc(max(1, n) * np.dtype(dtype).itemsize)
+    buf = (C.c_char * (max(1, n) * np.dtype(dtype).itemsize)).from_address(p.value)
+    return np.frombuffer(buf, dtype=dtype, count=n), p
+
+
+# --------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- workload
+
+def c2_workload():
+    from pv_dec_original_gb300 import geometry as G
+    surf = G.config_c2_bifurcation()
+    return surf, surf.tri12()
+
+
+def c2_bcs(capi, surf, mask):
+    fl = np.argwhere(mask > 0)  # (k, j, i)
+    kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
+    cx, cy = surf.meta["center"]
+    return [capi.bc_spec(capi.LBM_BC_VELOCITY, "z-", kin, 1.0, 1, cx, cy, surf.meta["parent_radius"]),
+            capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)], (kin, kout)
+
+
+def make_solver(capi, mask, surf, tri, Q, prec, origin, device):
+    from pv_dec_original_gb300 import waveform
+    s = capi.Solver(Q, prec, capi.LBM_PHYSICS, TAU, 1.0, origin, 1.0, PERIOD, device)
+    bcs, planes = c2_bcs(capi, surf, mask)
+    s.set_geometry(mask, bcs)
+    s.set_normals(tri)
+    s.set_inlet_table(waveform.sinusoid_table(U_MEAN, PERIOD))
+    return s, planes
+
+
+def time_steps(cr, s, steps, flush, stream):
+    """Per-step event timing with an L2 flush between steps (outside events)."""
+    evs = [(cr.event(), cr.event()) for _ in range(steps)]
+    for a, b in evs:
+        cr.memset_async(flush, 0, L2_FLUSH_BYTES, stream)
+        cr.record(a, stream)
+        s.step_async(1)
+        cr.record(b, stream)
+    ms = [cr.elapsed_ms(a, b) for a, b in evs]
+    s.check_status()
+    for a, b in evs:
+        cr.L.cudaEventDestroy(a)
+        cr.L.cudaEventDestroy(b)
+    return ms
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def read_traffic(name):
+    """dram bytes per launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch"):
+            try:
+                return float(line.split("=", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(tri, mask, bb, planes, cores, seconds=12.0, mode=None):
+    """The CPU oracle (FP64) on this host: as many C2 steps as fit in ~seconds."""
+    from oracle import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import classify
+    from pv_dec_original_gb300 import waveform
+    kin, kout = planes
+    cls = classify(mask, [(2, kin), (2, kout)])
+    surf_c = (0.5 * 255 + 0.213, 0.5 * 191 + 0.087)
+    bcs = [dict(kind=O.BC_VELOCITY, face=4, plane=kin, value=1.0, profile=1, c1=surf_c[0], c2=surf_c[1], R=24.0),
+           dict(kind=O.BC_PRESSURE, face=5, plane=kout, value=1.0)]
+    sim = O.Sim(19, O.PARITY if mode is None else mode, cls, (bb[0], bb[2], bb[4]), 1.0, TAU, bcs)
+    sim.set_amplitude(waveform.sinusoid_table(U_MEAN, PERIOD))
+    sim.step(1, cores)  # warm-up (page-in)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        sim.step(1, cores)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 200:
+            break
+    return sim.nactive * n / el / 1e6, n, el, sim.nactive
+
+
+# --------------------------------------------------------------------------- arms
+
+def dist_setup(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend=backend)
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def max_over_ranks(dist, x, backend_device=None):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=backend_device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args):
+    ws, rank, local, dist = dist_setup("nccl")
+    from pv_dec_original_gb300 import capi
+    capi.load(build_if_missing=True)
+    cr = Cudart()
+    cr.ck(cr.L.cudaSetDevice(local), "cudaSetDevice")
+    dev_t = None
+    if dist is not None:
+        import torch
+        torch.cuda.set_device(local)
+        dev_t = torch.device("cuda", local)
+
+    surf, tri = c2_workload()
+    mask, desc = capi.voxelize(tri, 1.0)
+    bb = np.array(desc.bbox[:])
+    origin = (bb[0], bb[2], bb[4])
+    s, planes = make_solver(capi, mask, surf, tri, args.Q, args.precision, origin, local)
+    cnt = s.counts()
+    active = cnt["active"]
+    stream = s.stream()
+    flush = cr.malloc(L2_FLUSH_BYTES)
+
+    s.step(args.warmup)
+    if dist is not None:
+        dist.barrier()
+    cr.ck(cr.L.cudaStreamSynchronize(C.c_void_p(stream)), "sync")
+    launches0 = s.launches()
+    with ClockSampler(local) as clk:
+        ms = time_steps(cr, s, args.steps, flush, stream)
+    launches = s.launches() - launches0
+    cr.ck(cr.L.cudaStreamSynchronize(C.c_void_p(stream)), "sync")
+    total_ms = sum(ms)
+    total_ms_max = max_over_ranks(dist, total_ms, dev_t)
+    mean_ms = total_ms / len(ms)
+    value = ws * active * args.steps / (total_ms_max * 1e-3) / 1e6
+    bpl = BYTES_PER_LU[(args.Q, args.precision)]
+    peak, peak_kind = read_peaks()
+    achieved = active * bpl / (mean_ms * 1e-3) / 1e9
+    traffic = read_traffic(f"step_kernel_c2_q{args.Q}_{args.precision}.txt")
+
+    # secondary: FP16-offset storage on the same lattice (the precision config's storage)
+    extra = {}
+    if args.precision == "f32" and not args.quick:
+        s16, _ = make_solver(capi, mask, surf, tri, args.Q, "f16", origin, local)
+        s16.step(args.warmup)
+        ms16 = time_steps(cr, s16, args.steps, flush, s16.stream())
+        m16 = sum(ms16) / len(ms16)
+        extra["f16_store"] = {"mlups": active / (m16 * 1e-3) / 1e6,
+                              "hbm_gbs": active * BYTES_PER_LU[(args.Q, "f16")] / (m16 * 1e-3) / 1e9,
+                              "ms_per_step": m16, "speedup_vs_f32": mean_ms / m16}
+        s16.close()
+
+    # end to end through the C ABI: per e2e step, H2D of a 100-step inlet
+    # table slice from pinned memory, 100 LBM steps (graph replay), D2H of
+    # the wall shear stress arrays and the rho/u field (the reference's
+    # output cadence, Simulation.cpp:589-591)
+    from pv_dec_original_gb300 import waveform
+    B = 100
+    table = waveform.sinusoid_table(U_MEAN, PERIOD, 4000)
+    amp_h, _ = pinned_array(cr, B, np.float64)
+    nnw = cnt["next_to_wall"]
+    wss_h = [pinned_array(cr, n, np.float64)[0] for n in (nnw, 3 * nnw, nnw, 3 * nnw, nnw, nnw, nnw)]
+    pt_h, _ = pinned_array(cr, nnw, np.int64)
+    rho_h, _ = pinned_array(cr, active, np.float64)
+    u_h, _ = pinned_array(cr, 3 * active, np.float64)
+    s.set_graph_steps(B)
+    L = capi.load()
+    P = lambda a: a.ctypes.data_as(C.c_void_p)
+    e2e_times = []
+    nb = max(2, min(5, args.steps // 10))
+    for it in range(nb + 1):
+        s0 = s.counts()["steps"]
+        t0 = time.perf_counter()
+        idx = np.arange(s0, s0 + B)
+        amp_h[idx % B] = table[idx % len(table)]  # step s reads amp[s % B]
+        capi._check(L.lbm_set_inlet_table(s.h, amp_h, B), s.h)
+        capi._check(L.lbm_step_async(s.h, B), s.h)
+        capi._check(L.lbm_get_wss(s.h, P(pt_h), P(wss_h[1]), P(wss_h[0]), P(wss_h[3]), P(wss_h[2]), P(wss_h[4]),
+                                  P(wss_h[5])), s.h)
+        capi._check(L.lbm_get_macro(s.h, P(rho_h), P(u_h)), s.h)
+        capi._check(L.lbm_check_status(s.h), s.h)
+        if it > 0:  # first batch captures the graph
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_t = max_over_ranks(dist, sum(e2e_times) / len(e2e_times), dev_t)
+    h2d = B * 8
+    d2h = nnw * 8 * (1 + 3 + 1 + 3 + 1 + 1 + 1) + active * 8 * 4
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            try:
+                cores = os.cpu_count() or 1
+                v, n, el, na = cpu_baseline(tri, mask, bb, planes, cores, seconds=args.cpu_seconds)
+                cpu = {"value": v, "unit": "MLUPS", "cores": cores, "kind": "port",
+                       "sample": f"{n} FP64 parity steps of the full 256x192x512 lattice ({na} active nodes), "
+                                 f"{el:.1f} s, OpenMP on {cores} host threads, normals not computed"}
+            except Exception as e:  # the baseline is reported, never required
+                cpu = {"value": None, "unit": "MLUPS", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+        out = {
+            "metric": "MLUPS (D3Q19 BGK lattice updates per second, active nodes)",
+            "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == "f32" else args.precision,
+            "data": "synthetic (seeded Y-bifurcation STL generated in-process)",
+            "config": {"workload": "Y-bifurcation 256x192x512, parent r=24, daughters r=17 at +/-30 deg, seed 0",
+                       "lattice": f"D3Q{args.Q}", "storage": args.precision, "tau": TAU,
+                       "inlet": "z-min Zou-He velocity, parabolic, u=0.03(1+0.5sin(2pi t/4000)+0.2sin(4pi t/4000))",
+                       "outlet": "z-max Zou-He density 1", "walls": "half-way bounce-back",
+                       "active_nodes": active, "lattice_points": cnt["points"],
+                       "boundary_list_nodes": cnt["special"], "next_to_wall": nnw,
+                       "l2": "flushed between timed steps (512 MB memset outside the events)",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "bytes_per_lu": bpl, "peak_source": peak_kind,
+                         "kernel": f"lbm::step_kernel<{args.Q}, {args.precision}, physics, step>"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": ws * active * B / e2e_t / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "step": f"{B} LBM steps per call batch + WSS/OSI/TAWSS and rho/u read-back (pinned host buffers)"},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "extra": extra,
+        }
+        print(json.dumps(out))
+    s.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def run_reference(args):
+    ws, rank, local, dist = dist_setup("gloo")
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return None
+    from oracle import oracle as O
+    O.build()
+    from pv_dec_original_gb300 import geometry as G
+    surf, tri = c2_workload()
+    mask, bb, d = O.voxelize(tri, 1.0, culled=True)
+    fl = np.argwhere(mask > 0)
+    planes = (int(fl[:, 0].min()), int(fl[:, 0].max()))
+    cores = os.cpu_count() or 1
+    per = []
+    na = 0
+    for _ in range(args.warmup):
+        cpu_baseline(tri, mask, bb, planes, cores, seconds=0.5)
+    total_n, total_t = 0, 0.0
+    for _ in range(max(1, min(args.steps, 3))):
+        v, n, el, na = cpu_baseline(tri, mask, bb, planes, cores, seconds=args.cpu_seconds / 3)
+        per.append(v)
+        total_n += n
+        total_t += el
+    value = na * total_n / total_t / 1e6
+    out = {
+        "impl": "reference", "metric": "MLUPS (D3Q19 BGK lattice updates per second, active nodes)",
+        "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": total_n, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_t / total_n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Y-bifurcation STL generated in-process)",
+        "config": {"workload": "Y-bifurcation 256x192x512, parent r=24, daughters r=17 at +/-30 deg, seed 0",
+                   "lattice": "D3Q19", "storage": "f64", "tau": TAU, "active_nodes": na,
+                   "implementation": "reference algorithm restated in C (oracle/lbm_oracle.c), parity semantics"},
+        "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port",
+                         "sample": f"{total_n} full-lattice FP64 steps in {total_t:.1f} s on {cores} threads"},
+        "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="f32", choices=["f32", "f16", "bf16", "f64"])
+    ap.add_argument("--Q", type=int, default=19, choices=[19, 27])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the secondary FP16 measurement")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,292 @@
+"""ctypes binding of liblbm_gb300.so (the C ABI in include/lbm_gb300.h).
+
+This is the same boundary a C, C++, Go or Java caller binds.  Loading fails
+loudly when the library has not been built: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LBM_D3Q19, LBM_D3Q27 = 19, 27
+LBM_F64, LBM_F32, LBM_F16, LBM_BF16 = 0, 1, 2, 3
+LBM_PARITY, LBM_PHYSICS = 0, 1
+LBM_BC_REF_INLET, LBM_BC_REF_OUTLET_YMAX, LBM_BC_REF_OUTLET_ZMIN, LBM_BC_VELOCITY, LBM_BC_PRESSURE = 1, 2, 3, 4, 5
+FACES = {"x-": 0, "x+": 1, "y-": 2, "y+": 3, "z-": 4, "z+": 5}
+PRECISIONS = {"f64": LBM_F64, "f32": LBM_F32, "f16": LBM_F16, "bf16": LBM_BF16}
+MAX_BC = 8
+
+ERRORS = {-1: "LBM_ERR_ARG", -2: "LBM_ERR_CUDA", -3: "LBM_ERR_STATE", -4: "LBM_ERR_NONFINITE",
+          -5: "LBM_ERR_ALLOC", -6: "LBM_ERR_IO", -7: "LBM_ERR_UNSUPPORTED"}
+
+
+class LbmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class VoxDesc(C.Structure):
+    _fields_ = [("spacing", C.c_double), ("reference_bbox", C.c_int), ("bbox", C.c_double * 6),
+                ("origin", C.c_double * 3), ("dims", C.c_int * 3), ("fluid_count", C.c_int64),
+                ("ray_tests", C.c_int64)]
+
+
+class Desc(C.Structure):
+    _fields_ = [("Q", C.c_int), ("precision", C.c_int), ("mode", C.c_int), ("tau", C.c_double),
+                ("spacing", C.c_double), ("origin", C.c_double * 3), ("wss_scale", C.c_double),
+                ("tawss_div", C.c_double), ("device", C.c_int)]
+
+
+class BCSpec(C.Structure):
+    _fields_ = [("kind", C.c_int), ("face", C.c_int), ("plane", C.c_int), ("value", C.c_double),
+                ("profile", C.c_int), ("c1", C.c_double), ("c2", C.c_double), ("R", C.c_double)]
+
+
+class Counts(C.Structure):
+    _fields_ = [("points", C.c_int64), ("active", C.c_int64), ("fluid", C.c_int64), ("wall", C.c_int64),
+                ("bc", C.c_int64 * MAX_BC), ("next_to_wall", C.c_int64), ("special", C.c_int64),
+                ("segments", C.c_int64), ("steps", C.c_int64), ("device_bytes", C.c_int64)]
+
+
+_lib = None
+EXPORTS = [
+    "lbm_voxelize", "lbm_read_stl_ascii", "lbm_create", "lbm_destroy", "lbm_last_error", "lbm_last_global_error",
+    "lbm_set_geometry", "lbm_set_normals_from_surface", "lbm_set_inlet_table", "lbm_init_equilibrium",
+    "lbm_init_from_macro", "lbm_step", "lbm_step_async", "lbm_check_status", "lbm_sync", "lbm_get_counts", "lbm_get_classes", "lbm_get_distributions",
+    "lbm_set_distributions", "lbm_get_macro", "lbm_get_wss", "lbm_get_conservation", "lbm_save", "lbm_load",
+    "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps",
+]
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load liblbm_gb300.so (building it in-tree when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise LbmError(-7, f"{path} is not built (run pv_dec_original_gb300.build)")
+        _build.build()
+    L = C.CDLL(path)
+    P = C.c_void_p
+    dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    u8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+    i64 = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+    L.lbm_voxelize.argtypes = [P, C.c_int64, C.POINTER(VoxDesc), P]
+    L.lbm_read_stl_ascii.argtypes = [C.c_char_p, P, C.POINTER(C.c_int64)]
+    L.lbm_create.argtypes = [C.POINTER(Desc), C.POINTER(P)]
+    L.lbm_destroy.argtypes = [P]
+    L.lbm_last_error.argtypes = [P]
+    L.lbm_last_error.restype = C.c_char_p
+    L.lbm_last_global_error.restype = C.c_char_p
+    L.lbm_set_geometry.argtypes = [P, u8, C.POINTER(C.c_int), C.POINTER(BCSpec), C.c_int]
+    L.lbm_set_normals_from_surface.argtypes = [P, dp, C.c_int64]
+    L.lbm_set_inlet_table.argtypes = [P, dp, C.c_int64]
+    L.lbm_init_equilibrium.argtypes = [P]
+    L.lbm_init_from_macro.argtypes = [P, fp, fp, C.c_int]
+    L.lbm_step.argtypes = [P, C.c_int]
+    L.lbm_step_async.argtypes = [P, C.c_int]
+    L.lbm_check_status.argtypes = [P]
+    L.lbm_sync.argtypes = [P]
+    L.lbm_get_counts.argtypes = [P, C.POINTER(Counts)]
+    L.lbm_get_classes.argtypes = [P, u8]
+    L.lbm_get_distributions.argtypes = [P, dp]
+    L.lbm_set_distributions.argtypes = [P, dp]
+    L.lbm_get_macro.argtypes = [P, P, P]
+    L.lbm_get_wss.argtypes = [P, P, P, P, P, P, P, P]
+    L.lbm_get_conservation.argtypes = [P, P, P, P]
+    L.lbm_save.argtypes = [P, C.c_char_p]
+    L.lbm_load.argtypes = [P, C.c_char_p]
+    L.lbm_get_stream.argtypes = [P, C.POINTER(P)]
+    L.lbm_get_launch_count.argtypes = [P, C.POINTER(C.c_int64)]
+    L.lbm_set_graph_steps.argtypes = [P, C.c_int]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _check(rc, h=None):
+    if rc != 0:
+        L = load()
+        msg = (L.lbm_last_error(h) if h else L.lbm_last_global_error()) or b""
+        raise LbmError(rc, msg.decode(errors="replace"))
+
+
+def read_stl(path: str) -> np.ndarray:
+    L = load()
+    n = C.c_int64(0)
+    _check(L.lbm_read_stl_ascii(path.encode(), None, C.byref(n)))
+    out = np.zeros((n.value, 12), np.float64)
+    _check(L.lbm_read_stl_ascii(path.encode(), _ptr(out), C.byref(n)))
+    return out
+
+
+def voxelize(tri12, spacing, bbox=None, origin=None, dims=None):
+    """GPU voxelization; returns (mask[k, j, i] uint8, desc).  Without bbox /
+    origin / dims the reference's bounding-box rule is used."""
+    L = load()
+    tri = np.ascontiguousarray(tri12, np.float64)
+    d = VoxDesc()
+    d.spacing = spacing
+    if bbox is None:
+        d.reference_bbox = 1
+    else:
+        d.reference_bbox = 0
+        d.bbox[:] = list(bbox)
+        d.origin[:] = list(origin)
+        d.dims[:] = list(dims)
+    _check(L.lbm_voxelize(_ptr(tri), len(tri), C.byref(d), None))
+    nx, ny, nz = d.dims
+    mask = np.zeros(nx * ny * nz, np.uint8)
+    _check(L.lbm_voxelize(_ptr(tri), len(tri), C.byref(d), _ptr(mask)))
+    return mask.reshape(nz, ny, nx), d
+
+
+def bc_spec(kind, face=0, plane=-1, value=1.0, profile=0, c1=0.0, c2=0.0, R=1.0):
+    if isinstance(face, str):
+        face = FACES[face]
+    return BCSpec(kind, face, plane, value, profile, c1, c2, R)
+
+
+class Solver:
+    """One device-resident lattice behind the C ABI."""
+
+    def __init__(self, Q=19, precision=LBM_F32, mode=LBM_PHYSICS, tau=0.8, spacing=1.0, origin=(0.0, 0.0, 0.0),
+                 wss_scale=1.0, tawss_div=0.9, device=0):
+        L = load()
+        if isinstance(precision, str):
+            precision = PRECISIONS[precision]
+        d = Desc(Q, precision, mode, tau, spacing, (C.c_double * 3)(*origin), wss_scale, tawss_div, device)
+        h = C.c_void_p()
+        _check(L.lbm_create(C.byref(d), C.byref(h)))
+        self.h = h
+        self.Q = Q
+        self.precision = precision
+        self.mode = mode
+        self.dims = None
+        self.nbc = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lbm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, rc):
+        _check(rc, self.h)
+
+    def set_geometry(self, mask, bcs=()):
+        L = load()
+        nz, ny, nx = mask.shape
+        self.dims = (nx, ny, nz)
+        arr = (BCSpec * max(1, len(bcs)))(*bcs)
+        self.nbc = len(bcs)
+        m = np.ascontiguousarray(mask.reshape(-1), np.uint8)
+        self._c(L.lbm_set_geometry(self.h, m, (C.c_int * 3)(nx, ny, nz), arr, len(bcs)))
+
+    def set_normals(self, tri12):
+        t = np.ascontiguousarray(tri12, np.float64)
+        self._c(load().lbm_set_normals_from_surface(self.h, t, len(t)))
+
+    def set_inlet_table(self, amp):
+        a = np.ascontiguousarray(np.atleast_1d(amp), np.float64)
+        self._c(load().lbm_set_inlet_table(self.h, a, len(a)))
+
+    def init_equilibrium(self):
+        self._c(load().lbm_init_equilibrium(self.h))
+
+    def init_from_macro(self, rho, u, regularized=True):
+        self._c(load().lbm_init_from_macro(self.h, np.ascontiguousarray(rho, np.float32),
+                                           np.ascontiguousarray(u, np.float32).reshape(-1), int(regularized)))
+
+    def step(self, n=1):
+        self._c(load().lbm_step(self.h, int(n)))
+
+    def step_async(self, n=1):
+        self._c(load().lbm_step_async(self.h, int(n)))
+
+    def check_status(self):
+        self._c(load().lbm_check_status(self.h))
+
+    def sync(self):
+        self._c(load().lbm_sync(self.h))
+
+    def set_graph_steps(self, n):
+        self._c(load().lbm_set_graph_steps(self.h, int(n)))
+
+    def counts(self) -> dict:
+        c = Counts()
+        self._c(load().lbm_get_counts(self.h, C.byref(c)))
+        d = {k: getattr(c, k) for k, _ in Counts._fields_ if k != "bc"}
+        d["bc"] = list(c.bc)[: self.nbc]
+        return d
+
+    def classes(self):
+        nx, ny, nz = self.dims
+        out = np.zeros(nx * ny * nz, np.uint8)
+        self._c(load().lbm_get_classes(self.h, out))
+        return out.reshape(nz, ny, nx)
+
+    def distributions(self):
+        out = np.zeros(self.counts()["active"] * self.Q, np.float64)
+        self._c(load().lbm_get_distributions(self.h, out))
+        return out.reshape(-1, self.Q)
+
+    def set_distributions(self, f):
+        self._c(load().lbm_set_distributions(self.h, np.ascontiguousarray(f, np.float64).reshape(-1)))
+
+    def macro(self):
+        n = self.counts()["active"]
+        rho, u = np.zeros(n), np.zeros(3 * n)
+        self._c(load().lbm_get_macro(self.h, _ptr(rho), _ptr(u)))
+        return rho, u.reshape(-1, 3)
+
+    def wss(self) -> dict:
+        n = self.counts()["next_to_wall"]
+        pt = np.zeros(n, np.int64)
+        nrm, w, acc, accm, osi, tawss = (np.zeros(3 * n), np.zeros(n), np.zeros(3 * n), np.zeros(n), np.zeros(n),
+                                         np.zeros(n))
+        self._c(load().lbm_get_wss(self.h, _ptr(pt), _ptr(nrm), _ptr(w), _ptr(acc), _ptr(accm), _ptr(osi),
+                                   _ptr(tawss)))
+        return {"pt": pt, "normal": nrm.reshape(-1, 3), "wss": w, "acc": acc.reshape(-1, 3), "acc_mag": accm,
+                "osi": osi, "tawss": tawss}
+
+    def conservation(self):
+        m, p, fl = np.zeros(1), np.zeros(3), np.zeros(MAX_BC)
+        self._c(load().lbm_get_conservation(self.h, _ptr(m), _ptr(p), _ptr(fl)))
+        return float(m[0]), p, fl[: self.nbc]
+
+    def save(self, path):
+        self._c(load().lbm_save(self.h, path.encode()))
+
+    def load_checkpoint(self, path):
+        self._c(load().lbm_load(self.h, path.encode()))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._c(load().lbm_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def launches(self) -> int:
+        n = C.c_int64()
+        self._c(load().lbm_get_launch_count(self.h, C.byref(n)))
+        return n.value

@@ -1,0 +1,873 @@
+// C ABI of liblbm_gb300.so (declared in include/lbm_gb300.h).
+//
+// A handle owns one device-resident lattice: the two population buffers
+// (ping-pong, structure of arrays), the class bytes, the compact boundary
+// list with its per-link masks, the next-to-wall accumulators and one CUDA
+// stream.  A step is one fused launch (step_kernels.cuh); batches of steps
+// can be replayed from a captured CUDA graph.  Host memory is only touched by
+// the explicit copy-in / read-out calls.
+//
+// State model.  A "start" (f = w, warm start, set_distributions or a loaded
+// checkpoint) writes f^N at each point's own index into buf[0] and runs the
+// prologue launch, which collides it into buf[1] (cur = 1).  Each step reads
+// buf[cur] and writes buf[1-cur].  A read-out pulls from buf[1-cur] -- the
+// previous step's populations -- and applies the boundary rules again, or
+// reads buf[0] directly if no step ran since the start.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "lbm_internal.cuh"
+#include "setup.cuh"
+
+using namespace lbm;
+
+struct lbm_handle {
+    lbm_desc d{};
+    cudaStream_t st = nullptr;
+    std::string err;
+    int nx = 0, ny = 0, nz = 0;
+    int64_t npts = 0, stride = 0;
+    GeometryLists g;
+    bool has_geo = false;
+    bool has_state = false;
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    void* stale = nullptr;
+    void* nw_prev = nullptr;
+    double *nw_n = nullptr, *nw_wss = nullptr, *nw_acc = nullptr, *nw_accm = nullptr;
+    double* amp = nullptr;
+    int64_t namp = 0;
+    std::vector<double> amp_host;
+    int64_t* slots = nullptr;   // step counter, two slots (even / odd launches)
+    int64_t steps = 0;          // steps taken
+    int64_t since_start = 0;    // steps since the last start
+    unsigned* flags = nullptr;
+    BCDev bc[LBM_MAX_BC]{};
+    int nbc = 0;
+    int64_t launches = 0;
+    int bulk_blocks = 0;
+    int64_t nblocks = 0;
+    double* partials = nullptr;
+    double* sums = nullptr;
+    double* out_f = nullptr;    // read-out scratch, allocated on first use
+    double* macro = nullptr;    // rho / u read-out scratch
+    int graph_steps = 0;
+    cudaGraphExec_t gexec = nullptr;
+    int gexec_parity = -1;
+    int gexec_cur = -1;
+    size_t geo_bytes = 0;
+    lbm_counts counts{};
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+const char* code_name(int code) {
+    switch (code) {
+        case LBM_ERR_ARG: return "invalid argument";
+        case LBM_ERR_CUDA: return "CUDA error";
+        case LBM_ERR_STATE: return "bad call order";
+        case LBM_ERR_NONFINITE: return "non-finite state";
+        case LBM_ERR_ALLOC: return "allocation failed";
+        case LBM_ERR_IO: return "I/O error";
+        case LBM_ERR_UNSUPPORTED: return "unsupported";
+        default: return "error";
+    }
+}
+
+int fail(lbm_handle* h, int code, const std::string& msg) {
+    std::string m = std::string(code_name(code)) + ": " + msg;
+    if (h) h->err = m;
+    else g_err = m;
+    return code;
+}
+
+#define CK(h, call)                                                                          \
+    do {                                                                                     \
+        cudaError_t _e = (call);                                                             \
+        if (_e != cudaSuccess)                                                               \
+            return fail(h, _e == cudaErrorMemoryAllocation ? LBM_ERR_ALLOC : LBM_ERR_CUDA,   \
+                        std::string(#call) + ": " + cudaGetErrorString(_e));                 \
+    } while (0)
+
+#define REQUIRE(h, cond, code, msg) \
+    do {                            \
+        if (!(cond)) return fail(h, code, msg); \
+    } while (0)
+
+int elem_size(int precision) {
+    switch (precision) {
+        case LBM_F64: return 8;
+        case LBM_F32: return 4;
+        case LBM_F16:
+        case LBM_BF16: return 2;
+        default: return 0;
+    }
+}
+
+size_t real_size(int precision) { return precision == LBM_F64 ? 8 : 4; }
+
+template <typename T>
+cudaError_t dalloc(lbm_handle* h, T** p, size_t bytes) {
+    bytes = bytes ? bytes : 16;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), bytes);
+    if (e == cudaSuccess) h->geo_bytes += bytes;
+    return e;
+}
+
+void drop_graph(lbm_handle* h) {
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+    h->gexec_parity = -1;
+}
+
+void free_geometry(lbm_handle* h) {
+    GeometryLists& g = h->g;
+    void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_prof, g.nw_pt, g.seg, g.act_idx, g.act_pt,
+                    h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
+                    h->partials, h->sums, h->out_f, h->macro};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    g = GeometryLists();
+    h->buf[0] = h->buf[1] = h->stale = h->nw_prev = nullptr;
+    h->nw_n = h->nw_wss = h->nw_acc = h->nw_accm = h->partials = h->sums = h->out_f = h->macro = nullptr;
+    drop_graph(h);
+    h->has_geo = h->has_state = false;
+    h->geo_bytes = 0;
+}
+
+StepParams make_params(lbm_handle* h, int kind) {
+    StepParams p{};
+    const int parity = (int)(h->steps & 1);
+    if (kind == 0) {
+        p.fin = h->buf[h->cur];
+        p.fout = h->buf[1 - h->cur];
+    } else if (kind == 1) {
+        p.fin = h->buf[0];
+        p.fout = h->buf[1];
+    } else {
+        p.fin = h->since_start == 0 ? h->buf[0] : h->buf[1 - h->cur];
+        p.direct = h->since_start == 0 ? 1 : 0;
+    }
+    p.stride = h->stride;
+    p.nx = h->nx;
+    p.ny = h->ny;
+    p.nxy = (int64_t)h->nx * h->ny;
+    p.cls = h->g.cls;
+    p.seg = h->g.seg;
+    p.nseg = h->g.nseg;
+    p.bulk_blocks = h->bulk_blocks;
+    p.nsp = h->g.nsp;
+    p.sp_pt = h->g.sp_pt;
+    p.sp_miss = h->g.sp_miss;
+    p.sp_cls = h->g.sp_cls;
+    p.sp_nw = h->g.sp_nw;
+    p.sp_prof = h->g.sp_prof;
+    p.stale = h->stale;
+    p.nnw = h->g.nnw;
+    p.nw_n = h->nw_n;
+    p.nw_wss = h->nw_wss;
+    p.nw_acc = h->nw_acc;
+    p.nw_accm = h->nw_accm;
+    p.nw_prev = h->nw_prev;
+    p.tau = h->d.tau;
+    p.wss_C = h->d.wss_scale;
+    p.amp = h->amp;
+    p.namp = h->namp;
+    p.step_base = h->slots + parity;
+    p.step_next = h->slots + (1 - parity);
+    p.step_off = kind == 2 ? -1 : 0;
+    for (int b = 0; b < LBM_MAX_BC; ++b) p.bc[b] = h->bc[b];
+    p.nbc = h->nbc;
+    p.flags = h->flags;
+    p.act_idx = h->g.act_idx;
+    p.partials = h->partials;
+    return p;
+}
+
+cudaError_t launch(lbm_handle* h, int kind, const StepParams& p) {
+    h->launches++;
+    if (h->d.precision == LBM_F64) return launch_step_f64(h->d.Q, h->d.mode, kind, p, h->st);
+    return launch_step_fast(h->d.Q, h->d.precision, h->d.mode, kind, p, h->st);
+}
+
+// buf[0] holds f^N at each point's own index: collide it into buf[1].
+int start_state(lbm_handle* h, bool reset) {
+    if (reset) {
+        CK(h, cudaMemsetAsync(h->nw_acc, 0, sizeof(double) * 3 * (h->g.nnw + 1), h->st));
+        CK(h, cudaMemsetAsync(h->nw_accm, 0, sizeof(double) * (h->g.nnw + 1), h->st));
+        CK(h, cudaMemsetAsync(h->nw_wss, 0, sizeof(double) * (h->g.nnw + 1), h->st));
+        h->steps = 0;
+    }
+    int64_t sl[2] = {h->steps, h->steps};
+    CK(h, cudaMemcpyAsync(h->slots, sl, sizeof(sl), cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaMemsetAsync(h->flags, 0, sizeof(unsigned), h->st));
+    StepParams p = make_params(h, 1);
+    CK(h, launch(h, 1, p));
+    h->cur = 1;
+    h->since_start = 0;
+    drop_graph(h);  // the graph's buffer roles depend on cur
+    CK(h, cudaStreamSynchronize(h->st));
+    h->has_state = true;
+    return LBM_OK;
+}
+
+int check_flags(lbm_handle* h) {
+    unsigned f = 0;
+    CK(h, cudaMemcpyAsync(&f, h->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    if (f & FLAG_NONFINITE)
+        return fail(h, LBM_ERR_NONFINITE, "a density became NaN/Inf: the run diverged (check tau and the inlet)");
+    return LBM_OK;
+}
+
+int one_step(lbm_handle* h) {
+    StepParams p = make_params(h, 0);
+    CK(h, launch(h, 0, p));
+    h->cur = 1 - h->cur;
+    h->steps++;
+    h->since_start++;
+    return LBM_OK;
+}
+
+// Capture graph_steps (even) launches starting at the current parity.
+int build_graph(lbm_handle* h) {
+    drop_graph(h);
+    const int64_t steps0 = h->steps, since0 = h->since_start, launches0 = h->launches;
+    const int cur0 = h->cur;
+    cudaGraph_t graph = nullptr;
+    CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < h->graph_steps; ++k) {
+        StepParams p = make_params(h, 0);
+        cudaError_t e = launch(h, 0, p);
+        if (e != cudaSuccess) {
+            cudaStreamEndCapture(h->st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            return fail(h, LBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        }
+        h->cur = 1 - h->cur;
+        h->steps++;
+    }
+    CK(h, cudaStreamEndCapture(h->st, &graph));
+    cudaError_t e = cudaGraphInstantiate(&h->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    h->steps = steps0;
+    h->since_start = since0;
+    h->cur = cur0;
+    h->launches = launches0;
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    h->gexec_parity = (int)(steps0 & 1);
+    h->gexec_cur = cur0;
+    return LBM_OK;
+}
+
+// Read-out launch: post-boundary f (optional FP64 copy) + per-block sums.
+int readout(lbm_handle* h, bool want_f) {
+    REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state: call lbm_init_equilibrium / lbm_set_geometry first");
+    if (want_f && !h->out_f) CK(h, dalloc(h, &h->out_f, sizeof(double) * h->g.nact * h->d.Q));
+    StepParams p = make_params(h, 2);
+    p.out_f = want_f ? h->out_f : nullptr;
+    CK(h, launch(h, 2, p));
+    CK(h, reduce_partials(h->partials, h->nblocks, h->sums, h->st));
+    return LBM_OK;
+}
+
+bool read_stl(const char* path, std::vector<double>& out) {
+    std::FILE* fp = std::fopen(path, "r");
+    if (!fp) return false;
+    std::vector<std::string> lines;
+    {
+        std::string cur;
+        char buf[4096];
+        while (std::fgets(buf, sizeof(buf), fp)) {
+            cur += buf;
+            if (!cur.empty() && cur.back() == '\n') {
+                cur.pop_back();
+                lines.push_back(cur);
+                cur.clear();
+            }
+        }
+        if (!cur.empty()) lines.push_back(cur);
+    }
+    std::fclose(fp);
+    auto tok = [](const std::string& s) {
+        std::vector<std::string> t;
+        size_t i = 0;
+        while (i < s.size()) {
+            while (i < s.size() && (s[i] == ' ' || s[i] == '\t' || s[i] == '\r')) ++i;
+            size_t j = i;
+            while (j < s.size() && s[j] != ' ' && s[j] != '\t' && s[j] != '\r') ++j;
+            if (j > i) t.push_back(s.substr(i, j - i));
+            i = j;
+        }
+        return t;
+    };
+    auto num = [](const std::string& s, double& v) {
+        char* end = nullptr;
+        v = std::strtod(s.c_str(), &end);
+        return end && *end == '\0' && end != s.c_str();
+    };
+    // facet normal / outer loop / 3 vertex / endloop / endfacet, in order
+    // (GeometryReader.cpp:50-110); a malformed facet is skipped
+    size_t i = 0, n = lines.size();
+    while (i < n) {
+        auto t = tok(lines[i++]);
+        double nn[3];
+        if (t.size() < 5 || t[0] != "facet" || t[1] != "normal" || !num(t[2], nn[0]) || !num(t[3], nn[1]) ||
+            !num(t[4], nn[2]))
+            continue;
+        if (i >= n) break;
+        t = tok(lines[i++]);
+        if (t.size() < 2 || t[0] != "outer" || t[1] != "loop") continue;
+        double v[9];
+        int got = 0;
+        for (int k = 0; k < 3 && i < n; ++k) {
+            t = tok(lines[i++]);
+            if (t.size() < 4 || t[0] != "vertex" || !num(t[1], v[3 * k]) || !num(t[2], v[3 * k + 1]) ||
+                !num(t[3], v[3 * k + 2]))
+                break;
+            ++got;
+        }
+        if (got < 3 || i >= n) continue;
+        t = tok(lines[i++]);
+        if (t.empty() || t[0] != "endloop" || i >= n) continue;
+        t = tok(lines[i++]);
+        if (t.empty() || t[0] != "endfacet") continue;
+        out.insert(out.end(), v, v + 9);
+        out.insert(out.end(), nn, nn + 3);
+    }
+    return true;
+}
+
+void reference_bbox(const double* t, int64_t ntri, double spacing, double* bb, int* dims) {
+    double mnx = INFINITY, mny = INFINITY, mnz = INFINITY, mxx = -INFINITY, mxy = -INFINITY, mxz = -INFINITY;
+    for (int64_t k = 0; k < ntri; ++k) {
+        const double* r = t + 12 * k;
+        // the y and z extremes ignore the third vertex (ComplexGeometry.cpp:147-151)
+        mnx = std::min(std::min(std::min(mnx, r[0]), r[3]), r[6]);
+        mny = std::min(std::min(mny, r[1]), r[4]);
+        mnz = std::min(std::min(mnz, r[2]), r[5]);
+        mxx = std::max(std::max(std::max(mxx, r[0]), r[3]), r[6]);
+        mxy = std::max(std::max(mxy, r[1]), r[4]);
+        mxz = std::max(std::max(mxz, r[2]), r[5]);
+    }
+    bb[0] = mnx; bb[1] = mxx; bb[2] = mny; bb[3] = mxy; bb[4] = mnz; bb[5] = mxz;
+    dims[0] = (int)std::ceil((mxx - mnx) / spacing) + 1;
+    dims[1] = (int)std::ceil((mxy - mny) / spacing) + 1;
+    dims[2] = (int)std::ceil((mxz - mnz) / spacing);
+}
+
+const uint32_t kCkptMagic = 0x4c424d43;  // "CMBL"
+const uint32_t kCkptVersion = 1;
+
+}  // namespace
+
+// ===========================================================================
+
+extern "C" {
+
+const char* lbm_last_global_error(void) { return g_err.c_str(); }
+
+const char* lbm_last_error(const lbm_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+lbm_status lbm_read_stl_ascii(const char* path, double* tri12, int64_t* ntri) {
+    if (!path || !ntri) return fail(nullptr, LBM_ERR_ARG, "null path or count");
+    std::vector<double> v;
+    if (!read_stl(path, v)) return fail(nullptr, LBM_ERR_IO, std::string("cannot open ") + path);
+    const int64_t n = (int64_t)(v.size() / 12);
+    if (tri12) {
+        const int64_t m = std::min(n, *ntri);
+        std::memcpy(tri12, v.data(), sizeof(double) * 12 * m);
+    }
+    *ntri = n;
+    return LBM_OK;
+}
+
+lbm_status lbm_voxelize(const double* tri12, int64_t ntri, lbm_vox_desc* desc, uint8_t* mask_out) {
+    if (!desc || (ntri > 0 && !tri12) || ntri < 0) return fail(nullptr, LBM_ERR_ARG, "null descriptor or triangles");
+    if (!(desc->spacing > 0)) return fail(nullptr, LBM_ERR_ARG, "spacing must be > 0");
+    if (desc->reference_bbox) {
+        if (ntri == 0) return fail(nullptr, LBM_ERR_ARG, "the reference bbox needs at least one triangle");
+        reference_bbox(tri12, ntri, desc->spacing, desc->bbox, desc->dims);
+        desc->origin[0] = desc->bbox[0];
+        desc->origin[1] = desc->bbox[2];
+        desc->origin[2] = desc->bbox[4];
+    }
+    const int nx = desc->dims[0], ny = desc->dims[1], nz = desc->dims[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0) return fail(nullptr, LBM_ERR_ARG, "empty lattice");
+    if (!mask_out) return LBM_OK;
+    const int64_t npts = (int64_t)nx * ny * nz;
+    cudaStream_t st = nullptr;
+    double* d_tri = nullptr;
+    uint8_t* d_mask = nullptr;
+    std::string err;
+    auto cleanup = [&]() {
+        if (d_tri) cudaFree(d_tri);
+        if (d_mask) cudaFree(d_mask);
+        if (st) cudaStreamDestroy(st);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&d_tri, sizeof(double) * 12 * (ntri > 0 ? ntri : 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_mask, npts);
+    if (e == cudaSuccess && ntri > 0)
+        e = cudaMemcpyAsync(d_tri, tri12, sizeof(double) * 12 * ntri, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_mask, 0, npts, st);
+    VoxResult res{};
+    if (e == cudaSuccess) {
+        e = voxelize_device(d_tri, ntri, desc->bbox, desc->origin, desc->spacing, desc->dims, d_mask, &res, st, &err);
+    } else {
+        err = cudaGetErrorString(e);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mask_out, d_mask, npts, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cleanup();
+    if (e != cudaSuccess)
+        return fail(nullptr, e == cudaErrorMemoryAllocation ? LBM_ERR_ALLOC : LBM_ERR_CUDA,
+                    "voxelize: " + (err.empty() ? std::string(cudaGetErrorString(e)) : err));
+    desc->fluid_count = res.fluid;
+    desc->ray_tests = res.tests;
+    return LBM_OK;
+}
+
+lbm_status lbm_create(const lbm_desc* desc, lbm_handle** out) {
+    if (!desc || !out) return fail(nullptr, LBM_ERR_ARG, "null descriptor or output");
+    if (desc->Q != 19 && desc->Q != 27) return fail(nullptr, LBM_ERR_ARG, "Q must be 19 or 27");
+    if (elem_size(desc->precision) == 0) return fail(nullptr, LBM_ERR_ARG, "unknown precision");
+    if (desc->mode != LBM_PARITY && desc->mode != LBM_PHYSICS) return fail(nullptr, LBM_ERR_ARG, "unknown mode");
+    if (!(desc->tau > 0.5)) return fail(nullptr, LBM_ERR_ARG, "tau must be > 0.5 (BGK stability)");
+    if (!(desc->spacing > 0)) return fail(nullptr, LBM_ERR_ARG, "spacing must be > 0");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, LBM_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (desc->device < 0 || desc->device >= ndev) return fail(nullptr, LBM_ERR_ARG, "device ordinal out of range");
+    lbm_handle* h = new lbm_handle();
+    h->d = *desc;
+    if (h->d.tawss_div == 0.0) h->d.tawss_div = 0.9;
+    e = cudaSetDevice(desc->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&h->slots, 2 * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&h->flags, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&h->amp, sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(h->amp, 0, sizeof(double));
+    if (e != cudaSuccess) {
+        int rc = fail(nullptr, LBM_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
+        lbm_destroy(h);
+        return rc;
+    }
+    h->namp = 1;
+    h->amp_host.assign(1, 0.0);
+    *out = h;
+    return LBM_OK;
+}
+
+lbm_status lbm_destroy(lbm_handle* h) {
+    if (!h) return LBM_OK;
+    cudaSetDevice(h->d.device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    free_geometry(h);
+    if (h->slots) cudaFree(h->slots);
+    if (h->flags) cudaFree(h->flags);
+    if (h->amp) cudaFree(h->amp);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3], const lbm_bc_spec* bc, int nbc) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, mask && dims, LBM_ERR_ARG, "null mask or dims");
+    REQUIRE(h, dims[0] > 0 && dims[1] > 0 && dims[2] > 0, LBM_ERR_ARG, "empty lattice");
+    REQUIRE(h, nbc >= 0 && nbc <= LBM_MAX_BC && (nbc == 0 || bc), LBM_ERR_ARG, "0..8 boundary conditions");
+    const int64_t npts = (int64_t)dims[0] * dims[1] * dims[2];
+    REQUIRE(h, npts < (int64_t)1 << 36, LBM_ERR_ARG, "lattice too large");
+    for (int b = 0; b < nbc; ++b) {
+        REQUIRE(h, bc[b].kind >= LBM_BC_REF_INLET && bc[b].kind <= LBM_BC_PRESSURE, LBM_ERR_ARG, "unknown bc kind");
+        REQUIRE(h, bc[b].face >= 0 && bc[b].face <= 5, LBM_ERR_ARG, "face must be 0..5");
+        REQUIRE(h, bc[b].kind != LBM_BC_PRESSURE || bc[b].value > 0, LBM_ERR_ARG, "pressure bc needs density > 0");
+        REQUIRE(h, bc[b].profile == 0 || bc[b].R > 0, LBM_ERR_ARG, "profile radius must be > 0");
+    }
+    CK(h, cudaSetDevice(h->d.device));
+    CK(h, cudaStreamSynchronize(h->st));
+    free_geometry(h);
+    h->nx = dims[0]; h->ny = dims[1]; h->nz = dims[2];
+    h->npts = npts;
+    h->stride = ceil_div(npts, 128) * 128;
+    uint8_t* d_mask = nullptr;
+    CK(h, cudaMalloc(&d_mask, npts));
+    cudaError_t e = cudaMemcpyAsync(d_mask, mask, npts, cudaMemcpyHostToDevice, h->st);
+    std::string err;
+    if (e == cudaSuccess)
+        e = build_geometry(h->d.Q, d_mask, h->nx, h->ny, h->nz, bc, nbc, h->d.origin, h->d.spacing, h->g, h->st, err);
+    cudaFree(d_mask);
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, "set_geometry: " + (err.empty() ? cudaGetErrorString(e) : err));
+    REQUIRE(h, h->g.nact < (int64_t)1 << 31, LBM_ERR_ARG, "too many active nodes");
+    h->nbc = nbc;
+    for (int b = 0; b < LBM_MAX_BC; ++b) {
+        h->bc[b] = BCDev{};
+        if (b < nbc) {
+            h->bc[b].kind = bc[b].kind;
+            h->bc[b].face = bc[b].face;
+            h->bc[b].value = bc[b].value;
+            h->bc[b].profile = bc[b].profile;
+            h->bc[b].c1 = bc[b].c1;
+            h->bc[b].c2 = bc[b].c2;
+            h->bc[b].R = bc[b].R;
+        }
+    }
+    const int Q = h->d.Q;
+    const size_t es = elem_size(h->d.precision), rs = real_size(h->d.precision);
+    CK(h, dalloc(h, &h->buf[0], es * Q * h->stride));
+    CK(h, dalloc(h, &h->buf[1], es * Q * h->stride));
+    CK(h, cudaMemsetAsync(h->buf[0], 0, es * Q * h->stride, h->st));
+    CK(h, cudaMemsetAsync(h->buf[1], 0, es * Q * h->stride, h->st));
+    if (h->d.mode == LBM_PARITY) {
+        CK(h, dalloc(h, &h->stale, rs * Q * (h->g.nsp + 1)));
+        CK(h, dalloc(h, &h->nw_prev, rs * 4 * (h->g.nnw + 1)));
+    }
+    CK(h, dalloc(h, &h->nw_n, sizeof(double) * 3 * (h->g.nnw + 1)));
+    CK(h, cudaMemsetAsync(h->nw_n, 0, sizeof(double) * 3 * (h->g.nnw + 1), h->st));
+    CK(h, dalloc(h, &h->nw_wss, sizeof(double) * (h->g.nnw + 1)));
+    CK(h, dalloc(h, &h->nw_acc, sizeof(double) * 3 * (h->g.nnw + 1)));
+    CK(h, dalloc(h, &h->nw_accm, sizeof(double) * (h->g.nnw + 1)));
+    h->bulk_blocks = (int)ceil_div(h->g.nseg, kStepThreads / 32);
+    h->nblocks = h->bulk_blocks + ceil_div(h->g.nsp, kStepThreads);
+    CK(h, dalloc(h, &h->partials, sizeof(double) * kPartialStride * (h->nblocks + 1)));
+    CK(h, dalloc(h, &h->sums, sizeof(double) * kPartialStride));
+    h->geo_bytes += h->npts * 5 + h->g.nsp * 25 + h->g.nseg * 4 + h->g.nact * 8;  // lists from setup
+    h->has_geo = true;
+    // counts
+    std::vector<uint8_t> spc(h->g.nsp);
+    if (h->g.nsp) CK(h, cudaMemcpyAsync(spc.data(), h->g.sp_cls, h->g.nsp, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    lbm_counts c{};
+    c.points = h->npts;
+    c.active = h->g.nact;
+    c.next_to_wall = h->g.nnw;
+    c.special = h->g.nsp;
+    c.segments = h->g.nseg;
+    int64_t bnd = 0;
+    for (uint8_t v : spc) {
+        if (v == CLS_WALL) c.wall++;
+        else if (v >= CLS_BC0 && v - CLS_BC0 < LBM_MAX_BC) c.bc[v - CLS_BC0]++;
+        if (v >= CLS_WALL) bnd++;
+    }
+    c.fluid = h->g.nact - bnd;
+    h->counts = c;
+    return lbm_init_equilibrium(h);
+}
+
+lbm_status lbm_set_normals_from_surface(lbm_handle* h, const double* tri12, int64_t ntri) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, ntri >= 0 && (ntri == 0 || tri12), LBM_ERR_ARG, "null triangles");
+    CK(h, cudaSetDevice(h->d.device));
+    double* d_tri = nullptr;
+    CK(h, cudaMalloc(&d_tri, sizeof(double) * 12 * (ntri > 0 ? ntri : 1)));
+    cudaError_t e = cudaSuccess;
+    if (ntri > 0) e = cudaMemcpyAsync(d_tri, tri12, sizeof(double) * 12 * ntri, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess)
+        e = surface_normals(d_tri, ntri, h->g.nw_pt, h->g.nnw, h->nx, h->ny, h->d.origin, h->d.spacing, h->nw_n, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(d_tri);
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("normals: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+lbm_status lbm_set_inlet_table(lbm_handle* h, const double* amp, int64_t n) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, amp && n > 0, LBM_ERR_ARG, "empty amplitude table");
+    CK(h, cudaSetDevice(h->d.device));
+    CK(h, cudaStreamSynchronize(h->st));
+    if (n != h->namp) {
+        drop_graph(h);  // the table pointer is baked into captured launches
+        cudaFree(h->amp);
+        h->amp = nullptr;
+        CK(h, cudaMalloc(&h->amp, sizeof(double) * n));
+    }
+    CK(h, cudaMemcpyAsync(h->amp, amp, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    h->namp = n;
+    h->amp_host.assign(amp, amp + n);
+    return LBM_OK;
+}
+
+lbm_status lbm_init_equilibrium(lbm_handle* h) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    CK(h, cudaSetDevice(h->d.device));
+    CK(h, init_state(h->d.precision, h->d.Q, 0, h->buf[0], h->stride, h->npts, nullptr, nullptr, 0, h->st));
+    return start_state(h, true);
+}
+
+lbm_status lbm_set_distributions(lbm_handle* h, const double* f) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, f, LBM_ERR_ARG, "null distributions");
+    CK(h, cudaSetDevice(h->d.device));
+    const size_t bytes = sizeof(double) * h->g.nact * h->d.Q;
+    if (!h->out_f) CK(h, dalloc(h, &h->out_f, bytes));
+    CK(h, cudaMemcpyAsync(h->out_f, f, bytes, cudaMemcpyHostToDevice, h->st));
+    CK(h, init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->npts, h->out_f, h->g.act_pt, h->g.nact, h->st));
+    return start_state(h, false);
+}
+
+lbm_status lbm_init_from_macro(lbm_handle* h, const float* rho, const float* u, int regularized) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, rho && u, LBM_ERR_ARG, "null rho or u");
+    CK(h, cudaSetDevice(h->d.device));
+    const int64_t na = h->g.nact;
+    float *d_rho = nullptr, *d_u = nullptr;
+    if (!h->out_f) CK(h, dalloc(h, &h->out_f, sizeof(double) * na * h->d.Q));
+    CK(h, cudaMalloc(&d_rho, sizeof(float) * (na + 1)));
+    cudaError_t e = cudaMalloc(&d_u, sizeof(float) * 3 * (na + 1));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rho, rho, sizeof(float) * na, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_u, u, sizeof(float) * 3 * na, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess)
+        e = warm_start_f(h->d.Q, d_rho, d_u, h->g.act_idx, h->g.act_pt, na, h->nx, h->ny, h->nz, h->d.tau,
+                         regularized, h->out_f, h->st);
+    if (e == cudaSuccess)
+        e = init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->npts, h->out_f, h->g.act_pt, na, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(d_rho);
+    if (d_u) cudaFree(d_u);
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("init_from_macro: ") + cudaGetErrorString(e));
+    return start_state(h, true);
+}
+
+lbm_status lbm_step(lbm_handle* h, int nsteps) {
+    int rc = lbm_step_async(h, nsteps);
+    if (rc) return rc;
+    return check_flags(h);
+}
+
+lbm_status lbm_check_status(lbm_handle* h) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state: set the geometry first");
+    return check_flags(h);
+}
+
+lbm_status lbm_step_async(lbm_handle* h, int nsteps) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state: set the geometry first");
+    REQUIRE(h, nsteps >= 0, LBM_ERR_ARG, "negative step count");
+    CK(h, cudaSetDevice(h->d.device));
+    int left = nsteps;
+    // Graph replay: a captured graph bakes the buffer roles (cur) and the
+    // counter slot (step parity); both flip every step, so a graph built at
+    // one (cur, parity) is valid whenever that pair recurs -- one direct step
+    // re-aligns otherwise.
+    while (h->graph_steps > 0 && left >= h->graph_steps) {
+        if (h->gexec && (h->gexec_parity != (int)(h->steps & 1) || h->gexec_cur != h->cur)) {
+            int rc = one_step(h);
+            if (rc) return rc;
+            --left;
+            continue;
+        }
+        if (!h->gexec) {
+            int rc = build_graph(h);
+            if (rc) return rc;
+        }
+        CK(h, cudaGraphLaunch(h->gexec, h->st));
+        h->launches += h->graph_steps;
+        h->steps += h->graph_steps;
+        h->since_start += h->graph_steps;
+        left -= h->graph_steps;  // even count: cur and parity return to the captured pair
+    }
+    for (; left > 0; --left) {
+        int rc = one_step(h);
+        if (rc) return rc;
+    }
+    return LBM_OK;
+}
+
+lbm_status lbm_sync(lbm_handle* h) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, steps_per_graph >= 0 && steps_per_graph % 2 == 0, LBM_ERR_ARG, "steps per graph must be even and >= 0");
+    drop_graph(h);
+    h->graph_steps = steps_per_graph;
+    return LBM_OK;
+}
+
+lbm_status lbm_get_counts(lbm_handle* h, lbm_counts* out) {
+    if (!h || !out) return fail(h, LBM_ERR_ARG, "null handle or output");
+    *out = h->counts;
+    out->steps = h->steps;
+    out->device_bytes = (int64_t)h->geo_bytes;
+    return LBM_OK;
+}
+
+lbm_status lbm_get_classes(lbm_handle* h, uint8_t* cls) {
+    if (!h || !cls) return fail(h, LBM_ERR_ARG, "null handle or output");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    CK(h, cudaMemcpyAsync(cls, h->g.cls, h->npts, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_distributions(lbm_handle* h, double* f) {
+    if (!h || !f) return fail(h, LBM_ERR_ARG, "null handle or output");
+    CK(h, cudaSetDevice(h->d.device));
+    int rc = readout(h, true);
+    if (rc) return rc;
+    CK(h, cudaMemcpyAsync(f, h->out_f, sizeof(double) * h->g.nact * h->d.Q, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    CK(h, cudaSetDevice(h->d.device));
+    int rc = readout(h, true);
+    if (rc) return rc;
+    const int64_t na = h->g.nact;
+    if (!h->macro) CK(h, dalloc(h, &h->macro, sizeof(double) * 4 * (na + 1)));
+    double* d_rho = h->macro;
+    double* d_u = h->macro + (na + 1);
+    CK(h, macro_from_f(h->d.Q, h->out_f, na, d_rho, d_u, h->st));
+    if (rho) CK(h, cudaMemcpyAsync(rho, d_rho, sizeof(double) * na, cudaMemcpyDeviceToHost, h->st));
+    if (u3) CK(h, cudaMemcpyAsync(u3, d_u, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3, double* acc_mag,
+                       double* osi, double* tawss) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    const int64_t n = h->g.nnw;
+    std::vector<double> nn(3 * n), w(n), a(3 * n), am(n);
+    if (n) {
+        CK(h, cudaMemcpyAsync(nn.data(), h->nw_n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(w.data(), h->nw_wss, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(a.data(), h->nw_acc, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(am.data(), h->nw_accm, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+        if (pt) CK(h, cudaMemcpyAsync(pt, h->g.nw_pt, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(h, cudaStreamSynchronize(h->st));
+    for (int64_t p = 0; p < n; ++p) {
+        const double a0 = a[p], a1 = a[n + p], a2 = a[2 * n + p];
+        if (normal3) { normal3[3 * p] = nn[p]; normal3[3 * p + 1] = nn[n + p]; normal3[3 * p + 2] = nn[2 * n + p]; }
+        if (wss) wss[p] = w[p];
+        if (acc3) { acc3[3 * p] = a0; acc3[3 * p + 1] = a1; acc3[3 * p + 2] = a2; }
+        if (acc_mag) acc_mag[p] = am[p];
+        // ComputeOSIAndTAWSS (Simulation.cpp:899-905)
+        if (tawss) tawss[p] = am[p] / h->d.tawss_div;
+        if (osi) {
+            double norm = std::sqrt(std::pow(a0, 2) + std::pow(a1, 2) + std::pow(a2, 2));
+            osi[p] = 0.5 * (1.0 - (norm / am[p]));
+        }
+    }
+    return LBM_OK;
+}
+
+lbm_status lbm_get_conservation(lbm_handle* h, double* mass, double* mom3, double* flux) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    CK(h, cudaSetDevice(h->d.device));
+    int rc = readout(h, false);
+    if (rc) return rc;
+    double s[kPartialStride];
+    CK(h, cudaMemcpyAsync(s, h->sums, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    if (mass) *mass = s[0];
+    if (mom3) { mom3[0] = s[1]; mom3[1] = s[2]; mom3[2] = s[3]; }
+    if (flux)
+        for (int b = 0; b < h->nbc; ++b) flux[b] = s[4 + b];
+    return LBM_OK;
+}
+
+lbm_status lbm_save(lbm_handle* h, const char* path) {
+    if (!h || !path) return fail(h, LBM_ERR_ARG, "null handle or path");
+    REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state to save");
+    const int64_t na = h->g.nact, nn = h->g.nnw;
+    std::vector<double> f(na * h->d.Q), acc(3 * nn), accm(nn), wss(nn);
+    int rc = lbm_get_distributions(h, f.data());
+    if (rc) return rc;
+    if (nn) {
+        CK(h, cudaMemcpyAsync(acc.data(), h->nw_acc, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(accm.data(), h->nw_accm, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(wss.data(), h->nw_wss, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(h, cudaStreamSynchronize(h->st));
+    std::FILE* fp = std::fopen(path, "wb");
+    REQUIRE(h, fp, LBM_ERR_IO, std::string("cannot write ") + path);
+    const uint32_t head[2] = {kCkptMagic, kCkptVersion};
+    const int32_t cfg[6] = {h->d.Q, h->d.precision, h->d.mode, h->nx, h->ny, h->nz};
+    const int64_t sz[4] = {na, nn, h->steps, h->namp};
+    bool ok = std::fwrite(head, sizeof(head), 1, fp) == 1 && std::fwrite(cfg, sizeof(cfg), 1, fp) == 1 &&
+              std::fwrite(sz, sizeof(sz), 1, fp) == 1 &&
+              std::fwrite(f.data(), sizeof(double), f.size(), fp) == f.size() &&
+              std::fwrite(acc.data(), sizeof(double), acc.size(), fp) == acc.size() &&
+              std::fwrite(accm.data(), sizeof(double), accm.size(), fp) == accm.size() &&
+              std::fwrite(wss.data(), sizeof(double), wss.size(), fp) == wss.size() &&
+              std::fwrite(h->amp_host.data(), sizeof(double), h->amp_host.size(), fp) == h->amp_host.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    REQUIRE(h, ok, LBM_ERR_IO, std::string("short write to ") + path);
+    return LBM_OK;
+}
+
+lbm_status lbm_load(lbm_handle* h, const char* path) {
+    if (!h || !path) return fail(h, LBM_ERR_ARG, "null handle or path");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the same geometry before loading");
+    std::FILE* fp = std::fopen(path, "rb");
+    REQUIRE(h, fp, LBM_ERR_IO, std::string("cannot open ") + path);
+    uint32_t head[2];
+    int32_t cfg[6];
+    int64_t sz[4];
+    bool ok = std::fread(head, sizeof(head), 1, fp) == 1 && std::fread(cfg, sizeof(cfg), 1, fp) == 1 &&
+              std::fread(sz, sizeof(sz), 1, fp) == 1;
+    if (!ok || head[0] != kCkptMagic || head[1] != kCkptVersion) {
+        std::fclose(fp);
+        return fail(h, LBM_ERR_IO, "not a checkpoint of this version");
+    }
+    if (cfg[0] != h->d.Q || cfg[3] != h->nx || cfg[4] != h->ny || cfg[5] != h->nz || sz[0] != h->g.nact ||
+        sz[1] != h->g.nnw || sz[3] < 1) {
+        std::fclose(fp);
+        return fail(h, LBM_ERR_ARG, "checkpoint lattice does not match this handle");
+    }
+    const int64_t na = sz[0], nn = sz[1];
+    std::vector<double> f(na * h->d.Q), acc(3 * nn), accm(nn), wss(nn), amp(sz[3]);
+    ok = std::fread(f.data(), sizeof(double), f.size(), fp) == f.size() &&
+         std::fread(acc.data(), sizeof(double), acc.size(), fp) == acc.size() &&
+         std::fread(accm.data(), sizeof(double), accm.size(), fp) == accm.size() &&
+         std::fread(wss.data(), sizeof(double), wss.size(), fp) == wss.size() &&
+         std::fread(amp.data(), sizeof(double), amp.size(), fp) == amp.size();
+    std::fclose(fp);
+    REQUIRE(h, ok, LBM_ERR_IO, std::string("truncated checkpoint ") + path);
+    int rc = lbm_set_inlet_table(h, amp.data(), (int64_t)amp.size());
+    if (rc) return rc;
+    if (nn) {
+        CK(h, cudaMemcpyAsync(h->nw_acc, acc.data(), sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, h->st));
+        CK(h, cudaMemcpyAsync(h->nw_accm, accm.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, h->st));
+        CK(h, cudaMemcpyAsync(h->nw_wss, wss.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, h->st));
+    }
+    h->steps = sz[2];
+    return lbm_set_distributions(h, f.data());
+}
+
+lbm_status lbm_get_stream(lbm_handle* h, void** stream) {
+    if (!h || !stream) return fail(h, LBM_ERR_ARG, "null handle or output");
+    *stream = (void*)h->st;
+    return LBM_OK;
+}
+
+lbm_status lbm_get_launch_count(lbm_handle* h, int64_t* launches) {
+    if (!h || !launches) return fail(h, LBM_ERR_ARG, "null handle or output");
+    *launches = h->launches;
+    return LBM_OK;
+}
+
+}  // extern "C"

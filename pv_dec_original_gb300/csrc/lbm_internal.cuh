@@ -1,0 +1,116 @@
+// Internal device structures shared by the library's translation units.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "lbm_lattice.cuh"
+#include "../../include/lbm_gb300.h"
+
+namespace lbm {
+
+// Class byte per lattice point.
+enum : uint8_t { CLS_SOLID = 0, CLS_FLUID = 1, CLS_WALL = 2, CLS_BC0 = 3, CLS_NW_BIT = 0x80, CLS_MASK = 0x7f };
+
+// Error flags raised by kernels (polled by the host after each batch).
+enum : unsigned { FLAG_NONFINITE = 1u, FLAG_EXACT_ZERO = 2u, FLAG_BOUNDS = 4u };
+
+struct BCDev {
+    int kind;
+    int face;
+    double value;
+    int profile;
+    double c1, c2, R;
+};
+
+// Everything one stream-collide launch needs (passed by value).
+struct StepParams {
+    const void* fin;
+    void* fout;
+    int64_t stride;        // elements per population plane
+    int nx, ny;
+    int64_t nxy;
+    const uint8_t* cls;    // per point
+    const int32_t* seg;    // bulk segments (start point / 32)
+    int64_t nseg;
+    int bulk_blocks;       // blocks [0, bulk_blocks) run the bulk part
+    // boundary-list part ("special": boundary + next-to-wall nodes)
+    int64_t nsp;
+    const int64_t* sp_pt;
+    const uint32_t* sp_miss;  // bit q: lattice point x + c_q is not active
+    const uint8_t* sp_cls;
+    const int32_t* sp_nw;     // next-to-wall index or -1
+    const double* sp_prof;    // inlet profile factor
+    void* stale;              // parity: previous post-boundary f, [q][nsp] in the arithmetic type
+    // next-to-wall accumulators
+    int64_t nnw;
+    const double* nw_n;       // [3][nnw]
+    double* nw_wss;
+    double* nw_acc;           // [3][nnw]
+    double* nw_accm;
+    void* nw_prev;            // parity: rho, ux, uy, uz of the previous collision, [4][nnw]
+    double tau;
+    double wss_C;
+    // inlet amplitude table: step index = *step_base + step_off
+    const double* amp;
+    int64_t namp;
+    const int64_t* step_base;  // step counter slot read by this launch
+    int64_t* step_next;        // the other slot: written with *step_base + 1
+    int step_off;
+    int direct;                // read-out of the initial state: no pull, no boundary rules
+    BCDev bc[LBM_MAX_BC];
+    int nbc;
+    unsigned* flags;
+    // readout (materialize) outputs
+    double* out_f;            // [a*Q + q] FP64, or null
+    const int32_t* act_idx;   // per point active index (readout only)
+    double* partials;         // per block: mass, mom3, flux[LBM_MAX_BC]
+};
+
+constexpr int kPartialStride = 4 + LBM_MAX_BC;
+constexpr int kStepThreads = 256;
+
+// Launchers (one per translation unit family).  kind: 0 step, 1 prologue
+// (collide the initial state), 2 materialize (post-boundary f + sums).
+cudaError_t launch_step_f64(int Q, int mode, int kind, const StepParams& p, cudaStream_t s);
+cudaError_t launch_step_fast(int Q, int precision, int mode, int kind, const StepParams& p, cudaStream_t s);
+
+// State initialisation: what = 0 fills f = w on every point, what = 1
+// scatters fa[a*Q + q] (FP64, per active node) into the planes.
+cudaError_t init_state(int precision, int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
+                       const int64_t* act_pt, int64_t nact, cudaStream_t s);
+cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
+                           const int64_t* act_pt, int64_t nact, cudaStream_t s);
+cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t stride, int64_t npts,
+                            const double* fa, const int64_t* act_pt, int64_t nact, cudaStream_t s);
+
+// Read-out helpers (step_f64.cu): ordered FP64 sum of per-block partials,
+// and rho/u from read-out distributions.
+cudaError_t reduce_partials(const double* partials, int64_t nblocks, double* out, cudaStream_t s);
+cudaError_t macro_from_f(int Q, const double* f, int64_t nact, double* rho, double* u3, cudaStream_t s);
+// Warm start: f = f_eq(rho, u) (+ regularised non-equilibrium part from
+// finite-difference velocity gradients), FP64 per active node.
+cudaError_t warm_start_f(int Q, const float* rho, const float* u, const int32_t* act_idx, const int64_t* act_pt,
+                         int64_t nact, int nx, int ny, int nz, double tau, int regularized, double* fa,
+                         cudaStream_t s);
+
+// Voxelizer (voxelize.cu).
+struct VoxResult {
+    int64_t fluid;
+    int64_t tests;
+};
+cudaError_t voxelize_device(const double* d_tri, int64_t ntri, const double bbox[6], const double origin[3],
+                            double spacing, const int dims[3], uint8_t* d_mask, VoxResult* res, cudaStream_t s,
+                            std::string* err);
+
+// Exclusive scan of int64 counts (scan.cu); returns the total.
+cudaError_t exclusive_scan_i64(const int64_t* d_in, int64_t* d_out, int64_t n, int64_t* total, cudaStream_t s);
+
+// Normals: for each listed point, the area / distance^2 weighted surface
+// normal (Subdomain.cpp:224-370).  out is [3][npts].
+cudaError_t surface_normals(const double* d_tri, int64_t ntri, const int64_t* d_pts, int64_t npts, int nx, int ny,
+                            const double origin[3], double spacing, double* d_out, cudaStream_t s);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace lbm

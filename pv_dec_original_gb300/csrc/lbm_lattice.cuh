@@ -1,0 +1,135 @@
+// Lattice tables and storage traits shared by every kernel.
+//
+// Direction numbering follows the reference so that distributions, boundary
+// formulas and dumps line up index for index:
+//   D3Q19: LatticeModel.cpp:51-151 (rest population is index 18),
+//   D3Q27: LatticeModel.cpp:208-334 (rest population is index 0).
+// Weights are the reference's literals (2/36, 1/36, 12/36; 8/27, 2/27, 1/54,
+// 1/216) so host and device produce identical doubles.
+#pragma once
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+namespace lbm {
+
+template <int Q> struct Lat;
+
+template <> struct Lat<19> {
+    static constexpr int Q = 19;
+    static constexpr int REST = 18;
+    __host__ __device__ static constexpr int cx(int q) {
+        constexpr int t[19] = {1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0, 0};
+        return t[q];
+    }
+    __host__ __device__ static constexpr int cy(int q) {
+        constexpr int t[19] = {0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0};
+        return t[q];
+    }
+    __host__ __device__ static constexpr int cz(int q) {
+        constexpr int t[19] = {0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1, 0};
+        return t[q];
+    }
+    __host__ __device__ static constexpr int opp(int q) {
+        constexpr int t[19] = {1, 0, 3, 2, 5, 4, 11, 10, 13, 12, 7, 6, 9, 8, 17, 16, 15, 14, 18};
+        return t[q];
+    }
+    __host__ __device__ static constexpr double w(int q) {
+        return q < 6 ? 2.0 / 36.0 : (q < 18 ? 1.0 / 36.0 : 12.0 / 36.0);
+    }
+    // Sum over the unknown populations of one face of c_t^2 for a transverse axis t.
+    static constexpr double ZH_M = 2.0;
+};
+
+template <> struct Lat<27> {
+    static constexpr int Q = 27;
+    static constexpr int REST = 0;
+    __host__ __device__ static constexpr int cx(int q) {
+        constexpr int t[27] = {0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+        return t[q];
+    }
+    __host__ __device__ static constexpr int cy(int q) {
+        constexpr int t[27] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 1, -1, -1, 1, -1, 1};
+        return t[q];
+    }
+    __host__ __device__ static constexpr int cz(int q) {
+        constexpr int t[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 1, -1, 1, -1, -1, 1, 1, -1, -1, 1};
+        return t[q];
+    }
+    __host__ __device__ static constexpr int opp(int q) {
+        constexpr int t[27] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15,
+                               20, 19, 22, 21, 24, 23, 26, 25};
+        return t[q];
+    }
+    __host__ __device__ static constexpr double w(int q) {
+        return q == 0 ? 8.0 / 27.0 : (q < 7 ? 2.0 / 27.0 : (q < 19 ? 1.0 / 54.0 : 1.0 / 216.0));
+    }
+    static constexpr double ZH_M = 6.0;
+};
+
+template <int Q>
+__host__ __device__ constexpr int lat_c(int q, int axis) {
+    return axis == 0 ? Lat<Q>::cx(q) : (axis == 1 ? Lat<Q>::cy(q) : Lat<Q>::cz(q));
+}
+
+// ---------------------------------------------------------------------------
+// Storage formats.  FP64 and FP32 store f directly.  FP16 and BF16 store the
+// offset from the lattice weight, relative to it and scaled:
+//     stored = (f - w) / w * S,   f = w + (w / S) * stored
+// S = 1024 for FP16 keeps offsets down to ~6e-8 in the normal range while
+// +-0.5 relative offsets stay far below the FP16 maximum; BF16 has FP32's
+// exponent range and uses S = 1.
+enum Precision : int { P_F64 = 0, P_F32 = 1, P_F16 = 2, P_BF16 = 3 };
+
+template <typename S> struct Store;
+
+template <> struct Store<double> {
+    using real = double;
+    static constexpr int precision = P_F64;
+    template <int Q>
+    __device__ static __forceinline__ real load(const double* p, int q) { return *p; }
+    template <int Q>
+    __device__ static __forceinline__ double pack(real f, int q) { return f; }
+};
+
+template <> struct Store<float> {
+    using real = float;
+    static constexpr int precision = P_F32;
+    template <int Q>
+    __device__ static __forceinline__ real load(const float* p, int q) { return __ldg(p); }
+    template <int Q>
+    __device__ static __forceinline__ float pack(real f, int q) { return f; }
+};
+
+template <> struct Store<__half> {
+    using real = float;
+    static constexpr int precision = P_F16;
+    static constexpr float S = 1024.0f;
+    template <int Q>
+    __device__ static __forceinline__ real load(const __half* p, int q) {
+        const float w = (float)Lat<Q>::w(q);
+        return fmaf(__half2float(__ldg(p)), w * (1.0f / S), w);
+    }
+    template <int Q>
+    __device__ static __forceinline__ __half pack(real f, int q) {
+        const float w = (float)Lat<Q>::w(q);
+        return __float2half_rn((f - w) * (S / w));
+    }
+};
+
+template <> struct Store<__nv_bfloat16> {
+    using real = float;
+    static constexpr int precision = P_BF16;
+    template <int Q>
+    __device__ static __forceinline__ real load(const __nv_bfloat16* p, int q) {
+        const float w = (float)Lat<Q>::w(q);
+        return fmaf(__bfloat162float(__ldg(p)), w, w);
+    }
+    template <int Q>
+    __device__ static __forceinline__ __nv_bfloat16 pack(real f, int q) {
+        const float w = (float)Lat<Q>::w(q);
+        return __float2bfloat16_rn((f - w) * (1.0f / w));
+    }
+};
+
+}  // namespace lbm

@@ -1,0 +1,357 @@
+// Geometry set-up on the device: node classes, boundary-node list,
+// next-to-wall nodes, bulk segments and wall normals.
+//
+// Replaces the reference's pointer-graph construction:
+//   findBoundaryPoints          ComplexGeometry.cpp:1259-1300
+//   classifyBoundaryPoints      ComplexGeometry.cpp:1369-1429 (plane rules instead of PV coordinates)
+//   SubDomain::CreateNodes      Subdomain.cpp:91-169 (Boundary vs Node by list membership)
+//   Connectivity                Subdomain.cpp:173-197 (-> per-link "missing" bit masks)
+//   IdentifyNextToWallLattices  Subdomain.cpp:201-218
+//   calculateBoundaryNormals    Subdomain.cpp:224-370
+// The reference links one heap object per node with shared_ptr neighbours
+// and finds list membership by linear search (Utility.cpp:18-33, O(A*B));
+// here a node is one class byte in a dense box and the boundary/next-to-wall
+// nodes form one compact, index-sorted list built by a scan.
+//
+// Compiled with --fmad=false: the normals keep the reference's rounding
+// (pow(d, 2) is evaluated as d*d).
+#include "lbm_internal.cuh"
+#include "setup.cuh"
+
+namespace lbm {
+namespace {
+
+template <int Q>
+__global__ void k_boundary(const uint8_t* __restrict__ mask, int nx, int ny, int nz, uint8_t* __restrict__ cls) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t npts = (int64_t)nx * ny * nz;
+    if (n >= npts) return;
+    if (!mask[n]) { cls[n] = CLS_SOLID; return; }
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+    bool b = false;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        int a = i + Lat<Q>::cx(q), bb = j + Lat<Q>::cy(q), c = k + Lat<Q>::cz(q);
+        if (a < 0 || a >= nx || bb < 0 || bb >= ny || c < 0 || c >= nz) { b = true; break; }
+        if (!mask[((int64_t)c * ny + bb) * nx + a]) { b = true; break; }
+    }
+    cls[n] = b ? CLS_WALL : CLS_FLUID;
+}
+
+// Extreme fluid layer per axis: ext[0..2] = min index, ext[3..5] = max index.
+__global__ void k_extent(const uint8_t* __restrict__ mask, int nx, int ny, int nz, int* __restrict__ ext) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t npts = (int64_t)nx * ny * nz;
+    if (n >= npts || !mask[n]) return;
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+    atomicMin(ext + 0, i); atomicMin(ext + 1, j); atomicMin(ext + 2, k);
+    atomicMax(ext + 3, i); atomicMax(ext + 4, j); atomicMax(ext + 5, k);
+}
+
+struct Rules {
+    int n;
+    int axis[LBM_MAX_BC];
+    int plane[LBM_MAX_BC];
+};
+
+__global__ void k_classify(uint8_t* __restrict__ cls, int nx, int ny, int64_t npts, Rules R) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts || cls[n] != CLS_WALL) return;
+    const int idx[3] = {(int)(n % nx), (int)((n / nx) % ny), (int)(n / ((int64_t)nx * ny))};
+    for (int r = 0; r < R.n; ++r)
+        if (idx[R.axis[r]] == R.plane[r]) { cls[n] = (uint8_t)(CLS_BC0 + r); return; }
+}
+
+template <int Q>
+__global__ void k_next_to_wall(uint8_t* __restrict__ cls, int nx, int ny, int nz) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t npts = (int64_t)nx * ny * nz;
+    if (n >= npts || cls[n] != CLS_FLUID) return;
+    // an interior fluid node has all Q neighbours inside the box
+    const int64_t nxy = (int64_t)nx * ny;
+    bool nw = false;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        int64_t m = n + Lat<Q>::cx(q) + Lat<Q>::cy(q) * (int64_t)nx + Lat<Q>::cz(q) * nxy;
+        if ((cls[m] & CLS_MASK) == CLS_WALL) nw = true;
+    }
+    if (nw) cls[n] = CLS_FLUID | CLS_NW_BIT;
+}
+
+__global__ void k_flag_special(const uint8_t* __restrict__ cls, int64_t npts, int64_t* __restrict__ flag,
+                               int64_t* __restrict__ nwflag) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts) return;
+    const uint8_t c = cls[n];
+    flag[n] = ((c & CLS_MASK) >= CLS_WALL || (c & CLS_NW_BIT)) ? 1 : 0;
+    nwflag[n] = (c & CLS_NW_BIT) ? 1 : 0;
+}
+
+__global__ void k_scatter(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t npts,
+                          int64_t* __restrict__ out) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts || !flag[n]) return;
+    out[pos[n]] = n;
+}
+
+template <int Q>
+__global__ void k_special_info(const int64_t* __restrict__ sp_pt, int64_t nsp, const uint8_t* __restrict__ cls,
+                               const int64_t* __restrict__ nwpos, int nx, int ny, int nz,
+                               uint32_t* __restrict__ miss, uint8_t* __restrict__ spc, int32_t* __restrict__ spnw,
+                               double* __restrict__ prof, ProfileSpec ps) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsp) return;
+    const int64_t n = sp_pt[s];
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+    uint32_t m = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        int a = i + Lat<Q>::cx(q), b = j + Lat<Q>::cy(q), c = k + Lat<Q>::cz(q);
+        bool missing = (a < 0 || a >= nx || b < 0 || b >= ny || c < 0 || c >= nz) ||
+                       cls[((int64_t)c * ny + b) * nx + a] == CLS_SOLID;
+        if (missing) m |= 1u << q;
+    }
+    miss[s] = m;
+    const uint8_t c = cls[n];
+    spc[s] = c & CLS_MASK;
+    spnw[s] = (c & CLS_NW_BIT) ? (int32_t)nwpos[n] : -1;
+    double p = 0.0;
+    const int b = (c & CLS_MASK) - CLS_BC0;
+    if ((c & CLS_MASK) >= CLS_BC0 && b < ps.n) {
+        if (ps.profile[b] == 0) {
+            p = 1.0;
+        } else {
+            // same expression as the reference harness / oracle profile factor
+            const double xyz[3] = {ps.org[0] + i * ps.s, ps.org[1] + j * ps.s, ps.org[2] + k * ps.s};
+            const int a = ps.axis[b];
+            const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+            double d1 = xyz[t1] - ps.c1[b], d2 = xyz[t2] - ps.c2[b];
+            double v = 1.0 - (d1 * d1 + d2 * d2) / (ps.R[b] * ps.R[b]);
+            p = v > 0.0 ? v : 0.0;
+        }
+    }
+    prof[s] = p;
+}
+
+__global__ void k_flag_segments(const uint8_t* __restrict__ cls, int64_t npts, int64_t nsegs,
+                                int64_t* __restrict__ flag) {
+    const int64_t sgi = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (sgi >= nsegs) return;
+    const int64_t n = sgi * 32 + lane;
+    const bool bulk = n < npts && cls[n] == CLS_FLUID;
+    const unsigned any = __ballot_sync(0xffffffffu, bulk);
+    if (lane == 0) flag[sgi] = any ? 1 : 0;
+}
+
+__global__ void k_scatter_seg(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t nsegs,
+                              int32_t* __restrict__ out) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsegs || !flag[s]) return;
+    out[pos[s]] = (int32_t)s;
+}
+
+__global__ void k_active_flags(const uint8_t* __restrict__ cls, int64_t npts, int64_t* __restrict__ flag) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts) return;
+    flag[n] = cls[n] != CLS_SOLID ? 1 : 0;
+}
+
+__global__ void k_active_index(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t npts,
+                               int32_t* __restrict__ act_idx, int64_t* __restrict__ act_pt) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts) return;
+    if (flag[n]) {
+        act_idx[n] = (int32_t)pos[n];
+        act_pt[pos[n]] = n;
+    } else {
+        act_idx[n] = -1;
+    }
+}
+
+// Per-triangle unit normal, area and centroid (Subdomain.cpp:244-267).
+__global__ void k_tri_weights(const double* __restrict__ tri, int64_t ntri, double* __restrict__ tw) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const double* T = tri + 12 * t;
+    double ux = T[3] - T[0], uy = T[4] - T[1], uz = T[5] - T[2];
+    double vx = T[6] - T[0], vy = T[7] - T[1], vz = T[8] - T[2];
+    double nx = uy * vz - uz * vy;
+    double ny = uz * vx - ux * vz;
+    double nz = ux * vy - uy * vx;
+    double norm = sqrt(nx * nx + ny * ny + nz * nz);
+    if (norm > 0) { nx /= norm; ny /= norm; nz /= norm; }
+    double area = 0.5 * norm;
+    double* o = tw + 7 * t;
+    o[0] = nx; o[1] = ny; o[2] = nz; o[3] = area;
+    o[4] = (T[0] + T[3] + T[6]) / 3.0;
+    o[5] = (T[1] + T[4] + T[7]) / 3.0;
+    o[6] = (T[2] + T[5] + T[8]) / 3.0;
+}
+
+constexpr int kNormThreads = 128;
+constexpr int kNormTile = 256;
+
+__global__ void __launch_bounds__(kNormThreads) k_normals(const double* __restrict__ tw, int64_t ntri,
+                                                         const int64_t* __restrict__ pts, int64_t npts, int nx,
+                                                         int ny, double ox, double oy, double oz, double s,
+                                                         double* __restrict__ out) {
+    __shared__ double tile[kNormTile * 7];
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double x = 0, y = 0, z = 0;
+    if (p < npts) {
+        const int64_t n = pts[p];
+        const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+        x = ox + i * s; y = oy + j * s; z = oz + k * s;
+    }
+    double n0 = 0.0, n1 = 0.0, n2 = 0.0;
+    for (int64_t t0 = 0; t0 < ntri; t0 += kNormTile) {
+        const int cnt = (int)min((int64_t)kNormTile, ntri - t0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt * 7; e += blockDim.x) tile[e] = tw[7 * t0 + e];
+        __syncthreads();
+        for (int t = 0; t < cnt; ++t) {
+            const double* o = tile + 7 * t;
+            double dx = x - o[4], dy = y - o[5], dz = z - o[6];
+            double distance = sqrt(dx * dx + dy * dy + dz * dz);
+            double w = o[3] / (distance * distance);
+            n0 += o[0] * w;
+            n1 += o[1] * w;
+            n2 += o[2] * w;
+        }
+    }
+    if (p < npts) {
+        double norm = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+        if (norm > 0) { n0 /= norm; n1 /= norm; n2 /= norm; }
+        out[p] = n0;
+        out[npts + p] = n1;
+        out[2 * npts + p] = n2;
+    }
+}
+
+inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)ceil_div(n > 0 ? n : 1, t); }
+
+}  // namespace
+
+#define SETUP_CHECK(call)                                                       \
+    do {                                                                        \
+        cudaError_t _e = (call);                                                \
+        if (_e != cudaSuccess) {                                                \
+            err = std::string(#call) + ": " + cudaGetErrorString(_e);          \
+            return _e;                                                          \
+        }                                                                       \
+    } while (0)
+
+cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz, const lbm_bc_spec* bc, int nbc,
+                           const double origin[3], double spacing, GeometryLists& out, cudaStream_t st,
+                           std::string& err) {
+    const int64_t npts = (int64_t)nx * ny * nz;
+    out.npts = npts;
+    SETUP_CHECK(cudaMallocAsync(&out.cls, npts, st));
+    if (Q == 19) k_boundary<19><<<blocks(npts), 256, 0, st>>>(d_mask, nx, ny, nz, out.cls);
+    else k_boundary<27><<<blocks(npts), 256, 0, st>>>(d_mask, nx, ny, nz, out.cls);
+    SETUP_CHECK(cudaGetLastError());
+
+    // plane rules; plane -1 = extreme fluid layer on the face
+    Rules R{};
+    R.n = nbc;
+    bool need_ext = false;
+    for (int b = 0; b < nbc; ++b) need_ext |= bc[b].plane < 0;
+    int ext[6] = {0, 0, 0, -1, -1, -1};
+    if (need_ext) {
+        int* d_ext = nullptr;
+        int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, -1, -1, -1};
+        SETUP_CHECK(cudaMallocAsync(&d_ext, sizeof(init), st));
+        SETUP_CHECK(cudaMemcpyAsync(d_ext, init, sizeof(init), cudaMemcpyHostToDevice, st));
+        k_extent<<<blocks(npts), 256, 0, st>>>(d_mask, nx, ny, nz, d_ext);
+        SETUP_CHECK(cudaMemcpyAsync(ext, d_ext, sizeof(ext), cudaMemcpyDeviceToHost, st));
+        SETUP_CHECK(cudaStreamSynchronize(st));
+        cudaFreeAsync(d_ext, st);
+    }
+    for (int b = 0; b < nbc; ++b) {
+        const int face = bc[b].face;
+        R.axis[b] = face / 2;
+        R.plane[b] = bc[b].plane >= 0 ? bc[b].plane : (face % 2 == 0 ? ext[face / 2] : ext[3 + face / 2]);
+        out.plane[b] = R.plane[b];
+    }
+    k_classify<<<blocks(npts), 256, 0, st>>>(out.cls, nx, ny, npts, R);
+    SETUP_CHECK(cudaGetLastError());
+    if (Q == 19) k_next_to_wall<19><<<blocks(npts), 256, 0, st>>>(out.cls, nx, ny, nz);
+    else k_next_to_wall<27><<<blocks(npts), 256, 0, st>>>(out.cls, nx, ny, nz);
+    SETUP_CHECK(cudaGetLastError());
+
+    // compact lists
+    int64_t *flag = nullptr, *pos = nullptr, *nwflag = nullptr, *nwpos = nullptr;
+    SETUP_CHECK(cudaMallocAsync(&flag, sizeof(int64_t) * npts, st));
+    SETUP_CHECK(cudaMallocAsync(&pos, sizeof(int64_t) * npts, st));
+    SETUP_CHECK(cudaMallocAsync(&nwflag, sizeof(int64_t) * npts, st));
+    SETUP_CHECK(cudaMallocAsync(&nwpos, sizeof(int64_t) * npts, st));
+    k_flag_special<<<blocks(npts), 256, 0, st>>>(out.cls, npts, flag, nwflag);
+    SETUP_CHECK(exclusive_scan_i64(flag, pos, npts, &out.nsp, st));
+    SETUP_CHECK(exclusive_scan_i64(nwflag, nwpos, npts, &out.nnw, st));
+    SETUP_CHECK(cudaMallocAsync(&out.sp_pt, sizeof(int64_t) * (out.nsp + 1), st));
+    SETUP_CHECK(cudaMallocAsync(&out.nw_pt, sizeof(int64_t) * (out.nnw + 1), st));
+    k_scatter<<<blocks(npts), 256, 0, st>>>(flag, pos, npts, out.sp_pt);
+    k_scatter<<<blocks(npts), 256, 0, st>>>(nwflag, nwpos, npts, out.nw_pt);
+    SETUP_CHECK(cudaGetLastError());
+    SETUP_CHECK(cudaMallocAsync(&out.sp_miss, sizeof(uint32_t) * (out.nsp + 1), st));
+    SETUP_CHECK(cudaMallocAsync(&out.sp_cls, out.nsp + 1, st));
+    SETUP_CHECK(cudaMallocAsync(&out.sp_nw, sizeof(int32_t) * (out.nsp + 1), st));
+    SETUP_CHECK(cudaMallocAsync(&out.sp_prof, sizeof(double) * (out.nsp + 1), st));
+    ProfileSpec ps{};
+    ps.n = nbc;
+    ps.s = spacing;
+    for (int d = 0; d < 3; ++d) ps.org[d] = origin[d];
+    for (int b = 0; b < nbc; ++b) {
+        ps.profile[b] = bc[b].profile;
+        ps.axis[b] = bc[b].face / 2;
+        ps.c1[b] = bc[b].c1; ps.c2[b] = bc[b].c2; ps.R[b] = bc[b].R;
+    }
+    if (out.nsp > 0) {
+        if (Q == 19)
+            k_special_info<19><<<blocks(out.nsp), 256, 0, st>>>(out.sp_pt, out.nsp, out.cls, nwpos, nx, ny, nz,
+                                                               out.sp_miss, out.sp_cls, out.sp_nw, out.sp_prof, ps);
+        else
+            k_special_info<27><<<blocks(out.nsp), 256, 0, st>>>(out.sp_pt, out.nsp, out.cls, nwpos, nx, ny, nz,
+                                                               out.sp_miss, out.sp_cls, out.sp_nw, out.sp_prof, ps);
+        SETUP_CHECK(cudaGetLastError());
+    }
+
+    // bulk segments: 32 consecutive points holding at least one interior node
+    const int64_t nsegs = ceil_div(npts, 32);
+    k_flag_segments<<<blocks(nsegs, 8), 256, 0, st>>>(out.cls, npts, nsegs, flag);
+    SETUP_CHECK(exclusive_scan_i64(flag, pos, nsegs, &out.nseg, st));
+    SETUP_CHECK(cudaMallocAsync(&out.seg, sizeof(int32_t) * (out.nseg + 1), st));
+    k_scatter_seg<<<blocks(nsegs), 256, 0, st>>>(flag, pos, nsegs, out.seg);
+    SETUP_CHECK(cudaGetLastError());
+
+    // active index (readouts)
+    k_active_flags<<<blocks(npts), 256, 0, st>>>(out.cls, npts, flag);
+    SETUP_CHECK(exclusive_scan_i64(flag, pos, npts, &out.nact, st));
+    SETUP_CHECK(cudaMallocAsync(&out.act_idx, sizeof(int32_t) * npts, st));
+    SETUP_CHECK(cudaMallocAsync(&out.act_pt, sizeof(int64_t) * (out.nact + 1), st));
+    k_active_index<<<blocks(npts), 256, 0, st>>>(flag, pos, npts, out.act_idx, out.act_pt);
+    SETUP_CHECK(cudaGetLastError());
+    cudaFreeAsync(flag, st);
+    cudaFreeAsync(pos, st);
+    cudaFreeAsync(nwflag, st);
+    cudaFreeAsync(nwpos, st);
+    SETUP_CHECK(cudaStreamSynchronize(st));
+    return cudaSuccess;
+}
+
+cudaError_t surface_normals(const double* d_tri, int64_t ntri, const int64_t* d_pts, int64_t npts, int nx, int ny,
+                            const double origin[3], double spacing, double* d_out, cudaStream_t st) {
+    if (npts <= 0) return cudaSuccess;
+    double* tw = nullptr;
+    cudaError_t e = cudaMallocAsync(&tw, sizeof(double) * 7 * (ntri > 0 ? ntri : 1), st);
+    if (e != cudaSuccess) return e;
+    if (ntri > 0) k_tri_weights<<<blocks(ntri), 256, 0, st>>>(d_tri, ntri, tw);
+    k_normals<<<blocks(npts, kNormThreads), kNormThreads, 0, st>>>(tw, ntri, d_pts, npts, nx, ny, origin[0],
+                                                                  origin[1], origin[2], spacing, d_out);
+    e = cudaGetLastError();
+    cudaFreeAsync(tw, st);
+    return e;
+}
+
+}  // namespace lbm

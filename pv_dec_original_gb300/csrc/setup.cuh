@@ -1,0 +1,40 @@
+// Device geometry lists built by setup.cu.
+#pragma once
+#include <string>
+#include "lbm_internal.cuh"
+
+namespace lbm {
+
+struct ProfileSpec {
+    int n;
+    double s;
+    double org[3];
+    int profile[LBM_MAX_BC];
+    int axis[LBM_MAX_BC];
+    double c1[LBM_MAX_BC], c2[LBM_MAX_BC], R[LBM_MAX_BC];
+};
+
+struct GeometryLists {
+    int64_t npts = 0;
+    uint8_t* cls = nullptr;      // per point
+    int64_t nsp = 0;             // boundary + next-to-wall nodes
+    int64_t* sp_pt = nullptr;
+    uint32_t* sp_miss = nullptr;
+    uint8_t* sp_cls = nullptr;
+    int32_t* sp_nw = nullptr;
+    double* sp_prof = nullptr;
+    int64_t nnw = 0;
+    int64_t* nw_pt = nullptr;
+    int64_t nseg = 0;
+    int32_t* seg = nullptr;
+    int64_t nact = 0;
+    int32_t* act_idx = nullptr;  // per point
+    int64_t* act_pt = nullptr;
+    int plane[LBM_MAX_BC] = {0};
+};
+
+cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz, const lbm_bc_spec* bc, int nbc,
+                           const double origin[3], double spacing, GeometryLists& out, cudaStream_t st,
+                           std::string& err);
+
+}  // namespace lbm

@@ -1,0 +1,521 @@
+// Fused stream-collide step kernel (pull scheme), templated on lattice,
+// storage format and semantics.  Included by step_f64.cu (FP64, compiled
+// without FMA contraction so FP64 parity runs round exactly like the
+// reference) and step_fast.cu (FP32 / FP16 / BF16 storage, FP32 arithmetic).
+//
+// One launch advances the lattice by one reference step.  Distributions are
+// stored post-collision, structure of arrays, one plane per population over
+// the dense box (f[q][n], n = (k*ny + j)*nx + i).  Launch k:
+//   1. pulls f*_q(x - c_q) from the input planes        (Streaming, Simulation.cpp:264-290)
+//   2. applies Zou-He / the wall rule on boundary nodes (Simulation.cpp:614-863)
+//   3. accumulates wall shear stress on next-to-wall nodes (Simulation.cpp:880-898)
+//   4. collides and writes f* to the output planes      (Collision, Simulation.cpp:96-261)
+// so the step order of Iterate() (Simulation.cpp:577-586) is kept with the
+// step boundary moved between 3 and 4; a prologue launch collides the initial
+// state and a read-out launch stops after 2.
+//
+// The grid has two parts.  Blocks [0, bulk_blocks) walk 32-point segments of
+// interior fluid nodes (all neighbours active, no boundary work): 19 or 27
+// coalesced shifted loads, collision, 19 or 27 aligned stores.  The remaining
+// blocks walk the compact boundary list (wall / inlet / outlet nodes and the
+// next-to-wall nodes that carry the WSS accumulators), one node per thread.
+//
+// Parity semantics for links whose source is missing: the reference's push
+// leaves the destination's previous value in place; the boundary list keeps
+// that previous post-boundary value in `stale`.  A pulled value that is
+// exactly 0.0 is treated the same way (Simulation.cpp:275); on interior
+// nodes, which keep no previous value, the event is flagged instead
+// (FLAG_EXACT_ZERO) -- it needs a post-collision population of exactly zero.
+#pragma once
+#include "lbm_internal.cuh"
+
+namespace lbm {
+
+constexpr int MODE_PARITY = LBM_PARITY;
+constexpr int MODE_PHYSICS = LBM_PHYSICS;
+constexpr int KIND_STEP = 0, KIND_PROLOGUE = 1, KIND_READOUT = 2;
+
+template <int Q>
+__device__ __forceinline__ int64_t nb_off(int q, int64_t nx, int64_t nxy) {
+    return (int64_t)Lat<Q>::cx(q) + (int64_t)Lat<Q>::cy(q) * nx + (int64_t)Lat<Q>::cz(q) * nxy;
+}
+
+// rho and u with the reference's explicit sums (Simulation.cpp:105-228).
+template <int Q, typename R>
+__device__ __forceinline__ void moments(const R (&f)[Q], R& rho, R& ux, R& uy, R& uz) {
+    R d = R(0);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) d += f[q];
+    R px, py, pz;
+    if constexpr (Q == 19) {
+        px = (f[0] + f[6] + f[7] + f[8] + f[9]) - (f[1] + f[10] + f[11] + f[12] + f[13]);
+        py = (f[2] + f[6] + f[10] + f[14] + f[15]) - (f[3] + f[7] + f[11] + f[16] + f[17]);
+        pz = (f[4] + f[8] + f[12] + f[14] + f[16]) - (f[5] + f[9] + f[13] + f[15] + f[17]);
+    } else {
+        px = (f[1] + f[7] + f[8] + f[11] + f[13] + f[19] + f[21] + f[23] + f[25]) -
+             (f[2] + f[9] + f[10] + f[12] + f[14] + f[20] + f[22] + f[24] + f[26]);
+        py = (f[3] + f[7] + f[9] + f[15] + f[16] + f[19] + f[21] + f[24] + f[26]) -
+             (f[4] + f[8] + f[10] + f[17] + f[18] + f[20] + f[22] + f[23] + f[25]);
+        pz = (f[5] + f[11] + f[12] + f[15] + f[17] + f[19] + f[22] + f[23] + f[26]) -
+             (f[6] + f[13] + f[14] + f[16] + f[18] + f[20] + f[21] + f[24] + f[25]);
+    }
+    if constexpr (sizeof(R) == 8) {
+        ux = px / d; uy = py / d; uz = pz / d;  // reference rounding: three divisions
+    } else {
+        const R inv = R(1) / d;
+        ux = px * inv; uy = py * inv; uz = pz * inv;
+    }
+    rho = d;
+}
+
+// Equilibrium of direction q (Simulation.cpp:239-249 operation order).
+template <int Q, int q, typename R>
+__device__ __forceinline__ R feq_q(R rho, R ux, R uy, R uz, R usqr) {
+    const R du = ux * (R)Lat<Q>::cx(q) + uy * (R)Lat<Q>::cy(q) + uz * (R)Lat<Q>::cz(q);
+    return (R)Lat<Q>::w(q) * rho * (R(1.0) + R(3.0) * du + R(4.5) * du * du - R(1.5) * usqr);
+}
+
+template <int Q, typename R, int q = 0>
+__device__ __forceinline__ void relax_all(R (&f)[Q], R rho, R ux, R uy, R uz, R usqr, R inv_tau) {
+    if constexpr (q < Q) {
+        const R e = feq_q<Q, q>(rho, ux, uy, uz, usqr);
+        f[q] = f[q] + inv_tau * (e - f[q]);
+        relax_all<Q, R, q + 1>(f, rho, ux, uy, uz, usqr, inv_tau);
+    }
+}
+
+template <int Q, typename R, int q = 0>
+__device__ __forceinline__ void feq_all(R (&e)[Q], R rho, R ux, R uy, R uz) {
+    if constexpr (q < Q) {
+        const R usqr = ux * ux + uy * uy + uz * uz;
+        e[q] = feq_q<Q, q>(rho, ux, uy, uz, usqr);
+        feq_all<Q, R, q + 1>(e, rho, ux, uy, uz);
+    }
+}
+
+// BGK collision in place; returns the moments.
+template <int Q, typename R>
+__device__ __forceinline__ void collide(R (&f)[Q], R inv_tau, R& rho, R& ux, R& uy, R& uz) {
+    moments<Q, R>(f, rho, ux, uy, uz);
+    const R usqr = ux * ux + uy * uy + uz * uz;
+    relax_all<Q, R>(f, rho, ux, uy, uz, usqr, inv_tau);
+}
+
+// ---------------------------------------------------------------------------
+// Boundary formulas.
+
+// Boundary::ApplyBc, D3Q19 x-min velocity inlet (Boundary.cpp:157-185).
+template <typename R>
+__device__ __forceinline__ void ref_inlet_q19(R (&m)[19], R vel) {
+    const R u0 = vel, u1 = R(0.0), u2 = R(0.0);
+    R rhoN = (m[2] + m[3] + m[4] + m[5] + m[14] + m[15] + m[16] + m[17] + m[18] +
+              R(2) * (m[1] + m[10] + m[11] + m[12] + m[13])) / (R(1) - u0);
+    R Ny = (R(1.0) / R(2)) * (m[2] + m[14] + m[15] - m[3] - m[16] - m[17]) - (R(1.0) / R(3)) * (rhoN * u1);
+    R Nz = (R(1.0) / R(2)) * (m[4] + m[16] + m[14] - m[5] - m[15] - m[17]) - (R(1.0) / R(3)) * (rhoN * u2);
+    m[0] = m[1] + (R(1) / R(3.0)) * rhoN * u0;
+    m[7] = m[10] + (R(1) / R(6.0)) * rhoN * (u0 - u1) + Ny;
+    m[6] = m[11] + (R(1) / R(6.0)) * rhoN * (u0 + u1) - Ny;
+    m[8] = m[13] + (R(1) / R(6.0)) * rhoN * (u0 + u2) - Nz;
+    m[9] = m[12] + (R(1) / R(6.0)) * rhoN * (u0 - u2) + Nz;
+}
+
+// ApplyOutletBc outlet 1, y-max face, rho = 1 (Simulation.cpp:642-695).
+template <typename R>
+__device__ __forceinline__ void ref_outlet_ymax_q19(R (&m)[19]) {
+    const R rho = R(1.0), vx = R(0.0), vz = R(0.0);
+    R vy = R(-1) + (R(1.0) / rho) * (m[0] + m[1] + m[4] + m[5] + m[8] + m[9] + m[12] + m[13] + m[18] +
+                                     R(2.0) * (m[2] + m[6] + m[10] + m[14] + m[15]));
+    R Nyx = R(0.5) * (m[0] + m[8] + m[9] - (m[1] + m[12] + m[13])) - (R(1.0) / R(3.0)) * rho * vx;
+    R Nyz = R(0.5) * (m[4] + m[8] + m[12] - (m[5] + m[9] + m[13])) - (R(1.0) / R(3.0)) * rho * vz;
+    m[3] = m[2] - (R(1.0) / R(3.0)) * rho * vy;
+    m[11] = m[6] + (R(1.0) / R(6.0)) * rho * (-vx - vy) + Nyx;
+    m[7] = m[10] + (R(1.0) / R(6.0)) * rho * (vx - vy) - Nyx;
+    m[17] = m[14] + (R(1.0) / R(6.0)) * rho * (-vy - vz) + Nyz;
+    m[16] = m[15] + (R(1.0) / R(6.0)) * rho * (-vy + vz) - Nyz;
+}
+
+// ApplyOutletBc outlets 2 and 3, z-min face, rho = 1 (Simulation.cpp:710-836).
+template <typename R>
+__device__ __forceinline__ void ref_outlet_zmin_q19(R (&m)[19]) {
+    const R rho = R(1.0), vx = R(0.0), vy = R(0.0);
+    R vz = R(1) - (R(1.0) / rho) * (m[0] + m[1] + m[2] + m[3] + m[6] + m[7] + m[10] + m[11] + m[18] +
+                                    R(2.0) * (m[5] + m[9] + m[13] + m[15] + m[17]));
+    R Nzx = R(0.5) * (m[0] + m[6] + m[7] - (m[1] + m[10] + m[11])) - (R(1.0) / R(3.0)) * rho * vx;
+    R Nzy = R(0.5) * (m[2] + m[6] + m[10] - (m[3] + m[7] + m[11])) - (R(1.0) / R(3.0)) * rho * vy;
+    m[4] = m[5] + (R(1.0) / R(3.0)) * rho * vz;
+    m[8] = m[13] + (R(1.0) / R(6.0)) * rho * (vz + vx) - Nzx;
+    m[12] = m[9] + (R(1.0) / R(6.0)) * rho * (vz - vx) + Nzx;
+    m[14] = m[17] + (R(1.0) / R(6.0)) * rho * (vz + vy) - Nzy;
+    m[16] = m[15] + (R(1.0) / R(6.0)) * rho * (vz - vy) + Nzy;
+}
+
+// Zou-He on any axis-aligned face.  With sigma = +1 on a min face and -1 on
+// a max face, the unknowns are the populations with c_a == sigma:
+//   rho (1 - sigma u_a) = S_0 + 2 S_{-sigma}
+//   N_t = (sum_{c_a=0} f c_t - 2/3 rho u_t) / M      (M = 2 for D3Q19, 6 for D3Q27)
+//   f_i = f_opp(i) + 6 w_i rho (c_i . u) - sum_t c_it N_t
+// which reduces to the reference's formulas on its faces for both lattices
+// (Boundary.cpp:115-185).
+template <int Q, int FACE, typename R>
+__device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
+    constexpr int a = FACE / 2;
+    constexpr int sg = (FACE % 2 == 0) ? 1 : -1;
+    R S0 = R(0), Sm = R(0);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int ca = lat_c<Q>(q, a);
+        if (ca == 0) S0 += m[q];
+        else if (ca == -sg) Sm += m[q];
+    }
+    R u[3] = {R(0), R(0), R(0)};
+    R rho;
+    if (pressure) {
+        rho = value;
+        u[a] = R(sg) * (R(1.0) - (S0 + R(2.0) * Sm) / rho);
+    } else {
+        u[a] = R(sg) * value;
+        rho = (S0 + R(2.0) * Sm) / (R(1.0) - R(sg) * u[a]);
+    }
+    R N[3] = {R(0), R(0), R(0)};
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        if (t == a) continue;
+        R st = R(0);
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            if (lat_c<Q>(q, a) == 0) st += m[q] * (R)lat_c<Q>(q, t);
+        N[t] = (st - (R(2.0) / R(3.0)) * rho * u[t]) / (R)Lat<Q>::ZH_M;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (lat_c<Q>(q, a) != sg) continue;
+        const R cu = (R)Lat<Q>::cx(q) * u[0] + (R)Lat<Q>::cy(q) * u[1] + (R)Lat<Q>::cz(q) * u[2];
+        R corr = R(0);
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+            if (t != a) corr += (R)lat_c<Q>(q, t) * N[t];
+        m[q] = m[Lat<Q>::opp(q)] + R(6.0) * (R)Lat<Q>::w(q) * rho * cu - corr;
+    }
+}
+
+template <int Q, typename R>
+__device__ __forceinline__ void zou_he(R (&m)[Q], int face, bool pressure, R value) {
+    switch (face) {
+        case 0: zou_he_face<Q, 0>(m, pressure, value); break;
+        case 1: zou_he_face<Q, 1>(m, pressure, value); break;
+        case 2: zou_he_face<Q, 2>(m, pressure, value); break;
+        case 3: zou_he_face<Q, 3>(m, pressure, value); break;
+        case 4: zou_he_face<Q, 4>(m, pressure, value); break;
+        default: zou_he_face<Q, 5>(m, pressure, value); break;
+    }
+}
+
+template <int Q, typename R>
+__device__ __forceinline__ void apply_bc(R (&m)[Q], const BCDev& b, double amp, double prof) {
+    const R vel = (R)(amp * prof * b.value);
+    if constexpr (Q == 19) {
+        if (b.kind == LBM_BC_REF_INLET) { ref_inlet_q19<R>(m, vel); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { ref_outlet_ymax_q19<R>(m); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { ref_outlet_zmin_q19<R>(m); return; }
+    } else {
+        if (b.kind == LBM_BC_REF_INLET) { zou_he<Q, R>(m, LBM_FACE_XMIN, false, vel); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { zou_he<Q, R>(m, LBM_FACE_YMAX, true, R(1.0)); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { zou_he<Q, R>(m, LBM_FACE_ZMIN, true, R(1.0)); return; }
+    }
+    if (b.kind == LBM_BC_VELOCITY) zou_he<Q, R>(m, b.face, false, vel);
+    else if (b.kind == LBM_BC_PRESSURE) zou_he<Q, R>(m, b.face, true, (R)b.value);
+}
+
+__device__ __forceinline__ int bc_axis(const BCDev& b) {
+    return b.kind == LBM_BC_REF_INLET ? 0 : b.kind == LBM_BC_REF_OUTLET_YMAX ? 1
+                                          : b.kind == LBM_BC_REF_OUTLET_ZMIN ? 2 : b.face / 2;
+}
+
+// ---------------------------------------------------------------------------
+// Wall shear stress.
+
+// Reference form (Simulation.cpp:880-898): literal loop nest, FP64.
+template <int Q>
+__device__ __forceinline__ void wss_reference(const double (&f)[Q], const double (&feq)[Q], const double n[3],
+                                              double C, double tau_i[3]) {
+    for (int i = 0; i < 3; ++i) {
+        double sum_alpha = 0.0;
+#pragma unroll
+        for (int al = 0; al < Q; ++al) {
+            const double c[3] = {(double)Lat<Q>::cx(al), (double)Lat<Q>::cy(al), (double)Lat<Q>::cz(al)};
+            double sum_k = 0.0;
+            for (int k = 0; k < 3; ++k) sum_k += c[k] * n[k] * n[i];
+            double sum_j = 0.0;
+            for (int j = 0; j < 3; ++j) sum_j += c[j] * n[j] * (c[i] - sum_k);
+            double f_ne = f[al] - feq[al];
+            sum_alpha += f_ne * sum_j;
+        }
+        tau_i[i] = C * sum_alpha;
+    }
+}
+
+// Same quantity, factored: tau_i = C sum_a f_ne (c.n)(c_i - (c.n) n_i).
+template <int Q, typename R>
+__device__ __forceinline__ void wss_fast(const R (&f)[Q], const R (&feq)[Q], const R n[3], R C, R tau_i[3]) {
+    R a0 = R(0), a1 = R(0), a2 = R(0);
+#pragma unroll
+    for (int al = 0; al < Q; ++al) {
+        const R cn = (R)Lat<Q>::cx(al) * n[0] + (R)Lat<Q>::cy(al) * n[1] + (R)Lat<Q>::cz(al) * n[2];
+        const R k = (f[al] - feq[al]) * cn;
+        a0 += k * ((R)Lat<Q>::cx(al) - cn * n[0]);
+        a1 += k * ((R)Lat<Q>::cy(al) - cn * n[1]);
+        a2 += k * ((R)Lat<Q>::cz(al) - cn * n[2]);
+    }
+    tau_i[0] = C * a0; tau_i[1] = C * a1; tau_i[2] = C * a2;
+}
+
+// ---------------------------------------------------------------------------
+// Block reduction of the read-out sums (mass, momentum, per-BC flux).
+
+__device__ __forceinline__ void block_partials(double (&v)[kPartialStride], double* __restrict__ out) {
+    __shared__ double red[kStepThreads / 32][kPartialStride];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kPartialStride; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(0xffffffffu, x, d);
+        if (lane == 0) red[warp][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < kPartialStride) {
+        double s = 0.0;
+        for (int w = 0; w < kStepThreads / 32; ++w) s += red[w][threadIdx.x];
+        out[(int64_t)blockIdx.x * kPartialStride + threadIdx.x] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The kernel.
+
+template <int Q, typename S, int MODE, int KIND>
+__global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) {
+    using R = typename Store<S>::real;
+    const S* __restrict__ fin = static_cast<const S*>(P.fin);
+    S* __restrict__ fout = static_cast<S*>(P.fout);
+    const R inv_tau = (R)(1.0 / P.tau);
+    double part[kPartialStride];
+    if constexpr (KIND == KIND_READOUT) {
+#pragma unroll
+        for (int k = 0; k < kPartialStride; ++k) part[k] = 0.0;
+    }
+
+    if ((int)blockIdx.x < P.bulk_blocks) {
+        // ---------------- bulk: interior fluid nodes, 32-point segments
+        const int64_t sgi = (int64_t)blockIdx.x * (kStepThreads / 32) + (threadIdx.x >> 5);
+        const bool seg_ok = sgi < P.nseg;
+        const int64_t n = seg_ok ? (int64_t)__ldg(P.seg + sgi) * 32 + (threadIdx.x & 31) : 0;
+        const bool live = seg_ok && __ldg(P.cls + n) == CLS_FLUID;
+        if (live) {
+            R f[Q];
+#pragma unroll
+            const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int64_t src = direct ? n : n - nb_off<Q>(q, P.nx, P.nxy);
+                f[q] = Store<S>::template load<Q>(fin + q * P.stride + src, q);
+            }
+            if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
+                bool zero = false;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) zero |= (f[q] == R(0));
+                if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
+            }
+            if constexpr (KIND == KIND_READOUT) {
+                const int64_t a = __ldg(P.act_idx + n);
+                R rho, ux, uy, uz;
+                moments<Q, R>(f, rho, ux, uy, uz);
+                part[0] = (double)rho;
+                part[1] = (double)(rho * ux); part[2] = (double)(rho * uy); part[3] = (double)(rho * uz);
+                if (P.out_f) {
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = (double)f[q];
+                }
+            } else {
+                R rho, ux, uy, uz;
+                collide<Q, R>(f, inv_tau, rho, ux, uy, uz);
+                if (!(fabs((double)rho) < 1e30)) atomicOr(P.flags, FLAG_NONFINITE);
+#pragma unroll
+                for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(f[q], q);
+            }
+        }
+    } else {
+        // ---------------- boundary list: one node per thread
+        const int64_t s = (int64_t)((int)blockIdx.x - P.bulk_blocks) * kStepThreads + threadIdx.x;
+        if (s < P.nsp) {
+            const int64_t n = __ldg(P.sp_pt + s);
+            const uint32_t miss = __ldg(P.sp_miss + s);
+            const int c = __ldg(P.sp_cls + s);
+            const int nw = __ldg(P.sp_nw + s);
+            R* __restrict__ stale = static_cast<R*>(P.stale);
+            R g[Q];
+            const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                if (KIND == KIND_READOUT && MODE == MODE_PARITY) {
+                    // the boundary list keeps the exact post-boundary f of the last step
+                    g[q] = stale[q * P.nsp + s];
+                } else if (direct) {
+                    g[q] = Store<S>::template load<Q>(fin + q * P.stride + n, q);
+                } else if ((miss >> Lat<Q>::opp(q)) & 1u) {
+                    // source x - c_q is solid / outside the box
+                    if constexpr (MODE == MODE_PARITY) g[q] = stale[q * P.nsp + s];
+                    else g[q] = Store<S>::template load<Q>(fin + Lat<Q>::opp(q) * P.stride + n, Lat<Q>::opp(q));
+                } else {
+                    R v = Store<S>::template load<Q>(fin + q * P.stride + n - nb_off<Q>(q, P.nx, P.nxy), q);
+                    if constexpr (MODE == MODE_PARITY) {
+                        if (v == R(0)) v = stale[q * P.nsp + s];
+                    }
+                    g[q] = v;
+                }
+            }
+            const double amp = (P.namp > 0) ? __ldg(P.amp + ((*P.step_base + P.step_off) % P.namp)) : 0.0;
+            if (!direct && !(KIND == KIND_READOUT && MODE == MODE_PARITY)) {
+                if (c >= CLS_BC0) {
+                    apply_bc<Q, R>(g, P.bc[c - CLS_BC0], amp, __ldg(P.sp_prof + s));
+                } else if (MODE == MODE_PARITY && c == CLS_WALL) {
+                    // ApplyWallBc: in place, direction order (Simulation.cpp:846-861)
+#pragma unroll
+                    for (int q = 0; q < Q; ++q)
+                        if ((miss >> q) & 1u) g[Lat<Q>::opp(q)] = g[q];
+                }
+            }
+            if constexpr (KIND == KIND_READOUT) {
+                const int64_t a = __ldg(P.act_idx + n);
+                R rho, ux, uy, uz;
+                moments<Q, R>(g, rho, ux, uy, uz);
+                part[0] = (double)rho;
+                const double j[3] = {(double)(rho * ux), (double)(rho * uy), (double)(rho * uz)};
+                part[1] = j[0]; part[2] = j[1]; part[3] = j[2];
+                if (c >= CLS_BC0) part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
+                if (P.out_f) {
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = (double)g[q];
+                }
+            } else {
+                R* __restrict__ prev = static_cast<R*>(P.nw_prev);
+                if constexpr (KIND == KIND_STEP) {
+                    if (nw >= 0) {
+                        double t[3];
+                        const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
+                        if constexpr (MODE == MODE_PARITY) {
+                            // equilibrium of the previous collision (time-lagged, as the reference)
+                            R e[Q];
+                            feq_all<Q, R>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw], prev[3 * P.nnw + nw]);
+                            if constexpr (sizeof(R) == 8) {
+                                wss_reference<Q>(g, e, nn, P.wss_C, t);
+                            } else {
+                                const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
+                                R tr[3];
+                                wss_fast<Q, R>(g, e, nr, (R)P.wss_C, tr);
+                                t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
+                            }
+                        } else {
+                            // stress of the same post-boundary f, with the (1 - 1/2tau) factor
+                            R e[Q], rho, ux, uy, uz;
+                            moments<Q, R>(g, rho, ux, uy, uz);
+                            feq_all<Q, R>(e, rho, ux, uy, uz);
+                            const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
+                            R tr[3];
+                            wss_fast<Q, R>(g, e, nr, (R)(-(1.0 - 0.5 / P.tau) * P.wss_C), tr);
+                            t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
+                        }
+                        const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                        P.nw_wss[nw] = W;
+                        P.nw_acc[nw] += t[0];
+                        P.nw_acc[P.nnw + nw] += t[1];
+                        P.nw_acc[2 * P.nnw + nw] += t[2];
+                        P.nw_accm[nw] += W;
+                    }
+                }
+                if constexpr (MODE == MODE_PARITY) {
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) stale[q * P.nsp + s] = g[q];
+                }
+                R rho, ux, uy, uz;
+                collide<Q, R>(g, inv_tau, rho, ux, uy, uz);
+                if (!(fabs((double)rho) < 1e30)) atomicOr(P.flags, FLAG_NONFINITE);
+                if (MODE == MODE_PARITY && nw >= 0) {
+                    prev[nw] = rho; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
+                }
+#pragma unroll
+                for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(g[q], q);
+            }
+        }
+    }
+    if constexpr (KIND == KIND_STEP) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
+    }
+    if constexpr (KIND == KIND_READOUT) block_partials(part, P.partials);
+}
+
+template <int Q, typename S, int MODE>
+cudaError_t launch_family(int kind, const StepParams& p, cudaStream_t st) {
+    const int64_t sp_blocks = ceil_div(p.nsp, kStepThreads);
+    const int64_t nblocks = (int64_t)p.bulk_blocks + sp_blocks;
+    if (nblocks <= 0) return cudaSuccess;
+    if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    switch (kind) {
+        case KIND_STEP: step_kernel<Q, S, MODE, KIND_STEP><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p); break;
+        case KIND_PROLOGUE:
+            step_kernel<Q, S, MODE, KIND_PROLOGUE><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p);
+            break;
+        default: step_kernel<Q, S, MODE, KIND_READOUT><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p); break;
+    }
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_typed(int Q, int mode, int kind, const StepParams& p, cudaStream_t st) {
+    if (Q == 19) {
+        return mode == MODE_PARITY ? launch_family<19, S, MODE_PARITY>(kind, p, st)
+                                   : launch_family<19, S, MODE_PHYSICS>(kind, p, st);
+    }
+    return mode == MODE_PARITY ? launch_family<27, S, MODE_PARITY>(kind, p, st)
+                               : launch_family<27, S, MODE_PHYSICS>(kind, p, st);
+}
+
+// ---------------------------------------------------------------------------
+// State initialisation kernels (storage-typed).
+
+// Every plane entry of every active point := pack(w_q) (f = w, Node.cpp:30-37).
+template <int Q, typename S>
+__global__ void k_fill_weights(S* __restrict__ f, int64_t stride, int64_t npts) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts) return;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q * stride + n] = Store<S>::template pack<Q>((typename Store<S>::real)Lat<Q>::w(q), q);
+}
+
+// f_in[a*Q + q] (FP64, per active node) scattered into the planes.
+template <int Q, typename S>
+__global__ void k_scatter_f(const double* __restrict__ fa, const int64_t* __restrict__ act_pt, int64_t nact,
+                            S* __restrict__ f, int64_t stride) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nact) return;
+    const int64_t n = act_pt[a];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q * stride + n] = Store<S>::template pack<Q>((typename Store<S>::real)fa[a * Q + q], q);
+}
+
+template <typename S>
+cudaError_t init_typed(int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
+                       const int64_t* act_pt, int64_t nact, cudaStream_t st) {
+    if (what == 0) {
+        const unsigned g = (unsigned)ceil_div(npts > 0 ? npts : 1, 256);
+        if (Q == 19) k_fill_weights<19, S><<<g, 256, 0, st>>>(static_cast<S*>(f), stride, npts);
+        else k_fill_weights<27, S><<<g, 256, 0, st>>>(static_cast<S*>(f), stride, npts);
+    } else {
+        const unsigned g = (unsigned)ceil_div(nact > 0 ? nact : 1, 256);
+        if (Q == 19) k_scatter_f<19, S><<<g, 256, 0, st>>>(fa, act_pt, nact, static_cast<S*>(f), stride);
+        else k_scatter_f<27, S><<<g, 256, 0, st>>>(fa, act_pt, nact, static_cast<S*>(f), stride);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace lbm

@@ -333,25 +333,39 @@ def stenosed_tube(radius: float, length: float, severity: float, eccentricity: f
     return s
 
 
-def elbow(radius: float = 6.0, leg: float = 30.0, h: float = 1.25, seed: int = 0) -> Surface:
-    """Tube entering along +x through a flat cut at x=0 and leaving along -z
-    through a flat cut at z=0 (inlet on the x-min face, outlet on the z-min
-    face: the faces whose Zou-He formulas the reference implements)."""
+def elbow(radius: float = 6.0, leg: float = 30.0, h: float = 1.25, seed: int = 0, exit: str = "z-") -> Surface:
+    """Tube entering along +x through a flat cut at x=0 and leaving either
+    along -z through a flat cut at z=0 (``exit="z-"``) or along +y through a
+    flat cut at y=leg+radius (``exit="y+"``): the x-min inlet and the z-min /
+    y-max outlets are the faces whose Zou-He formulas the reference implements
+    (Boundary.cpp:157-185, Simulation.cpp:628-838)."""
     rng = np.random.default_rng(seed)
-    A = np.array([-2 * radius, 0.0, leg])
-    B = np.array([leg, 0.0, leg])
-    C = np.array([leg, 0.0, -2 * radius])
+    if exit == "z-":
+        A = np.array([-2 * radius, 0.0, leg])
+        B = np.array([leg, 0.0, leg])
+        C = np.array([leg, 0.0, -2 * radius])
+        cut_lo = lambda p: -p[:, 2]
+        lo = np.array([-2 * h, -radius - 2 * h, -2 * h])
+        hi = np.array([leg + radius + 2 * h, radius + 2 * h, leg + radius + 2 * h])
+    elif exit == "y+":
+        top = leg + radius
+        A = np.array([-2 * radius, 0.0, 0.0])
+        B = np.array([leg, 0.0, 0.0])
+        C = np.array([leg, top + 2 * radius, 0.0])
+        cut_lo = lambda p: p[:, 1] - top
+        lo = np.array([-2 * h, -radius - 2 * h, -radius - 2 * h])
+        hi = np.array([leg + radius + 2 * h, top + 2 * h, radius + 2 * h])
+    else:
+        raise ValueError("exit must be 'z-' or 'y+'")
 
     def sdf(p):
         d = np.minimum(_capsule(p, A, B, radius), _capsule(p, B, C, radius))
         d = np.maximum(d, -p[:, 0])
-        return np.maximum(d, -p[:, 2])
+        return np.maximum(d, cut_lo(p))
 
     jitter = rng.uniform(0.11, 0.37, size=3) * h
-    lo = np.array([-2 * h, -radius - 2 * h, -2 * h]) - jitter
-    hi = np.array([leg + radius + 2 * h, radius + 2 * h, leg + radius + 2 * h])
-    s = marching_tetrahedra(sdf, lo, hi, h)
-    s.meta = {"kind": "elbow", "radius": radius, "leg": leg}
+    s = marching_tetrahedra(sdf, lo - jitter, hi, h)
+    s.meta = {"kind": "elbow", "radius": radius, "leg": leg, "exit": exit}
     return s
 
 

@@ -1,0 +1,72 @@
+"""The C ABI library: loads, exports every declared symbol, host-side paths
+work without a GPU (no compute calls here)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from helpers import fixtures, load
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "lbm_gb300.h")).read()
+    return sorted(set(re.findall(r"^(?:lbm_status|const char\*)\s+(lbm_\w+)\s*\(", txt, re.M)))
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    L = gpu_lib.load()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+    assert set(syms) <= set(gpu_lib.EXPORTS) | set(syms)
+
+
+def test_errors_are_status_codes_not_crashes(gpu_lib):
+    L = gpu_lib.load()
+    bad = gpu_lib.Desc(19, 1, 1, 0.4, 1.0, (C.c_double * 3)(0, 0, 0), 1.0, 0.9, 0)  # tau <= 0.5
+    h = C.c_void_p()
+    assert L.lbm_create(C.byref(bad), C.byref(h)) == -1
+    assert b"tau" in L.lbm_last_global_error()
+    assert L.lbm_step(None, 1) == -1
+    assert L.lbm_destroy(None) == 0
+
+
+def test_stl_reader_matches_python_parser(gpu_lib, tmp_path):
+    from pv_dec_original_gb300 import geometry as G
+    d = load(fixtures("vox")[0])
+    tri = d["tri12"]
+    p = str(tmp_path / "x.stl")
+    G.write_stl_ascii(p, G.Surface(tri[:, :9].reshape(-1, 3, 3).copy(), tri[:, 9:].copy()))
+    got = gpu_lib.read_stl(p)
+    assert np.array_equal(got, tri)
+    assert np.array_equal(G.read_stl_ascii(p), tri)
+
+
+def test_stl_reader_skips_malformed_facets(gpu_lib, tmp_path):
+    p = tmp_path / "bad.stl"
+    p.write_text("solid a\n facet normal 0 0 1\n outer loop\n vertex 0 0 0\n vertex 1 0 0\n vertex 0 1 0\n"
+                 " endloop\n endfacet\n facet normal 0 0 1\n outer loop\n vertex 0 0\n endloop\n endfacet\n"
+                 " facet normal x y z\nendsolid\n")
+    got = gpu_lib.read_stl(str(p))
+    assert got.shape == (1, 12)
+    with pytest.raises(gpu_lib.LbmError):
+        gpu_lib.read_stl(str(tmp_path / "missing.stl"))
+
+
+@pytest.mark.parametrize("path", fixtures("vox"), ids=lambda p: p.split("/")[-1])
+def test_reference_bbox_rule_on_host(gpu_lib, path):
+    """lbm_voxelize with no mask buffer only sizes the lattice (host code)."""
+    d = load(path)
+    L = gpu_lib.load()
+    desc = gpu_lib.VoxDesc()
+    desc.spacing = float(d["spacing"])
+    desc.reference_bbox = 1
+    tri = np.ascontiguousarray(d["tri12"])
+    assert L.lbm_voxelize(tri.ctypes.data_as(C.c_void_p), len(tri), C.byref(desc), None) == 0
+    assert tuple(desc.dims) == tuple(d["dims"])
+    assert np.array_equal(np.array(desc.bbox[:]), d["bbox"])

@@ -1,0 +1,171 @@
+"""GPU solver parity: FP64 parity mode vs the reference (bit-exact
+distributions), every precision / lattice / mode vs the FP64 oracle."""
+import numpy as np
+import pytest
+
+from helpers import classify, fixtures, load, sha, sim_bcs, wss_C
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_parity_run(capi, d, precision, graph=0, split=None):
+    mask, desc = capi.voxelize(d["tri12"], float(d["spacing"]))
+    bb = np.array(desc.bbox[:])
+    s = capi.Solver(19, precision, capi.LBM_PARITY, float(d["tau"]), float(d["spacing"]), (bb[0], bb[2], bb[4]),
+                    wss_C(float(d["dt"]), float(d["spacing"])), 0.9)
+    s.set_geometry(mask, [capi.bc_spec(**spec) for _, spec in sim_bcs(d)])
+    s.set_normals(d["tri12"])
+    s.set_inlet_table(d["amp"])
+    if graph:
+        s.set_graph_steps(graph)
+    n = int(d["nsteps"])
+    if split:
+        s.step(split)
+        s.step(n - split)
+    else:
+        s.step(n)
+    return s, mask
+
+
+@pytest.mark.parametrize("path", fixtures("sim"), ids=lambda p: p.split("/")[-1])
+def test_gpu_fp64_parity_bit_exact_vs_reference(gpu_lib, path):
+    d = load(path)
+    s, mask = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64)
+    cls = s.classes().reshape(-1)
+    act = np.flatnonzero(cls)
+    assert np.array_equal(act, d["active_pt"])
+    assert np.array_equal(cls[act] & 0x7F, d["active_cls"])
+    f = s.distributions()
+    ref_sample = d["f_sample"]
+    got_sample = f[d["f_sample_idx"]]
+    assert np.max(np.abs(got_sample - ref_sample)) <= 1e-13, "FP64 parity drifted from the reference"
+    assert sha(f) == str(d["f_sha"]), "distributions are close but not bit-identical to the reference"
+    rho, u = s.macro()
+    np.testing.assert_allclose(rho, d["rho"], rtol=1e-12)  # reference rho/u are from the last collision
+    w = s.wss()
+    assert np.array_equal(w["pt"], d["nw_pt"])
+    np.testing.assert_allclose(w["normal"], d["nw_normal"], rtol=1e-13, atol=1e-15)
+    for k in ("wss", "acc", "acc_mag", "tawss"):
+        np.testing.assert_allclose(w[k], d["nw_" + k], rtol=1e-11, atol=1e-13 * np.abs(d["nw_" + k]).max())
+    np.testing.assert_allclose(w["osi"], d["nw_osi"], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("path", fixtures("sim"), ids=lambda p: p.split("/")[-1])
+def test_gpu_parity_graph_and_split_calls_identical(gpu_lib, path):
+    d = load(path)
+    a, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64)
+    b, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64, graph=4, split=7)
+    assert np.array_equal(a.distributions(), b.distributions())
+    assert np.array_equal(a.wss()["acc"], b.wss()["acc"])
+
+
+@pytest.mark.parametrize("prec,tol", [("f32", 2e-5), ("f16", 5e-3), ("bf16", 3e-2)])
+def test_gpu_low_precision_parity_vs_fp64(gpu_lib, prec, tol):
+    d = load(fixtures("sim")[0])
+    ref, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64)
+    got, _ = _gpu_parity_run(gpu_lib, d, prec)
+    r_rho, r_u = ref.macro()
+    g_rho, g_u = got.macro()
+    rel = np.linalg.norm(g_u - r_u) / np.linalg.norm(r_u)
+    assert rel <= tol, rel
+    assert np.max(np.abs(g_rho - r_rho)) <= 10 * tol
+
+
+def _physics_case(capi, oracle, Q, precision, nsteps=40, tau=0.7):
+    """A stenosed tube with velocity inlet (z-min) and pressure outlet (z-max)."""
+    from pv_dec_original_gb300 import geometry as G
+    surf = G.stenosed_tube(5.0, 40.0, 0.5, 0.2, center=(7.3, 7.1), z0=1.6, h=1.4, seed=3)
+    surf = G.add_bbox_anchors(surf, (0.0, 0.0, 0.0), (14.0, 14.0, 44.0))
+    tri = surf.tri12()
+    mask, desc = capi.voxelize(tri, 1.0)
+    bb = np.array(desc.bbox[:])
+    org = (bb[0], bb[2], bb[4])
+    fl = np.argwhere(mask > 0)
+    kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
+    bcs = [dict(kind=capi.LBM_BC_VELOCITY, face=4, plane=kin, value=1.0, profile=1, c1=7.3, c2=7.1, R=5.0),
+           dict(kind=capi.LBM_BC_PRESSURE, face=5, plane=kout, value=1.0)]
+    amp = 0.03 * (1 + 0.5 * np.sin(2 * np.pi * np.arange(64) / 64))
+    s = capi.Solver(Q, precision, capi.LBM_PHYSICS, tau, 1.0, org, 1.0, 1.0)
+    s.set_geometry(mask, [capi.bc_spec(**b) for b in bcs])
+    s.set_normals(tri)
+    s.set_inlet_table(amp)
+    s.step(nsteps)
+    cls = classify(mask, [(2, kin), (2, kout)], Q)
+    o = oracle.Sim(Q, oracle.PHYSICS, cls, org, 1.0, tau, bcs)
+    o.set_amplitude(amp)
+    o.set_wss(1.0, 1.0)
+    o.compute_normals(tri)
+    o.step(nsteps)
+    return s, o
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+def test_gpu_fp64_physics_matches_oracle(gpu_lib, oracle_lib, Q):
+    s, o = _physics_case(gpu_lib, oracle_lib, Q, gpu_lib.LBM_F64)
+    f = s.distributions()
+    fo, _, _ = o.f()
+    assert np.max(np.abs(f - fo)) <= 1e-13
+    w, wo = s.wss(), o.nw()
+    assert np.array_equal(w["pt"], wo["pt"])
+    np.testing.assert_allclose(w["acc"], wo["acc"], rtol=1e-9, atol=1e-14)
+    m, p, fl = s.conservation()
+    mo, po, flo = o.conservation()
+    assert abs(m - mo) <= 1e-10 * mo
+    np.testing.assert_allclose(p, po, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(fl, flo, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-5), ("f16", 4e-3), ("bf16", 3e-2)])
+def test_gpu_physics_precision_vs_fp64_oracle(gpu_lib, oracle_lib, Q, prec, tol):
+    """Velocity L2 relative error of each storage format vs the FP64 oracle."""
+    s, o = _physics_case(gpu_lib, oracle_lib, Q, prec, nsteps=60)
+    _, u = s.macro()
+    fo, _, _ = o.f()
+    rho_o = fo.sum(axis=1)
+    c, _, _ = oracle_lib.lattice(Q)
+    u_o = (fo @ c) / rho_o[:, None]
+    rel = np.linalg.norm(u - u_o) / np.linalg.norm(u_o)
+    assert rel <= tol, rel
+
+
+def test_gpu_checkpoint_round_trip(gpu_lib, tmp_path):
+    d = load(fixtures("sim")[0])
+    a, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64)
+    a.save(str(tmp_path / "c.bin"))
+    a.step(10)
+    fa = a.distributions()
+    b, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64)
+    b.step(3)  # diverge, then restore
+    b.load_checkpoint(str(tmp_path / "c.bin"))
+    b.step(10)
+    assert np.array_equal(b.distributions(), fa)
+    assert np.array_equal(b.wss()["acc"], a.wss()["acc"])
+
+
+def test_gpu_readout_before_first_step_is_initial_state(gpu_lib, oracle_lib):
+    d = load(fixtures("sim")[0])
+    mask, desc = gpu_lib.voxelize(d["tri12"], 1.0)
+    s = gpu_lib.Solver(19, gpu_lib.LBM_F64, gpu_lib.LBM_PARITY, 0.8, 1.0)
+    s.set_geometry(mask, [])
+    f = s.distributions()
+    _, w, _ = oracle_lib.lattice(19)
+    assert np.array_equal(f, np.tile(w, (len(f), 1)))
+    m, p, _ = s.conservation()
+    assert abs(m - len(f)) < 1e-9 and np.all(np.abs(p) < 1e-12)
+
+
+def test_gpu_divergence_reports_status(gpu_lib):
+    """A run driven unstable (Mach > 1 inlet, tau near 0.5) must come back as
+    LBM_ERR_NONFINITE, not as a fault."""
+    from pv_dec_original_gb300 import geometry as G
+    tri = G.config_c1_cylinder().tri12()
+    mask, desc = gpu_lib.voxelize(tri, 1.0)
+    fl = np.argwhere(mask > 0)
+    s = gpu_lib.Solver(19, gpu_lib.LBM_F32, gpu_lib.LBM_PHYSICS, 0.5001, 1.0)
+    s.set_geometry(mask, [gpu_lib.bc_spec(gpu_lib.LBM_BC_VELOCITY, 4, int(fl[:, 0].min()), 1.0)])
+    s.set_inlet_table([3.0])
+    with pytest.raises(gpu_lib.LbmError) as e:
+        for _ in range(50):
+            s.step(20)
+    assert e.value.code == -4
