@@ -245,12 +245,12 @@ int64_t oracle_voxelize(const double* tri, int64_t ntri, const double* bb, const
                 const double* T = tri + 12 * t;
                 double x0 = dmin(dmin(T[0], T[3]), T[6]) - m, x1 = dmax(dmax(T[0], T[3]), T[6]) + m;
                 double y0 = dmin(dmin(T[1], T[4]), T[7]) - m, y1 = dmax(dmax(T[1], T[4]), T[7]) + m;
-                int i0 = (int)floor((x0 - org[0]) / s) - 1, i1 = (int)ceil((x1 - org[0]) / s) + 1;
-                int j0 = (int)floor((y0 - org[1]) / s) - 1, j1 = (int)ceil((y1 - org[1]) / s) + 1;
-                if (i0 < 0) i0 = 0;
-                if (j0 < 0) j0 = 0;
-                if (i1 > nx - 1) i1 = nx - 1;
-                if (j1 > ny - 1) j1 = ny - 1;
+                double fi0 = dmax(floor((x0 - org[0]) / s) - 1.0, 0.0);
+                double fi1 = dmin(ceil((x1 - org[0]) / s) + 1.0, nx - 1.0);
+                double fj0 = dmax(floor((y0 - org[1]) / s) - 1.0, 0.0);
+                double fj1 = dmin(ceil((y1 - org[1]) / s) + 1.0, ny - 1.0);
+                if (!(fi0 <= fi1) || !(fj0 <= fj1)) continue;
+                int i0 = (int)fi0, i1 = (int)fi1, j0 = (int)fj0, j1 = (int)fj1;
                 for (int j = j0; j <= j1; ++j) {
                     if (coly[j] < y0 || coly[j] > y1) continue;
                     for (int i = i0; i <= i1; ++i) {

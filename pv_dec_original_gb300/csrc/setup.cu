@@ -247,7 +247,11 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
                            std::string& err) {
     const int64_t npts = (int64_t)nx * ny * nz;
     out.npts = npts;
-    SETUP_CHECK(cudaMallocAsync(&out.cls, npts, st));
+    // padded to whole 32-point segments: the bulk kernel reads the class
+    // byte of every lane of a segment
+    const int64_t npad = ceil_div(npts, 32) * 32;
+    SETUP_CHECK(cudaMallocAsync(&out.cls, npad, st));
+    SETUP_CHECK(cudaMemsetAsync(out.cls, 0, npad, st));
     if (Q == 19) k_boundary<19><<<blocks(npts), 256, 0, st>>>(d_mask, nx, ny, nz, out.cls);
     else k_boundary<27><<<blocks(npts), 256, 0, st>>>(d_mask, nx, ny, nz, out.cls);
     SETUP_CHECK(cudaGetLastError());

@@ -374,9 +374,14 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                     g[q] = v;
                 }
             }
-            const double amp = (P.namp > 0) ? __ldg(P.amp + ((*P.step_base + P.step_off) % P.namp)) : 0.0;
             if (!direct && !(KIND == KIND_READOUT && MODE == MODE_PARITY)) {
                 if (c >= CLS_BC0) {
+                    double amp = 0.0;
+                    if (P.namp > 0) {
+                        int64_t t = (*P.step_base + P.step_off) % P.namp;
+                        if (t < 0) t += P.namp;
+                        amp = __ldg(P.amp + t);
+                    }
                     apply_bc<Q, R>(g, P.bc[c - CLS_BC0], amp, __ldg(P.sp_prof + s));
                 } else if (MODE == MODE_PARITY && c == CLS_WALL) {
                     // ApplyWallBc: in place, direction order (Simulation.cpp:846-861)

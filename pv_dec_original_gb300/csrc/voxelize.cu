@@ -153,10 +153,11 @@ __global__ void tri_bin(int64_t ntri, const TriBox* __restrict__ box, const uint
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntri || status[t] != 1) return;
     TriBox b = box[t];
-    int i0 = (int)floor((b.x0 - ox) / s) - 1, i1 = (int)ceil((b.x1 - ox) / s) + 1;
-    int j0 = (int)floor((b.y0 - oy) / s) - 1, j1 = (int)ceil((b.y1 - oy) / s) + 1;
-    i0 = max(i0, 0); j0 = max(j0, 0);
-    i1 = min(i1, nx - 1); j1 = min(j1, ny - 1);
+    // clamp in FP64 before converting: margins can be far outside int range
+    const double fi0 = fmax(floor((b.x0 - ox) / s) - 1.0, 0.0), fi1 = fmin(ceil((b.x1 - ox) / s) + 1.0, nx - 1.0);
+    const double fj0 = fmax(floor((b.y0 - oy) / s) - 1.0, 0.0), fj1 = fmin(ceil((b.y1 - oy) / s) + 1.0, ny - 1.0);
+    if (!(fi0 <= fi1) || !(fj0 <= fj1)) return;
+    const int i0 = (int)fi0, i1 = (int)fi1, j0 = (int)fj0, j1 = (int)fj1;
     for (int j = j0; j <= j1; ++j) {
         double yy = coly[j];
         if (yy < b.y0 || yy > b.y1) continue;
