@@ -50,7 +50,6 @@ struct lbm_handle {
     BCDev bc[LBM_MAX_BC]{};
     int nbc = 0;
     int64_t launches = 0;
-    int bulk_blocks = 0;
     int64_t nblocks = 0;
     double* partials = nullptr;
     double* sums = nullptr;
@@ -129,7 +128,8 @@ void drop_graph(lbm_handle* h) {
 
 void free_geometry(lbm_handle* h) {
     GeometryLists& g = h->g;
-    void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_prof, g.nw_pt, g.seg, g.act_idx, g.act_pt,
+    void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_prof, g.nw_pt, g.act_word, g.sp_of_act,
+                    g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
                     h->partials, h->sums, h->out_f, h->macro};
     for (void* p : ptrs)
@@ -159,12 +159,10 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.nx = h->nx;
     p.ny = h->ny;
     p.nxy = (int64_t)h->nx * h->ny;
-    p.cls = h->g.cls;
-    p.seg = h->g.seg;
-    p.nseg = h->g.nseg;
-    p.bulk_blocks = h->bulk_blocks;
+    p.nact = h->g.nact;
+    p.act_word = h->g.act_word;
+    p.sp_of_act = h->g.sp_of_act;
     p.nsp = h->g.nsp;
-    p.sp_pt = h->g.sp_pt;
     p.sp_miss = h->g.sp_miss;
     p.sp_cls = h->g.sp_cls;
     p.sp_nw = h->g.sp_nw;
@@ -486,7 +484,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     REQUIRE(h, dims[0] > 0 && dims[1] > 0 && dims[2] > 0, LBM_ERR_ARG, "empty lattice");
     REQUIRE(h, nbc >= 0 && nbc <= LBM_MAX_BC && (nbc == 0 || bc), LBM_ERR_ARG, "0..8 boundary conditions");
     const int64_t npts = (int64_t)dims[0] * dims[1] * dims[2];
-    REQUIRE(h, npts < (int64_t)1 << 36, LBM_ERR_ARG, "lattice too large");
+    REQUIRE(h, npts < (int64_t)1 << 31, LBM_ERR_ARG, "lattice too large (more than 2^31 points)");
     for (int b = 0; b < nbc; ++b) {
         REQUIRE(h, bc[b].kind >= LBM_BC_REF_INLET && bc[b].kind <= LBM_BC_PRESSURE, LBM_ERR_ARG, "unknown bc kind");
         REQUIRE(h, bc[b].face >= 0 && bc[b].face <= 5, LBM_ERR_ARG, "face must be 0..5");
@@ -536,11 +534,10 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     CK(h, dalloc(h, &h->nw_wss, sizeof(double) * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_acc, sizeof(double) * 3 * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_accm, sizeof(double) * (h->g.nnw + 1)));
-    h->bulk_blocks = (int)ceil_div(h->g.nseg, kStepThreads / 32);
-    h->nblocks = h->bulk_blocks + ceil_div(h->g.nsp, kStepThreads);
+    h->nblocks = ceil_div(h->g.nact, kStepThreads);
     CK(h, dalloc(h, &h->partials, sizeof(double) * kPartialStride * (h->nblocks + 1)));
     CK(h, dalloc(h, &h->sums, sizeof(double) * kPartialStride));
-    h->geo_bytes += h->npts * 5 + h->g.nsp * 25 + h->g.nseg * 4 + h->g.nact * 8;  // lists from setup
+    h->geo_bytes += h->npts * 5 + h->g.nsp * 25 + h->g.nact * 16;  // lists from setup
     h->has_geo = true;
     // counts
     std::vector<uint8_t> spc(h->g.nsp);
@@ -551,7 +548,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     c.active = h->g.nact;
     c.next_to_wall = h->g.nnw;
     c.special = h->g.nsp;
-    c.segments = h->g.nseg;
+    c.segments = ceil_div(h->g.nact, 32);
     int64_t bnd = 0;
     for (uint8_t v : spc) {
         if (v == CLS_WALL) c.wall++;
@@ -782,7 +779,7 @@ lbm_status lbm_get_conservation(lbm_handle* h, double* mass, double* mom3, doubl
     double s[kPartialStride];
     CK(h, cudaMemcpyAsync(s, h->sums, sizeof(s), cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
-    if (mass) *mass = s[0];
+    if (mass) *mass = (double)h->g.nact + s[0];  // the kernel sums rho - 1
     if (mom3) { mom3[0] = s[1]; mom3[1] = s[2]; mom3[2] = s[3]; }
     if (flux)
         for (int b = 0; b < h->nbc; ++b) flux[b] = s[4 + b];

@@ -30,13 +30,12 @@ struct StepParams {
     int64_t stride;        // elements per population plane
     int nx, ny;
     int64_t nxy;
-    const uint8_t* cls;    // per point
-    const int32_t* seg;    // bulk segments (start point / 32)
-    int64_t nseg;
-    int bulk_blocks;       // blocks [0, bulk_blocks) run the bulk part
-    // boundary-list part ("special": boundary + next-to-wall nodes)
+    // one thread per active node: word = point index | (boundary-list flag << 31)
+    int64_t nact;
+    const uint32_t* act_word;
+    const int32_t* sp_of_act;  // boundary-list entry of an active node (or -1)
+    // boundary list ("special": boundary + next-to-wall nodes)
     int64_t nsp;
-    const int64_t* sp_pt;
     const uint32_t* sp_miss;  // bit q: lattice point x + c_q is not active
     const uint8_t* sp_cls;
     const int32_t* sp_nw;     // next-to-wall index or -1

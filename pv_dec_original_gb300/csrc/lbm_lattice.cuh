@@ -73,19 +73,24 @@ __host__ __device__ constexpr int lat_c(int q, int axis) {
 }
 
 // ---------------------------------------------------------------------------
-// Storage formats.  FP64 and FP32 store f directly.  FP16 and BF16 store the
-// offset from the lattice weight, relative to it and scaled:
-//     stored = (f - w) / w * S,   f = w + (w / S) * stored
-// S = 1024 for FP16 keeps offsets down to ~6e-8 in the normal range while
-// +-0.5 relative offsets stay far below the FP16 maximum; BF16 has FP32's
-// exponent range and uses S = 1.
+// Storage formats and the arithmetic value they hold.
+//
+// FP64: f itself, FP64 arithmetic in the reference's operation order.
+// FP32, FP16, BF16: the offset d = f - w from the lattice weight, with all
+// arithmetic in FP32 on d (the collision, Zou-He and stress formulas are
+// affine in f and are written for d).  Near rest |d| << w, so carrying d
+// keeps ~5 more significant bits than carrying f.  Storage of d:
+//   FP32: d,            FP16: d / w * 1024,          BF16: d / w.
+// The relative scaling by 1/w gives every direction the same range; the
+// factor 1024 keeps FP16 offsets down to ~6e-8 normal while +-0.5 relative
+// offsets stay far below the FP16 maximum.  BF16 has FP32's exponent range.
 enum Precision : int { P_F64 = 0, P_F32 = 1, P_F16 = 2, P_BF16 = 3 };
 
 template <typename S> struct Store;
 
 template <> struct Store<double> {
     using real = double;
-    static constexpr int precision = P_F64;
+    static constexpr bool offset = false;
     template <int Q>
     __device__ static __forceinline__ real load(const double* p, int q) { return *p; }
     template <int Q>
@@ -94,41 +99,37 @@ template <> struct Store<double> {
 
 template <> struct Store<float> {
     using real = float;
-    static constexpr int precision = P_F32;
+    static constexpr bool offset = true;
     template <int Q>
     __device__ static __forceinline__ real load(const float* p, int q) { return __ldg(p); }
     template <int Q>
-    __device__ static __forceinline__ float pack(real f, int q) { return f; }
+    __device__ static __forceinline__ float pack(real d, int q) { return d; }
 };
 
 template <> struct Store<__half> {
     using real = float;
-    static constexpr int precision = P_F16;
+    static constexpr bool offset = true;
     static constexpr float S = 1024.0f;
     template <int Q>
     __device__ static __forceinline__ real load(const __half* p, int q) {
-        const float w = (float)Lat<Q>::w(q);
-        return fmaf(__half2float(__ldg(p)), w * (1.0f / S), w);
+        return __half2float(__ldg(p)) * ((float)Lat<Q>::w(q) * (1.0f / S));
     }
     template <int Q>
-    __device__ static __forceinline__ __half pack(real f, int q) {
-        const float w = (float)Lat<Q>::w(q);
-        return __float2half_rn((f - w) * (S / w));
+    __device__ static __forceinline__ __half pack(real d, int q) {
+        return __float2half_rn(d * (S / (float)Lat<Q>::w(q)));
     }
 };
 
 template <> struct Store<__nv_bfloat16> {
     using real = float;
-    static constexpr int precision = P_BF16;
+    static constexpr bool offset = true;
     template <int Q>
     __device__ static __forceinline__ real load(const __nv_bfloat16* p, int q) {
-        const float w = (float)Lat<Q>::w(q);
-        return fmaf(__bfloat162float(__ldg(p)), w, w);
+        return __bfloat162float(__ldg(p)) * (float)Lat<Q>::w(q);
     }
     template <int Q>
-    __device__ static __forceinline__ __nv_bfloat16 pack(real f, int q) {
-        const float w = (float)Lat<Q>::w(q);
-        return __float2bfloat16_rn((f - w) * (1.0f / w));
+    __device__ static __forceinline__ __nv_bfloat16 pack(real d, int q) {
+        return __float2bfloat16_rn(d * (1.0f / (float)Lat<Q>::w(q)));
     }
 };
 

@@ -133,37 +133,24 @@ __global__ void k_special_info(const int64_t* __restrict__ sp_pt, int64_t nsp, c
     prof[s] = p;
 }
 
-__global__ void k_flag_segments(const uint8_t* __restrict__ cls, int64_t npts, int64_t nsegs,
-                                int64_t* __restrict__ flag) {
-    const int64_t sgi = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    const int lane = threadIdx.x & 31;
-    if (sgi >= nsegs) return;
-    const int64_t n = sgi * 32 + lane;
-    const bool bulk = n < npts && cls[n] == CLS_FLUID;
-    const unsigned any = __ballot_sync(0xffffffffu, bulk);
-    if (lane == 0) flag[sgi] = any ? 1 : 0;
-}
-
-__global__ void k_scatter_seg(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t nsegs,
-                              int32_t* __restrict__ out) {
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nsegs || !flag[s]) return;
-    out[pos[s]] = (int32_t)s;
-}
-
 __global__ void k_active_flags(const uint8_t* __restrict__ cls, int64_t npts, int64_t* __restrict__ flag) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= npts) return;
     flag[n] = cls[n] != CLS_SOLID ? 1 : 0;
 }
 
-__global__ void k_active_index(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t npts,
-                               int32_t* __restrict__ act_idx, int64_t* __restrict__ act_pt) {
+__global__ void k_active_index(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos,
+                               const int64_t* __restrict__ spflag, const int64_t* __restrict__ sppos, int64_t npts,
+                               int32_t* __restrict__ act_idx, int64_t* __restrict__ act_pt,
+                               uint32_t* __restrict__ act_word, int32_t* __restrict__ sp_of_act) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= npts) return;
     if (flag[n]) {
-        act_idx[n] = (int32_t)pos[n];
-        act_pt[pos[n]] = n;
+        const int64_t a = pos[n];
+        act_idx[n] = (int32_t)a;
+        act_pt[a] = n;
+        act_word[a] = (uint32_t)n | (spflag[n] ? 0x80000000u : 0u);
+        sp_of_act[a] = spflag[n] ? (int32_t)sppos[n] : -1;
     } else {
         act_idx[n] = -1;
     }
@@ -321,21 +308,21 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
         SETUP_CHECK(cudaGetLastError());
     }
 
-    // bulk segments: 32 consecutive points holding at least one interior node
-    const int64_t nsegs = ceil_div(npts, 32);
-    k_flag_segments<<<blocks(nsegs, 8), 256, 0, st>>>(out.cls, npts, nsegs, flag);
-    SETUP_CHECK(exclusive_scan_i64(flag, pos, nsegs, &out.nseg, st));
-    SETUP_CHECK(cudaMallocAsync(&out.seg, sizeof(int32_t) * (out.nseg + 1), st));
-    k_scatter_seg<<<blocks(nsegs), 256, 0, st>>>(flag, pos, nsegs, out.seg);
-    SETUP_CHECK(cudaGetLastError());
-
-    // active index (readouts)
-    k_active_flags<<<blocks(npts), 256, 0, st>>>(out.cls, npts, flag);
-    SETUP_CHECK(exclusive_scan_i64(flag, pos, npts, &out.nact, st));
+    // active index and the packed per-node words of the step kernel
+    int64_t *aflag = nullptr, *apos = nullptr;
+    SETUP_CHECK(cudaMallocAsync(&aflag, sizeof(int64_t) * npts, st));
+    SETUP_CHECK(cudaMallocAsync(&apos, sizeof(int64_t) * npts, st));
+    k_active_flags<<<blocks(npts), 256, 0, st>>>(out.cls, npts, aflag);
+    SETUP_CHECK(exclusive_scan_i64(aflag, apos, npts, &out.nact, st));
     SETUP_CHECK(cudaMallocAsync(&out.act_idx, sizeof(int32_t) * npts, st));
     SETUP_CHECK(cudaMallocAsync(&out.act_pt, sizeof(int64_t) * (out.nact + 1), st));
-    k_active_index<<<blocks(npts), 256, 0, st>>>(flag, pos, npts, out.act_idx, out.act_pt);
+    SETUP_CHECK(cudaMallocAsync(&out.act_word, sizeof(uint32_t) * (out.nact + 1), st));
+    SETUP_CHECK(cudaMallocAsync(&out.sp_of_act, sizeof(int32_t) * (out.nact + 1), st));
+    k_active_index<<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, npts, out.act_idx, out.act_pt,
+                                                 out.act_word, out.sp_of_act);
     SETUP_CHECK(cudaGetLastError());
+    cudaFreeAsync(aflag, st);
+    cudaFreeAsync(apos, st);
     cudaFreeAsync(flag, st);
     cudaFreeAsync(pos, st);
     cudaFreeAsync(nwflag, st);

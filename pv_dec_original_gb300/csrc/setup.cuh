@@ -25,9 +25,9 @@ struct GeometryLists {
     double* sp_prof = nullptr;
     int64_t nnw = 0;
     int64_t* nw_pt = nullptr;
-    int64_t nseg = 0;
-    int32_t* seg = nullptr;
     int64_t nact = 0;
+    uint32_t* act_word = nullptr;  // per active node: point index | boundary-list flag << 31
+    int32_t* sp_of_act = nullptr;  // per active node: boundary-list entry or -1
     int32_t* act_idx = nullptr;  // per point
     int64_t* act_pt = nullptr;
     int plane[LBM_MAX_BC] = {0};

@@ -54,7 +54,7 @@ __global__ void k_macro(const double* __restrict__ f, int64_t nact, double* __re
 #pragma unroll
     for (int q = 0; q < Q; ++q) g[q] = f[a * Q + q];
     double r, ux, uy, uz;
-    moments<Q, double>(g, r, ux, uy, uz);
+    moments<Q, double, false>(g, r, ux, uy, uz);
     if (rho) rho[a] = r;
     if (u) { u[3 * a] = ux; u[3 * a + 1] = uy; u[3 * a + 2] = uz; }
 }
@@ -70,7 +70,7 @@ __global__ void k_warm(const float* __restrict__ rho, const float* __restrict__ 
     const double r = rho[a];
     const double ux = u[3 * a], uy = u[3 * a + 1], uz = u[3 * a + 2];
     double e[Q];
-    feq_all<Q, double>(e, r, ux, uy, uz);
+    feq_all<Q, double, false>(e, r, ux, uy, uz);
     if (regularized) {
         const int64_t n = act_pt[a];
         const int idx[3] = {(int)(n % nx), (int)((n / nx) % ny), (int)(n / ((int64_t)nx * ny))};

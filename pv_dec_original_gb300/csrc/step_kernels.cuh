@@ -1,11 +1,12 @@
 // Fused stream-collide step kernel (pull scheme), templated on lattice,
 // storage format and semantics.  Included by step_f64.cu (FP64, compiled
 // without FMA contraction so FP64 parity runs round exactly like the
-// reference) and step_fast.cu (FP32 / FP16 / BF16 storage, FP32 arithmetic).
+// reference) and step_fast.cu (FP32 / FP16 / BF16 storage, FP32 arithmetic
+// on offsets d = f - w).
 //
-// One launch advances the lattice by one reference step.  Distributions are
+// One launch advances the lattice by one reference step.  Populations are
 // stored post-collision, structure of arrays, one plane per population over
-// the dense box (f[q][n], n = (k*ny + j)*nx + i).  Launch k:
+// the dense box (plane q holds entry n = (k*ny + j)*nx + i).  Launch k:
 //   1. pulls f*_q(x - c_q) from the input planes        (Streaming, Simulation.cpp:264-290)
 //   2. applies Zou-He / the wall rule on boundary nodes (Simulation.cpp:614-863)
 //   3. accumulates wall shear stress on next-to-wall nodes (Simulation.cpp:880-898)
@@ -14,11 +15,13 @@
 // step boundary moved between 3 and 4; a prologue launch collides the initial
 // state and a read-out launch stops after 2.
 //
-// The grid has two parts.  Blocks [0, bulk_blocks) walk 32-point segments of
-// interior fluid nodes (all neighbours active, no boundary work): 19 or 27
-// coalesced shifted loads, collision, 19 or 27 aligned stores.  The remaining
-// blocks walk the compact boundary list (wall / inlet / outlet nodes and the
-// next-to-wall nodes that carry the WSS accumulators), one node per thread.
+// Thread a handles the a-th active (non-solid) node in increasing n, so the
+// 32 lanes of a warp sit on consecutive runs of x and every population load
+// and store is coalesced.  A packed word per node gives n and one flag bit:
+// interior nodes (all neighbours active, no boundary work) take the short
+// path; boundary and next-to-wall nodes take the long path, which looks up
+// their entry in the compact boundary list (per-link missing mask, class,
+// WSS accumulators, parity history).
 //
 // Parity semantics for links whose source is missing: the reference's push
 // leaves the destination's previous value in place; the boundary list keeps
@@ -40,13 +43,10 @@ __device__ __forceinline__ int64_t nb_off(int q, int64_t nx, int64_t nxy) {
     return (int64_t)Lat<Q>::cx(q) + (int64_t)Lat<Q>::cy(q) * nx + (int64_t)Lat<Q>::cz(q) * nxy;
 }
 
-// rho and u with the reference's explicit sums (Simulation.cpp:105-228).
+// Momentum sums with the reference's explicit index lists (Simulation.cpp:122-228);
+// the same lists apply to offsets because sum_q w_q c_q = 0.
 template <int Q, typename R>
-__device__ __forceinline__ void moments(const R (&f)[Q], R& rho, R& ux, R& uy, R& uz) {
-    R d = R(0);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) d += f[q];
-    R px, py, pz;
+__device__ __forceinline__ void momentum(const R (&f)[Q], R& px, R& py, R& pz) {
     if constexpr (Q == 19) {
         px = (f[0] + f[6] + f[7] + f[8] + f[9]) - (f[1] + f[10] + f[11] + f[12] + f[13]);
         py = (f[2] + f[6] + f[10] + f[14] + f[15]) - (f[3] + f[7] + f[11] + f[16] + f[17]);
@@ -59,94 +59,109 @@ __device__ __forceinline__ void moments(const R (&f)[Q], R& rho, R& ux, R& uy, R
         pz = (f[5] + f[11] + f[12] + f[15] + f[17] + f[19] + f[22] + f[23] + f[26]) -
              (f[6] + f[13] + f[14] + f[16] + f[18] + f[20] + f[21] + f[24] + f[25]);
     }
-    if constexpr (sizeof(R) == 8) {
-        ux = px / d; uy = py / d; uz = pz / d;  // reference rounding: three divisions
-    } else {
-        const R inv = R(1) / d;
+}
+
+// Moments.  Full f (FP64): rho = sum f and u = j / rho with three divisions,
+// as the reference rounds them (Simulation.cpp:105-158).  Offsets (FP32):
+// r = rho - 1 = sum d, u = j / (1 + r).  `r` returns rho (full) or rho - 1.
+template <int Q, typename R, bool OFF>
+__device__ __forceinline__ void moments(const R (&f)[Q], R& r, R& ux, R& uy, R& uz) {
+    R d = R(0);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) d += f[q];
+    R px, py, pz;
+    momentum<Q, R>(f, px, py, pz);
+    if constexpr (OFF) {
+        const R inv = R(1) / (R(1) + d);
         ux = px * inv; uy = py * inv; uz = pz * inv;
+    } else {
+        ux = px / d; uy = py / d; uz = pz / d;
     }
-    rho = d;
+    r = d;
 }
 
-// Equilibrium of direction q (Simulation.cpp:239-249 operation order).
-template <int Q, int q, typename R>
-__device__ __forceinline__ R feq_q(R rho, R ux, R uy, R uz, R usqr) {
+// Equilibrium of direction q.  Full: w rho (1 + 3cu + 4.5(cu)^2 - 1.5u^2) in the
+// reference's operation order (Simulation.cpp:239-249).  Offset:
+// feq - w = w (r + rho (3cu + 4.5(cu)^2 - 1.5u^2)) with r = rho - 1.
+template <int Q, int q, typename R, bool OFF>
+__device__ __forceinline__ R feq_q(R r, R ux, R uy, R uz, R usqr) {
     const R du = ux * (R)Lat<Q>::cx(q) + uy * (R)Lat<Q>::cy(q) + uz * (R)Lat<Q>::cz(q);
-    return (R)Lat<Q>::w(q) * rho * (R(1.0) + R(3.0) * du + R(4.5) * du * du - R(1.5) * usqr);
-}
-
-template <int Q, typename R, int q = 0>
-__device__ __forceinline__ void relax_all(R (&f)[Q], R rho, R ux, R uy, R uz, R usqr, R inv_tau) {
-    if constexpr (q < Q) {
-        const R e = feq_q<Q, q>(rho, ux, uy, uz, usqr);
-        f[q] = f[q] + inv_tau * (e - f[q]);
-        relax_all<Q, R, q + 1>(f, rho, ux, uy, uz, usqr, inv_tau);
+    if constexpr (OFF) {
+        return (R)Lat<Q>::w(q) * (r + (R(1) + r) * (R(3.0) * du + R(4.5) * du * du - R(1.5) * usqr));
+    } else {
+        return (R)Lat<Q>::w(q) * r * (R(1.0) + R(3.0) * du + R(4.5) * du * du - R(1.5) * usqr);
     }
 }
 
-template <int Q, typename R, int q = 0>
-__device__ __forceinline__ void feq_all(R (&e)[Q], R rho, R ux, R uy, R uz) {
+template <int Q, typename R, bool OFF, int q = 0>
+__device__ __forceinline__ void relax_all(R (&f)[Q], R r, R ux, R uy, R uz, R usqr, R inv_tau) {
+    if constexpr (q < Q) {
+        const R e = feq_q<Q, q, R, OFF>(r, ux, uy, uz, usqr);
+        f[q] = f[q] + inv_tau * (e - f[q]);
+        relax_all<Q, R, OFF, q + 1>(f, r, ux, uy, uz, usqr, inv_tau);
+    }
+}
+
+template <int Q, typename R, bool OFF, int q = 0>
+__device__ __forceinline__ void feq_all(R (&e)[Q], R r, R ux, R uy, R uz) {
     if constexpr (q < Q) {
         const R usqr = ux * ux + uy * uy + uz * uz;
-        e[q] = feq_q<Q, q>(rho, ux, uy, uz, usqr);
-        feq_all<Q, R, q + 1>(e, rho, ux, uy, uz);
+        e[q] = feq_q<Q, q, R, OFF>(r, ux, uy, uz, usqr);
+        feq_all<Q, R, OFF, q + 1>(e, r, ux, uy, uz);
     }
 }
 
-// BGK collision in place; returns the moments.
-template <int Q, typename R>
-__device__ __forceinline__ void collide(R (&f)[Q], R inv_tau, R& rho, R& ux, R& uy, R& uz) {
-    moments<Q, R>(f, rho, ux, uy, uz);
+// BGK collision in place; returns the moments (r as in `moments`).
+template <int Q, typename R, bool OFF>
+__device__ __forceinline__ void collide(R (&f)[Q], R inv_tau, R& r, R& ux, R& uy, R& uz) {
+    moments<Q, R, OFF>(f, r, ux, uy, uz);
     const R usqr = ux * ux + uy * uy + uz * uz;
-    relax_all<Q, R>(f, rho, ux, uy, uz, usqr, inv_tau);
+    relax_all<Q, R, OFF>(f, r, ux, uy, uz, usqr, inv_tau);
 }
 
 // ---------------------------------------------------------------------------
 // Boundary formulas.
 
-// Boundary::ApplyBc, D3Q19 x-min velocity inlet (Boundary.cpp:157-185).
-template <typename R>
-__device__ __forceinline__ void ref_inlet_q19(R (&m)[19], R vel) {
-    const R u0 = vel, u1 = R(0.0), u2 = R(0.0);
-    R rhoN = (m[2] + m[3] + m[4] + m[5] + m[14] + m[15] + m[16] + m[17] + m[18] +
-              R(2) * (m[1] + m[10] + m[11] + m[12] + m[13])) / (R(1) - u0);
-    R Ny = (R(1.0) / R(2)) * (m[2] + m[14] + m[15] - m[3] - m[16] - m[17]) - (R(1.0) / R(3)) * (rhoN * u1);
-    R Nz = (R(1.0) / R(2)) * (m[4] + m[16] + m[14] - m[5] - m[15] - m[17]) - (R(1.0) / R(3)) * (rhoN * u2);
-    m[0] = m[1] + (R(1) / R(3.0)) * rhoN * u0;
-    m[7] = m[10] + (R(1) / R(6.0)) * rhoN * (u0 - u1) + Ny;
-    m[6] = m[11] + (R(1) / R(6.0)) * rhoN * (u0 + u1) - Ny;
-    m[8] = m[13] + (R(1) / R(6.0)) * rhoN * (u0 + u2) - Nz;
-    m[9] = m[12] + (R(1) / R(6.0)) * rhoN * (u0 - u2) + Nz;
+// Boundary::ApplyBc, D3Q19 x-min velocity inlet (Boundary.cpp:157-185), full f.
+__device__ __forceinline__ void ref_inlet_q19(double (&m)[19], double vel) {
+    const double u0 = vel, u1 = 0.0, u2 = 0.0;
+    double rhoN = (m[2] + m[3] + m[4] + m[5] + m[14] + m[15] + m[16] + m[17] + m[18] +
+                   2 * (m[1] + m[10] + m[11] + m[12] + m[13])) / (1 - u0);
+    double Ny = (1.0 / 2) * (m[2] + m[14] + m[15] - m[3] - m[16] - m[17]) - (1.0 / 3) * (rhoN * u1);
+    double Nz = (1.0 / 2) * (m[4] + m[16] + m[14] - m[5] - m[15] - m[17]) - (1.0 / 3) * (rhoN * u2);
+    m[0] = m[1] + (1 / 3.0) * rhoN * u0;
+    m[7] = m[10] + (1 / 6.0) * rhoN * (u0 - u1) + Ny;
+    m[6] = m[11] + (1 / 6.0) * rhoN * (u0 + u1) - Ny;
+    m[8] = m[13] + (1 / 6.0) * rhoN * (u0 + u2) - Nz;
+    m[9] = m[12] + (1 / 6.0) * rhoN * (u0 - u2) + Nz;
 }
 
-// ApplyOutletBc outlet 1, y-max face, rho = 1 (Simulation.cpp:642-695).
-template <typename R>
-__device__ __forceinline__ void ref_outlet_ymax_q19(R (&m)[19]) {
-    const R rho = R(1.0), vx = R(0.0), vz = R(0.0);
-    R vy = R(-1) + (R(1.0) / rho) * (m[0] + m[1] + m[4] + m[5] + m[8] + m[9] + m[12] + m[13] + m[18] +
-                                     R(2.0) * (m[2] + m[6] + m[10] + m[14] + m[15]));
-    R Nyx = R(0.5) * (m[0] + m[8] + m[9] - (m[1] + m[12] + m[13])) - (R(1.0) / R(3.0)) * rho * vx;
-    R Nyz = R(0.5) * (m[4] + m[8] + m[12] - (m[5] + m[9] + m[13])) - (R(1.0) / R(3.0)) * rho * vz;
-    m[3] = m[2] - (R(1.0) / R(3.0)) * rho * vy;
-    m[11] = m[6] + (R(1.0) / R(6.0)) * rho * (-vx - vy) + Nyx;
-    m[7] = m[10] + (R(1.0) / R(6.0)) * rho * (vx - vy) - Nyx;
-    m[17] = m[14] + (R(1.0) / R(6.0)) * rho * (-vy - vz) + Nyz;
-    m[16] = m[15] + (R(1.0) / R(6.0)) * rho * (-vy + vz) - Nyz;
+// ApplyOutletBc outlet 1, y-max face, rho = 1 (Simulation.cpp:642-695), full f.
+__device__ __forceinline__ void ref_outlet_ymax_q19(double (&m)[19]) {
+    const double rho = 1.0, vx = 0.0, vz = 0.0;
+    double vy = -1 + (1.0 / rho) * (m[0] + m[1] + m[4] + m[5] + m[8] + m[9] + m[12] + m[13] + m[18] +
+                                    2.0 * (m[2] + m[6] + m[10] + m[14] + m[15]));
+    double Nyx = 0.5 * (m[0] + m[8] + m[9] - (m[1] + m[12] + m[13])) - (1.0 / 3.0) * rho * vx;
+    double Nyz = 0.5 * (m[4] + m[8] + m[12] - (m[5] + m[9] + m[13])) - (1.0 / 3.0) * rho * vz;
+    m[3] = m[2] - (1.0 / 3.0) * rho * vy;
+    m[11] = m[6] + (1.0 / 6.0) * rho * (-vx - vy) + Nyx;
+    m[7] = m[10] + (1.0 / 6.0) * rho * (vx - vy) - Nyx;
+    m[17] = m[14] + (1.0 / 6.0) * rho * (-vy - vz) + Nyz;
+    m[16] = m[15] + (1.0 / 6.0) * rho * (-vy + vz) - Nyz;
 }
 
-// ApplyOutletBc outlets 2 and 3, z-min face, rho = 1 (Simulation.cpp:710-836).
-template <typename R>
-__device__ __forceinline__ void ref_outlet_zmin_q19(R (&m)[19]) {
-    const R rho = R(1.0), vx = R(0.0), vy = R(0.0);
-    R vz = R(1) - (R(1.0) / rho) * (m[0] + m[1] + m[2] + m[3] + m[6] + m[7] + m[10] + m[11] + m[18] +
-                                    R(2.0) * (m[5] + m[9] + m[13] + m[15] + m[17]));
-    R Nzx = R(0.5) * (m[0] + m[6] + m[7] - (m[1] + m[10] + m[11])) - (R(1.0) / R(3.0)) * rho * vx;
-    R Nzy = R(0.5) * (m[2] + m[6] + m[10] - (m[3] + m[7] + m[11])) - (R(1.0) / R(3.0)) * rho * vy;
-    m[4] = m[5] + (R(1.0) / R(3.0)) * rho * vz;
-    m[8] = m[13] + (R(1.0) / R(6.0)) * rho * (vz + vx) - Nzx;
-    m[12] = m[9] + (R(1.0) / R(6.0)) * rho * (vz - vx) + Nzx;
-    m[14] = m[17] + (R(1.0) / R(6.0)) * rho * (vz + vy) - Nzy;
-    m[16] = m[15] + (R(1.0) / R(6.0)) * rho * (vz - vy) + Nzy;
+// ApplyOutletBc outlets 2 and 3, z-min face, rho = 1 (Simulation.cpp:710-836), full f.
+__device__ __forceinline__ void ref_outlet_zmin_q19(double (&m)[19]) {
+    const double rho = 1.0, vx = 0.0, vy = 0.0;
+    double vz = 1 - (1.0 / rho) * (m[0] + m[1] + m[2] + m[3] + m[6] + m[7] + m[10] + m[11] + m[18] +
+                                   2.0 * (m[5] + m[9] + m[13] + m[15] + m[17]));
+    double Nzx = 0.5 * (m[0] + m[6] + m[7] - (m[1] + m[10] + m[11])) - (1.0 / 3.0) * rho * vx;
+    double Nzy = 0.5 * (m[2] + m[6] + m[10] - (m[3] + m[7] + m[11])) - (1.0 / 3.0) * rho * vy;
+    m[4] = m[5] + (1.0 / 3.0) * rho * vz;
+    m[8] = m[13] + (1.0 / 6.0) * rho * (vz + vx) - Nzx;
+    m[12] = m[9] + (1.0 / 6.0) * rho * (vz - vx) + Nzx;
+    m[14] = m[17] + (1.0 / 6.0) * rho * (vz + vy) - Nzy;
+    m[16] = m[15] + (1.0 / 6.0) * rho * (vz - vy) + Nzy;
 }
 
 // Zou-He on any axis-aligned face.  With sigma = +1 on a min face and -1 on
@@ -155,8 +170,10 @@ __device__ __forceinline__ void ref_outlet_zmin_q19(R (&m)[19]) {
 //   N_t = (sum_{c_a=0} f c_t - 2/3 rho u_t) / M      (M = 2 for D3Q19, 6 for D3Q27)
 //   f_i = f_opp(i) + 6 w_i rho (c_i . u) - sum_t c_it N_t
 // which reduces to the reference's formulas on its faces for both lattices
-// (Boundary.cpp:115-185).
-template <int Q, int FACE, typename R>
+// (Boundary.cpp:115-185).  On offsets d = f - w the same lines hold with
+// S_0 + 2 S_{-sigma} gaining +1 (the weights of those populations sum to 1)
+// and everything else unchanged (w_i = w_opp(i), sum_{c_a=0} w c_t = 0).
+template <int Q, int FACE, typename R, bool OFF>
 __device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
     constexpr int a = FACE / 2;
     constexpr int sg = (FACE % 2 == 0) ? 1 : -1;
@@ -167,14 +184,15 @@ __device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
         if (ca == 0) S0 += m[q];
         else if (ca == -sg) Sm += m[q];
     }
+    const R S = (OFF ? R(1) : R(0)) + S0 + R(2.0) * Sm;
     R u[3] = {R(0), R(0), R(0)};
     R rho;
     if (pressure) {
         rho = value;
-        u[a] = R(sg) * (R(1.0) - (S0 + R(2.0) * Sm) / rho);
+        u[a] = R(sg) * (R(1.0) - S / rho);
     } else {
         u[a] = R(sg) * value;
-        rho = (S0 + R(2.0) * Sm) / (R(1.0) - R(sg) * u[a]);
+        rho = S / (R(1.0) - R(sg) * u[a]);
     }
     R N[3] = {R(0), R(0), R(0)};
 #pragma unroll
@@ -198,32 +216,34 @@ __device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
     }
 }
 
-template <int Q, typename R>
+template <int Q, typename R, bool OFF>
 __device__ __forceinline__ void zou_he(R (&m)[Q], int face, bool pressure, R value) {
     switch (face) {
-        case 0: zou_he_face<Q, 0>(m, pressure, value); break;
-        case 1: zou_he_face<Q, 1>(m, pressure, value); break;
-        case 2: zou_he_face<Q, 2>(m, pressure, value); break;
-        case 3: zou_he_face<Q, 3>(m, pressure, value); break;
-        case 4: zou_he_face<Q, 4>(m, pressure, value); break;
-        default: zou_he_face<Q, 5>(m, pressure, value); break;
+        case 0: zou_he_face<Q, 0, R, OFF>(m, pressure, value); break;
+        case 1: zou_he_face<Q, 1, R, OFF>(m, pressure, value); break;
+        case 2: zou_he_face<Q, 2, R, OFF>(m, pressure, value); break;
+        case 3: zou_he_face<Q, 3, R, OFF>(m, pressure, value); break;
+        case 4: zou_he_face<Q, 4, R, OFF>(m, pressure, value); break;
+        default: zou_he_face<Q, 5, R, OFF>(m, pressure, value); break;
     }
 }
 
-template <int Q, typename R>
+// The reference's literal D3Q19 formulas run where they can be bit-exact
+// (FP64, full f); elsewhere the reference kinds use the equivalent face form.
+template <int Q, typename R, bool OFF>
 __device__ __forceinline__ void apply_bc(R (&m)[Q], const BCDev& b, double amp, double prof) {
     const R vel = (R)(amp * prof * b.value);
-    if constexpr (Q == 19) {
-        if (b.kind == LBM_BC_REF_INLET) { ref_inlet_q19<R>(m, vel); return; }
-        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { ref_outlet_ymax_q19<R>(m); return; }
-        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { ref_outlet_zmin_q19<R>(m); return; }
+    if constexpr (Q == 19 && !OFF) {
+        if (b.kind == LBM_BC_REF_INLET) { ref_inlet_q19(m, vel); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { ref_outlet_ymax_q19(m); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { ref_outlet_zmin_q19(m); return; }
     } else {
-        if (b.kind == LBM_BC_REF_INLET) { zou_he<Q, R>(m, LBM_FACE_XMIN, false, vel); return; }
-        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { zou_he<Q, R>(m, LBM_FACE_YMAX, true, R(1.0)); return; }
-        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { zou_he<Q, R>(m, LBM_FACE_ZMIN, true, R(1.0)); return; }
+        if (b.kind == LBM_BC_REF_INLET) { zou_he<Q, R, OFF>(m, LBM_FACE_XMIN, false, vel); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { zou_he<Q, R, OFF>(m, LBM_FACE_YMAX, true, R(1.0)); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { zou_he<Q, R, OFF>(m, LBM_FACE_ZMIN, true, R(1.0)); return; }
     }
-    if (b.kind == LBM_BC_VELOCITY) zou_he<Q, R>(m, b.face, false, vel);
-    else if (b.kind == LBM_BC_PRESSURE) zou_he<Q, R>(m, b.face, true, (R)b.value);
+    if (b.kind == LBM_BC_VELOCITY) zou_he<Q, R, OFF>(m, b.face, false, vel);
+    else if (b.kind == LBM_BC_PRESSURE) zou_he<Q, R, OFF>(m, b.face, true, (R)b.value);
 }
 
 __device__ __forceinline__ int bc_axis(const BCDev& b) {
@@ -270,7 +290,7 @@ __device__ __forceinline__ void wss_fast(const R (&f)[Q], const R (&feq)[Q], con
 }
 
 // ---------------------------------------------------------------------------
-// Block reduction of the read-out sums (mass, momentum, per-BC flux).
+// Block reduction of the read-out sums (rho - 1, momentum, per-BC flux).
 
 __device__ __forceinline__ void block_partials(double (&v)[kPartialStride], double* __restrict__ out) {
     __shared__ double red[kStepThreads / 32][kPartialStride];
@@ -290,12 +310,24 @@ __device__ __forceinline__ void block_partials(double (&v)[kPartialStride], doub
     }
 }
 
+template <int Q, typename R, bool OFF>
+__device__ __forceinline__ double full_value(R v, int q) {
+    return OFF ? Lat<Q>::w(q) + (double)v : (double)v;
+}
+
+// f* == 0.0 in the arithmetic's own representation.
+template <int Q, typename R, bool OFF>
+__device__ __forceinline__ bool is_exact_zero(R v, int q) {
+    return OFF ? (v == -(R)Lat<Q>::w(q)) : (v == R(0));
+}
+
 // ---------------------------------------------------------------------------
 // The kernel.
 
 template <int Q, typename S, int MODE, int KIND>
 __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) {
     using R = typename Store<S>::real;
+    constexpr bool OFF = Store<S>::offset;
     const S* __restrict__ fin = static_cast<const S*>(P.fin);
     S* __restrict__ fout = static_cast<S*>(P.fout);
     const R inv_tau = (R)(1.0 / P.tau);
@@ -304,17 +336,15 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
 #pragma unroll
         for (int k = 0; k < kPartialStride; ++k) part[k] = 0.0;
     }
+    const int64_t a = (int64_t)blockIdx.x * kStepThreads + threadIdx.x;
+    const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
 
-    if ((int)blockIdx.x < P.bulk_blocks) {
-        // ---------------- bulk: interior fluid nodes, 32-point segments
-        const int64_t sgi = (int64_t)blockIdx.x * (kStepThreads / 32) + (threadIdx.x >> 5);
-        const bool seg_ok = sgi < P.nseg;
-        const int64_t n = seg_ok ? (int64_t)__ldg(P.seg + sgi) * 32 + (threadIdx.x & 31) : 0;
-        const bool live = seg_ok && __ldg(P.cls + n) == CLS_FLUID;
-        if (live) {
+    if (a < P.nact) {
+        const uint32_t word = __ldg(P.act_word + a);
+        const int64_t n = (int64_t)(word & 0x7fffffffu);
+        if (!(word >> 31)) {
+            // ---------------- interior fluid node: every neighbour is active
             R f[Q];
-#pragma unroll
-            const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 const int64_t src = direct ? n : n - nb_off<Q>(q, P.nx, P.nxy);
@@ -323,41 +353,38 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
             if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
                 bool zero = false;
 #pragma unroll
-                for (int q = 0; q < Q; ++q) zero |= (f[q] == R(0));
+                for (int q = 0; q < Q; ++q) zero |= is_exact_zero<Q, R, OFF>(f[q], q);
                 if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
             }
             if constexpr (KIND == KIND_READOUT) {
-                const int64_t a = __ldg(P.act_idx + n);
-                R rho, ux, uy, uz;
-                moments<Q, R>(f, rho, ux, uy, uz);
-                part[0] = (double)rho;
-                part[1] = (double)(rho * ux); part[2] = (double)(rho * uy); part[3] = (double)(rho * uz);
+                R r, ux, uy, uz;
+                moments<Q, R, OFF>(f, r, ux, uy, uz);
+                const double rho = OFF ? 1.0 + (double)r : (double)r;
+                part[0] = OFF ? (double)r : rho - 1.0;
+                part[1] = rho * ux; part[2] = rho * uy; part[3] = rho * uz;
                 if (P.out_f) {
 #pragma unroll
-                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = (double)f[q];
+                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(f[q], q);
                 }
             } else {
-                R rho, ux, uy, uz;
-                collide<Q, R>(f, inv_tau, rho, ux, uy, uz);
-                if (!(fabs((double)rho) < 1e30)) atomicOr(P.flags, FLAG_NONFINITE);
+                R r, ux, uy, uz;
+                collide<Q, R, OFF>(f, inv_tau, r, ux, uy, uz);
+                if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
 #pragma unroll
                 for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(f[q], q);
             }
-        }
-    } else {
-        // ---------------- boundary list: one node per thread
-        const int64_t s = (int64_t)((int)blockIdx.x - P.bulk_blocks) * kStepThreads + threadIdx.x;
-        if (s < P.nsp) {
-            const int64_t n = __ldg(P.sp_pt + s);
+        } else {
+            // ---------------- boundary-list node
+            const int64_t s = __ldg(P.sp_of_act + a);
             const uint32_t miss = __ldg(P.sp_miss + s);
             const int c = __ldg(P.sp_cls + s);
             const int nw = __ldg(P.sp_nw + s);
             R* __restrict__ stale = static_cast<R*>(P.stale);
+            const bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
             R g[Q];
-            const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
-                if (KIND == KIND_READOUT && MODE == MODE_PARITY) {
+                if (parity_readout) {
                     // the boundary list keeps the exact post-boundary f of the last step
                     g[q] = stale[q * P.nsp + s];
                 } else if (direct) {
@@ -369,12 +396,12 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                 } else {
                     R v = Store<S>::template load<Q>(fin + q * P.stride + n - nb_off<Q>(q, P.nx, P.nxy), q);
                     if constexpr (MODE == MODE_PARITY) {
-                        if (v == R(0)) v = stale[q * P.nsp + s];
+                        if (is_exact_zero<Q, R, OFF>(v, q)) v = stale[q * P.nsp + s];
                     }
                     g[q] = v;
                 }
             }
-            if (!direct && !(KIND == KIND_READOUT && MODE == MODE_PARITY)) {
+            if (!direct && !parity_readout) {
                 if (c >= CLS_BC0) {
                     double amp = 0.0;
                     if (P.namp > 0) {
@@ -382,7 +409,7 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                         if (t < 0) t += P.namp;
                         amp = __ldg(P.amp + t);
                     }
-                    apply_bc<Q, R>(g, P.bc[c - CLS_BC0], amp, __ldg(P.sp_prof + s));
+                    apply_bc<Q, R, OFF>(g, P.bc[c - CLS_BC0], amp, __ldg(P.sp_prof + s));
                 } else if (MODE == MODE_PARITY && c == CLS_WALL) {
                     // ApplyWallBc: in place, direction order (Simulation.cpp:846-861)
 #pragma unroll
@@ -391,16 +418,16 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                 }
             }
             if constexpr (KIND == KIND_READOUT) {
-                const int64_t a = __ldg(P.act_idx + n);
-                R rho, ux, uy, uz;
-                moments<Q, R>(g, rho, ux, uy, uz);
-                part[0] = (double)rho;
-                const double j[3] = {(double)(rho * ux), (double)(rho * uy), (double)(rho * uz)};
+                R r, ux, uy, uz;
+                moments<Q, R, OFF>(g, r, ux, uy, uz);
+                const double rho = OFF ? 1.0 + (double)r : (double)r;
+                part[0] = OFF ? (double)r : rho - 1.0;
+                const double j[3] = {rho * ux, rho * uy, rho * uz};
                 part[1] = j[0]; part[2] = j[1]; part[3] = j[2];
                 if (c >= CLS_BC0) part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
                 if (P.out_f) {
 #pragma unroll
-                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = (double)g[q];
+                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
                 }
             } else {
                 R* __restrict__ prev = static_cast<R*>(P.nw_prev);
@@ -411,8 +438,9 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                         if constexpr (MODE == MODE_PARITY) {
                             // equilibrium of the previous collision (time-lagged, as the reference)
                             R e[Q];
-                            feq_all<Q, R>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw], prev[3 * P.nnw + nw]);
-                            if constexpr (sizeof(R) == 8) {
+                            feq_all<Q, R, OFF>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
+                                               prev[3 * P.nnw + nw]);
+                            if constexpr (!OFF) {
                                 wss_reference<Q>(g, e, nn, P.wss_C, t);
                             } else {
                                 const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
@@ -422,9 +450,9 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                             }
                         } else {
                             // stress of the same post-boundary f, with the (1 - 1/2tau) factor
-                            R e[Q], rho, ux, uy, uz;
-                            moments<Q, R>(g, rho, ux, uy, uz);
-                            feq_all<Q, R>(e, rho, ux, uy, uz);
+                            R e[Q], r, ux, uy, uz;
+                            moments<Q, R, OFF>(g, r, ux, uy, uz);
+                            feq_all<Q, R, OFF>(e, r, ux, uy, uz);
                             const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
                             R tr[3];
                             wss_fast<Q, R>(g, e, nr, (R)(-(1.0 - 0.5 / P.tau) * P.wss_C), tr);
@@ -442,11 +470,11 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
 #pragma unroll
                     for (int q = 0; q < Q; ++q) stale[q * P.nsp + s] = g[q];
                 }
-                R rho, ux, uy, uz;
-                collide<Q, R>(g, inv_tau, rho, ux, uy, uz);
-                if (!(fabs((double)rho) < 1e30)) atomicOr(P.flags, FLAG_NONFINITE);
+                R r, ux, uy, uz;
+                collide<Q, R, OFF>(g, inv_tau, r, ux, uy, uz);
+                if (!(fabs((double)r) < 1e30)) atomicOr(P.flags, FLAG_NONFINITE);
                 if (MODE == MODE_PARITY && nw >= 0) {
-                    prev[nw] = rho; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
+                    prev[nw] = r; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
                 }
 #pragma unroll
                 for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(g[q], q);
@@ -461,8 +489,7 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
 
 template <int Q, typename S, int MODE>
 cudaError_t launch_family(int kind, const StepParams& p, cudaStream_t st) {
-    const int64_t sp_blocks = ceil_div(p.nsp, kStepThreads);
-    const int64_t nblocks = (int64_t)p.bulk_blocks + sp_blocks;
+    const int64_t nblocks = ceil_div(p.nact, kStepThreads);
     if (nblocks <= 0) return cudaSuccess;
     if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     switch (kind) {
@@ -488,16 +515,23 @@ cudaError_t launch_typed(int Q, int mode, int kind, const StepParams& p, cudaStr
 // ---------------------------------------------------------------------------
 // State initialisation kernels (storage-typed).
 
-// Every plane entry of every active point := pack(w_q) (f = w, Node.cpp:30-37).
+template <int Q, typename S>
+__device__ __forceinline__ S encode_full(double f, int q) {
+    using R = typename Store<S>::real;
+    if constexpr (Store<S>::offset) return Store<S>::template pack<Q>((R)(f - Lat<Q>::w(q)), q);
+    else return Store<S>::template pack<Q>((R)f, q);
+}
+
+// Every plane entry := f = w (Node.cpp:30-37).
 template <int Q, typename S>
 __global__ void k_fill_weights(S* __restrict__ f, int64_t stride, int64_t npts) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= npts) return;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) f[q * stride + n] = Store<S>::template pack<Q>((typename Store<S>::real)Lat<Q>::w(q), q);
+    for (int q = 0; q < Q; ++q) f[q * stride + n] = encode_full<Q, S>(Lat<Q>::w(q), q);
 }
 
-// f_in[a*Q + q] (FP64, per active node) scattered into the planes.
+// fa[a*Q + q] (FP64 f, per active node) scattered into the planes.
 template <int Q, typename S>
 __global__ void k_scatter_f(const double* __restrict__ fa, const int64_t* __restrict__ act_pt, int64_t nact,
                             S* __restrict__ f, int64_t stride) {
@@ -505,7 +539,7 @@ __global__ void k_scatter_f(const double* __restrict__ fa, const int64_t* __rest
     if (a >= nact) return;
     const int64_t n = act_pt[a];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) f[q * stride + n] = Store<S>::template pack<Q>((typename Store<S>::real)fa[a * Q + q], q);
+    for (int q = 0; q < Q; ++q) f[q * stride + n] = encode_full<Q, S>(fa[a * Q + q], q);
 }
 
 template <typename S>
