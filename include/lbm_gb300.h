@@ -142,6 +142,14 @@ typedef struct {
     int profile;   /* 0 uniform, 1 parabolic 1 - (d1^2 + d2^2)/R^2 */
     double c1, c2; /* profile centre on the two transverse axes (x<y<z order) */
     double R;      /* profile radius */
+    /* Region rule (the form of ComplexGeometry.cpp:1369-1409): when region
+     * != 0 a boundary point matches if |its coordinate on the face axis -
+     * coord| <= tol and lo[t] < coordinate < hi[t] on the two transverse axes
+     * (x<y<z order); `plane` is then unused.  Coordinates are origin +
+     * index * spacing. */
+    int region;
+    double coord, tol;
+    double lo[2], hi[2];
 } lbm_bc_spec;
 
 /* mask: nx*ny*nz bytes (nonzero = Fluid).  Builds classes, boundary lists,

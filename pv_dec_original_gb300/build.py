@@ -35,6 +35,7 @@ UNITS = [
 HOST_UNITS = ["host/LatticeModel.cpp", "host/GeometryReader.cpp", "host/ComplexGeometry.cpp",
               "host/Subdomain.cpp", "host/Simulation.cpp", "host/Boundary.cpp", "host/ConfigReader.cpp",
               "host/OutputFile.cpp", "host/pulsatile.cpp"]
+RUNNER = os.path.join(OUT, "lbm_run")
 
 
 def nvcc() -> str:
@@ -116,6 +117,15 @@ def build(verbose: bool = False, jobs: int = 0) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("host link failed:\n" + r.stderr)
+    drv = os.path.join(CSRC, "host", "LBM.cpp")
+    if os.path.exists(drv) and _stale(RUNNER, [drv, HOST_LIB, LIB] + _deps("host/LBM.cpp")):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(HERE, "..", "include"), "-I",
+               os.path.join(CSRC, "host"), drv, "-o", RUNNER, f"-L{OUT}", "-llbm_host", "-llbm_gb300",
+               f"-Wl,-rpath,{OUT}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("lbm_run link failed:\n" + r.stderr)
     return LIB
 
 

@@ -44,7 +44,9 @@ class Desc(C.Structure):
 
 class BCSpec(C.Structure):
     _fields_ = [("kind", C.c_int), ("face", C.c_int), ("plane", C.c_int), ("value", C.c_double),
-                ("profile", C.c_int), ("c1", C.c_double), ("c2", C.c_double), ("R", C.c_double)]
+                ("profile", C.c_int), ("c1", C.c_double), ("c2", C.c_double), ("R", C.c_double),
+                ("region", C.c_int), ("coord", C.c_double), ("tol", C.c_double), ("lo", C.c_double * 2),
+                ("hi", C.c_double * 2)]
 
 
 class Counts(C.Structure):
@@ -156,10 +158,18 @@ def voxelize(tri12, spacing, bbox=None, origin=None, dims=None):
     return mask.reshape(nz, ny, nx), d
 
 
-def bc_spec(kind, face=0, plane=-1, value=1.0, profile=0, c1=0.0, c2=0.0, R=1.0):
+def bc_spec(kind, face=0, plane=-1, value=1.0, profile=0, c1=0.0, c2=0.0, R=1.0, region=None):
+    """Boundary rule.  region=(coord, tol, (lo1, hi1), (lo2, hi2)) selects
+    points by coordinates instead of a lattice plane."""
     if isinstance(face, str):
         face = FACES[face]
-    return BCSpec(kind, face, plane, value, profile, c1, c2, R)
+    b = BCSpec(kind, face, plane, value, profile, c1, c2, R)
+    if region is not None:
+        coord, tol, (lo1, hi1), (lo2, hi2) = region
+        b.region, b.coord, b.tol = 1, coord, tol
+        b.lo[:] = [lo1, lo2]
+        b.hi[:] = [hi1, hi2]
+    return b
 
 
 class Solver:

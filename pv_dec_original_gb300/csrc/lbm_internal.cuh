@@ -30,9 +30,9 @@ struct StepParams {
     int64_t stride;        // elements per population plane
     int nx, ny;
     int64_t nxy;
-    // one thread per active node: word = point index | (boundary-list flag << 31)
+    // one thread per active node; packed word layout in step_kernels.cuh
     int64_t nact;
-    const uint32_t* act_word;
+    const uint64_t* act_word;
     const int32_t* sp_of_act;  // boundary-list entry of an active node (or -1)
     // boundary list ("special": boundary + next-to-wall nodes)
     int64_t nsp;

@@ -52,14 +52,32 @@ struct Rules {
     int n;
     int axis[LBM_MAX_BC];
     int plane[LBM_MAX_BC];
+    int region[LBM_MAX_BC];
+    double coord[LBM_MAX_BC], tol[LBM_MAX_BC], lo[LBM_MAX_BC][2], hi[LBM_MAX_BC][2];
+    double org[3];
+    double s;
 };
 
+// Plane rules match a lattice index; region rules match coordinates the way
+// classifyBoundaryPoints does (ComplexGeometry.cpp:1380-1407; the reference
+// compares in long double, here in FP64).  First match wins.
 __global__ void k_classify(uint8_t* __restrict__ cls, int nx, int ny, int64_t npts, Rules R) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= npts || cls[n] != CLS_WALL) return;
     const int idx[3] = {(int)(n % nx), (int)((n / nx) % ny), (int)(n / ((int64_t)nx * ny))};
-    for (int r = 0; r < R.n; ++r)
-        if (idx[R.axis[r]] == R.plane[r]) { cls[n] = (uint8_t)(CLS_BC0 + r); return; }
+    for (int r = 0; r < R.n; ++r) {
+        const int a = R.axis[r];
+        bool hit;
+        if (!R.region[r]) {
+            hit = idx[a] == R.plane[r];
+        } else {
+            const double x[3] = {R.org[0] + idx[0] * R.s, R.org[1] + idx[1] * R.s, R.org[2] + idx[2] * R.s};
+            const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+            hit = fabs(x[a] - R.coord[r]) <= R.tol[r] && R.lo[r][0] < x[t1] && x[t1] < R.hi[r][0] &&
+                  R.lo[r][1] < x[t2] && x[t2] < R.hi[r][1];
+        }
+        if (hit) { cls[n] = (uint8_t)(CLS_BC0 + r); return; }
+    }
 }
 
 template <int Q>
@@ -139,21 +157,38 @@ __global__ void k_active_flags(const uint8_t* __restrict__ cls, int64_t npts, in
     flag[n] = cls[n] != CLS_SOLID ? 1 : 0;
 }
 
+// Per active node: index maps and the step kernel's packed word
+// (n | special << 31 | missing mask << 32 | class << 59 | next-to-wall << 63).
+template <int Q>
 __global__ void k_active_index(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos,
-                               const int64_t* __restrict__ spflag, const int64_t* __restrict__ sppos, int64_t npts,
+                               const int64_t* __restrict__ spflag, const int64_t* __restrict__ sppos,
+                               const uint8_t* __restrict__ cls, int nx, int ny, int nz,
                                int32_t* __restrict__ act_idx, int64_t* __restrict__ act_pt,
-                               uint32_t* __restrict__ act_word, int32_t* __restrict__ sp_of_act) {
+                               uint64_t* __restrict__ act_word, int32_t* __restrict__ sp_of_act) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t npts = (int64_t)nx * ny * nz;
     if (n >= npts) return;
-    if (flag[n]) {
-        const int64_t a = pos[n];
-        act_idx[n] = (int32_t)a;
-        act_pt[a] = n;
-        act_word[a] = (uint32_t)n | (spflag[n] ? 0x80000000u : 0u);
-        sp_of_act[a] = spflag[n] ? (int32_t)sppos[n] : -1;
-    } else {
+    if (!flag[n]) {
         act_idx[n] = -1;
+        return;
     }
+    const int64_t a = pos[n];
+    act_idx[n] = (int32_t)a;
+    act_pt[a] = n;
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+    uint64_t miss = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        int x = i + Lat<Q>::cx(q), y = j + Lat<Q>::cy(q), z = k + Lat<Q>::cz(q);
+        bool m = (x < 0 || x >= nx || y < 0 || y >= ny || z < 0 || z >= nz) ||
+                 cls[((int64_t)z * ny + y) * nx + x] == CLS_SOLID;
+        if (m) miss |= 1ull << q;
+    }
+    const uint8_t c = cls[n];
+    const bool sp = spflag[n] != 0;
+    act_word[a] = (uint64_t)n | ((uint64_t)sp << 31) | (miss << 32) | ((uint64_t)(c & CLS_MASK & 0xf) << 59) |
+                  ((uint64_t)((c & CLS_NW_BIT) ? 1 : 0) << 63);
+    sp_of_act[a] = sp ? (int32_t)sppos[n] : -1;
 }
 
 // Per-triangle unit normal, area and centroid (Subdomain.cpp:244-267).
@@ -247,7 +282,7 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     Rules R{};
     R.n = nbc;
     bool need_ext = false;
-    for (int b = 0; b < nbc; ++b) need_ext |= bc[b].plane < 0;
+    for (int b = 0; b < nbc; ++b) need_ext |= bc[b].plane < 0 && !bc[b].region;
     int ext[6] = {0, 0, 0, -1, -1, -1};
     if (need_ext) {
         int* d_ext = nullptr;
@@ -259,10 +294,16 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
         SETUP_CHECK(cudaStreamSynchronize(st));
         cudaFreeAsync(d_ext, st);
     }
+    R.org[0] = origin[0]; R.org[1] = origin[1]; R.org[2] = origin[2];
+    R.s = spacing;
     for (int b = 0; b < nbc; ++b) {
         const int face = bc[b].face;
         R.axis[b] = face / 2;
         R.plane[b] = bc[b].plane >= 0 ? bc[b].plane : (face % 2 == 0 ? ext[face / 2] : ext[3 + face / 2]);
+        R.region[b] = bc[b].region;
+        R.coord[b] = bc[b].coord;
+        R.tol[b] = bc[b].tol;
+        for (int t = 0; t < 2; ++t) { R.lo[b][t] = bc[b].lo[t]; R.hi[b][t] = bc[b].hi[t]; }
         out.plane[b] = R.plane[b];
     }
     k_classify<<<blocks(npts), 256, 0, st>>>(out.cls, nx, ny, npts, R);
@@ -316,10 +357,14 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     SETUP_CHECK(exclusive_scan_i64(aflag, apos, npts, &out.nact, st));
     SETUP_CHECK(cudaMallocAsync(&out.act_idx, sizeof(int32_t) * npts, st));
     SETUP_CHECK(cudaMallocAsync(&out.act_pt, sizeof(int64_t) * (out.nact + 1), st));
-    SETUP_CHECK(cudaMallocAsync(&out.act_word, sizeof(uint32_t) * (out.nact + 1), st));
+    SETUP_CHECK(cudaMallocAsync(&out.act_word, sizeof(uint64_t) * (out.nact + 1), st));
     SETUP_CHECK(cudaMallocAsync(&out.sp_of_act, sizeof(int32_t) * (out.nact + 1), st));
-    k_active_index<<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, npts, out.act_idx, out.act_pt,
-                                                 out.act_word, out.sp_of_act);
+    if (Q == 19)
+        k_active_index<19><<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, out.cls, nx, ny, nz, out.act_idx,
+                                                         out.act_pt, out.act_word, out.sp_of_act);
+    else
+        k_active_index<27><<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, out.cls, nx, ny, nz, out.act_idx,
+                                                         out.act_pt, out.act_word, out.sp_of_act);
     SETUP_CHECK(cudaGetLastError());
     cudaFreeAsync(aflag, st);
     cudaFreeAsync(apos, st);

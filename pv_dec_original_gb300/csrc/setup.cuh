@@ -26,7 +26,7 @@ struct GeometryLists {
     int64_t nnw = 0;
     int64_t* nw_pt = nullptr;
     int64_t nact = 0;
-    uint32_t* act_word = nullptr;  // per active node: point index | boundary-list flag << 31
+    uint64_t* act_word = nullptr;  // per active node: packed word (see step_kernels.cuh)
     int32_t* sp_of_act = nullptr;  // per active node: boundary-list entry or -1
     int32_t* act_idx = nullptr;  // per point
     int64_t* act_pt = nullptr;

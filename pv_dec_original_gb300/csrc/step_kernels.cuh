@@ -17,11 +17,11 @@
 //
 // Thread a handles the a-th active (non-solid) node in increasing n, so the
 // 32 lanes of a warp sit on consecutive runs of x and every population load
-// and store is coalesced.  A packed word per node gives n and one flag bit:
-// interior nodes (all neighbours active, no boundary work) take the short
-// path; boundary and next-to-wall nodes take the long path, which looks up
-// their entry in the compact boundary list (per-link missing mask, class,
-// WSS accumulators, parity history).
+// and store is coalesced.  One 64-bit word per node carries n, the node's
+// missing-link mask and class, so every lane issues the same Q loads and the
+// same Q stores; only boundary work (history, boundary rules, wall shear
+// stress on next-to-wall nodes) diverges, and only those lanes look up their
+// entry in the compact boundary list.
 //
 // Parity semantics for links whose source is missing: the reference's push
 // leaves the destination's previous value in place; the boundary list keeps
@@ -324,6 +324,17 @@ __device__ __forceinline__ bool is_exact_zero(R v, int q) {
 // ---------------------------------------------------------------------------
 // The kernel.
 
+// Packed per-node word (built by setup.cu):
+//   bits  0-30  lattice point n
+//   bit   31    boundary-list node (needs the long path)
+//   bits 32-58  missing-link mask: bit q set when x + c_q is solid / outside
+//   bits 59-62  class (1 fluid, 2 wall, 3+b boundary condition b)
+//   bit   63    next-to-wall node (accumulates wall shear stress)
+__device__ __forceinline__ int64_t word_point(uint64_t w) { return (int64_t)(w & 0x7fffffffull); }
+__device__ __forceinline__ bool word_special(uint64_t w) { return (w >> 31) & 1ull; }
+__device__ __forceinline__ uint32_t word_miss(uint64_t w) { return (uint32_t)((w >> 32) & 0x7ffffffull); }
+__device__ __forceinline__ int word_class(uint64_t w) { return (int)((w >> 59) & 0xfull); }
+
 template <int Q, typename S, int MODE, int KIND>
 __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) {
     using R = typename Store<S>::real;
@@ -338,67 +349,48 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
     }
     const int64_t a = (int64_t)blockIdx.x * kStepThreads + threadIdx.x;
     const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
+    constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
 
     if (a < P.nact) {
-        const uint32_t word = __ldg(P.act_word + a);
-        const int64_t n = (int64_t)(word & 0x7fffffffu);
-        if (!(word >> 31)) {
-            // ---------------- interior fluid node: every neighbour is active
-            R f[Q];
+        const uint64_t word = __ldg(P.act_word + a);
+        const int64_t n = word_point(word);
+        const uint32_t miss = word_miss(word);  // zero on interior nodes
+
+        // ---- stream: one load per population, issued by every lane together.
+        // A link whose source is missing reads, in physics mode, the node's
+        // own opposite population (half-way bounce-back); in parity mode any
+        // valid address -- the previous value replaces it below.
+        R g[Q];
 #pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                const int64_t src = direct ? n : n - nb_off<Q>(q, P.nx, P.nxy);
-                f[q] = Store<S>::template load<Q>(fin + q * P.stride + src, q);
-            }
-            if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
-                bool zero = false;
-#pragma unroll
-                for (int q = 0; q < Q; ++q) zero |= is_exact_zero<Q, R, OFF>(f[q], q);
-                if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
-            }
-            if constexpr (KIND == KIND_READOUT) {
-                R r, ux, uy, uz;
-                moments<Q, R, OFF>(f, r, ux, uy, uz);
-                const double rho = OFF ? 1.0 + (double)r : (double)r;
-                part[0] = OFF ? (double)r : rho - 1.0;
-                part[1] = rho * ux; part[2] = rho * uy; part[3] = rho * uz;
-                if (P.out_f) {
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(f[q], q);
-                }
+        for (int q = 0; q < Q; ++q) {
+            const bool src_missing = !direct && ((miss >> Lat<Q>::opp(q)) & 1u);
+            const S* p;
+            if (direct) {
+                p = fin + q * P.stride + n;
+            } else if (MODE == MODE_PHYSICS) {
+                p = src_missing ? fin + Lat<Q>::opp(q) * P.stride + n
+                                : fin + q * P.stride + n - nb_off<Q>(q, P.nx, P.nxy);
             } else {
-                R r, ux, uy, uz;
-                collide<Q, R, OFF>(f, inv_tau, r, ux, uy, uz);
-                if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
-#pragma unroll
-                for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(f[q], q);
+                p = fin + q * P.stride + (src_missing ? n : n - nb_off<Q>(q, P.nx, P.nxy));
             }
-        } else {
-            // ---------------- boundary-list node
+            g[q] = Store<S>::template load<Q>(p, q);  // w_opp(q) == w_q: same decode
+        }
+
+        if (word_special(word)) {
+            // ---- boundary-list node: history, boundary rules, wall shear stress
             const int64_t s = __ldg(P.sp_of_act + a);
-            const uint32_t miss = __ldg(P.sp_miss + s);
-            const int c = __ldg(P.sp_cls + s);
-            const int nw = __ldg(P.sp_nw + s);
+            const int c = word_class(word);
             R* __restrict__ stale = static_cast<R*>(P.stale);
-            const bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
-            R g[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) {
+            if constexpr (MODE == MODE_PARITY) {
                 if (parity_readout) {
                     // the boundary list keeps the exact post-boundary f of the last step
-                    g[q] = stale[q * P.nsp + s];
-                } else if (direct) {
-                    g[q] = Store<S>::template load<Q>(fin + q * P.stride + n, q);
-                } else if ((miss >> Lat<Q>::opp(q)) & 1u) {
-                    // source x - c_q is solid / outside the box
-                    if constexpr (MODE == MODE_PARITY) g[q] = stale[q * P.nsp + s];
-                    else g[q] = Store<S>::template load<Q>(fin + Lat<Q>::opp(q) * P.stride + n, Lat<Q>::opp(q));
-                } else {
-                    R v = Store<S>::template load<Q>(fin + q * P.stride + n - nb_off<Q>(q, P.nx, P.nxy), q);
-                    if constexpr (MODE == MODE_PARITY) {
-                        if (is_exact_zero<Q, R, OFF>(v, q)) v = stale[q * P.nsp + s];
-                    }
-                    g[q] = v;
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) g[q] = stale[q * P.nsp + s];
+                } else if (!direct) {
+#pragma unroll
+                    for (int q = 0; q < Q; ++q)
+                        if (((miss >> Lat<Q>::opp(q)) & 1u) || is_exact_zero<Q, R, OFF>(g[q], q))
+                            g[q] = stale[q * P.nsp + s];
                 }
             }
             if (!direct && !parity_readout) {
@@ -418,67 +410,84 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                 }
             }
             if constexpr (KIND == KIND_READOUT) {
-                R r, ux, uy, uz;
-                moments<Q, R, OFF>(g, r, ux, uy, uz);
-                const double rho = OFF ? 1.0 + (double)r : (double)r;
-                part[0] = OFF ? (double)r : rho - 1.0;
-                const double j[3] = {rho * ux, rho * uy, rho * uz};
-                part[1] = j[0]; part[2] = j[1]; part[3] = j[2];
-                if (c >= CLS_BC0) part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
-                if (P.out_f) {
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
+                if (c >= CLS_BC0) {
+                    R r, ux, uy, uz;
+                    moments<Q, R, OFF>(g, r, ux, uy, uz);
+                    const double rho = OFF ? 1.0 + (double)r : (double)r;
+                    const double j[3] = {rho * ux, rho * uy, rho * uz};
+                    part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
                 }
             } else {
+                const int nw = __ldg(P.sp_nw + s);
                 R* __restrict__ prev = static_cast<R*>(P.nw_prev);
-                if constexpr (KIND == KIND_STEP) {
-                    if (nw >= 0) {
-                        double t[3];
-                        const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
-                        if constexpr (MODE == MODE_PARITY) {
-                            // equilibrium of the previous collision (time-lagged, as the reference)
-                            R e[Q];
-                            feq_all<Q, R, OFF>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
-                                               prev[3 * P.nnw + nw]);
-                            if constexpr (!OFF) {
-                                wss_reference<Q>(g, e, nn, P.wss_C, t);
-                            } else {
-                                const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
-                                R tr[3];
-                                wss_fast<Q, R>(g, e, nr, (R)P.wss_C, tr);
-                                t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
-                            }
+                if (KIND == KIND_STEP && nw >= 0) {
+                    double t[3];
+                    const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
+                    if constexpr (MODE == MODE_PARITY) {
+                        // equilibrium of the previous collision (time-lagged, as the reference)
+                        R e[Q];
+                        feq_all<Q, R, OFF>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
+                                           prev[3 * P.nnw + nw]);
+                        if constexpr (!OFF) {
+                            wss_reference<Q>(g, e, nn, P.wss_C, t);
                         } else {
-                            // stress of the same post-boundary f, with the (1 - 1/2tau) factor
-                            R e[Q], r, ux, uy, uz;
-                            moments<Q, R, OFF>(g, r, ux, uy, uz);
-                            feq_all<Q, R, OFF>(e, r, ux, uy, uz);
                             const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
                             R tr[3];
-                            wss_fast<Q, R>(g, e, nr, (R)(-(1.0 - 0.5 / P.tau) * P.wss_C), tr);
+                            wss_fast<Q, R>(g, e, nr, (R)P.wss_C, tr);
                             t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
                         }
-                        const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-                        P.nw_wss[nw] = W;
-                        P.nw_acc[nw] += t[0];
-                        P.nw_acc[P.nnw + nw] += t[1];
-                        P.nw_acc[2 * P.nnw + nw] += t[2];
-                        P.nw_accm[nw] += W;
+                    } else {
+                        // stress of the same post-boundary f, with the (1 - 1/2tau) factor
+                        R e[Q], r, ux, uy, uz;
+                        moments<Q, R, OFF>(g, r, ux, uy, uz);
+                        feq_all<Q, R, OFF>(e, r, ux, uy, uz);
+                        const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
+                        R tr[3];
+                        wss_fast<Q, R>(g, e, nr, (R)(-(1.0 - 0.5 / P.tau) * P.wss_C), tr);
+                        t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
                     }
+                    const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                    P.nw_wss[nw] = W;
+                    P.nw_acc[nw] += t[0];
+                    P.nw_acc[P.nnw + nw] += t[1];
+                    P.nw_acc[2 * P.nnw + nw] += t[2];
+                    P.nw_accm[nw] += W;
                 }
                 if constexpr (MODE == MODE_PARITY) {
 #pragma unroll
                     for (int q = 0; q < Q; ++q) stale[q * P.nsp + s] = g[q];
+                    if (nw >= 0) {
+                        // moments of this step's collision, for the next step's lagged stress
+                        R r, ux, uy, uz;
+                        moments<Q, R, OFF>(g, r, ux, uy, uz);
+                        prev[nw] = r; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
+                    }
                 }
-                R r, ux, uy, uz;
-                collide<Q, R, OFF>(g, inv_tau, r, ux, uy, uz);
-                if (!(fabs((double)r) < 1e30)) atomicOr(P.flags, FLAG_NONFINITE);
-                if (MODE == MODE_PARITY && nw >= 0) {
-                    prev[nw] = r; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
-                }
-#pragma unroll
-                for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(g[q], q);
             }
+        } else if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
+            bool zero = false;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) zero |= is_exact_zero<Q, R, OFF>(g[q], q);
+            if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
+        }
+
+        // ---- collide and store (every lane), or read out
+        if constexpr (KIND == KIND_READOUT) {
+            R r, ux, uy, uz;
+            moments<Q, R, OFF>(g, r, ux, uy, uz);
+            const double rho = OFF ? 1.0 + (double)r : (double)r;
+            part[0] = OFF ? (double)r : rho - 1.0;
+            part[1] = rho * ux; part[2] = rho * uy; part[3] = rho * uz;
+            if (P.out_f) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
+            }
+        } else {
+            R r, ux, uy, uz;
+            collide<Q, R, OFF>(g, inv_tau, r, ux, uy, uz);
+            if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(g[q], q);
         }
     }
     if constexpr (KIND == KIND_STEP) {

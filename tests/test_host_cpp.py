@@ -1,0 +1,88 @@
+"""The C++ host layer (reference class names over the C ABI)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, fixtures, load
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BUILD = os.path.join(ROOT, "pv_dec_original_gb300", "_build")
+HOST_INC = os.path.join(ROOT, "pv_dec_original_gb300", "csrc", "host")
+
+
+def _compile(tmp_path, src, name):
+    from pv_dec_original_gb300 import build
+    build.build()
+    exe = str(tmp_path / name)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-I",
+                    HOST_INC, src, "-o", exe, f"-L{BUILD}", "-llbm_host", "-llbm_gb300", f"-Wl,-rpath,{BUILD}"],
+                   check=True)
+    return exe
+
+
+def test_host_layer_cpu(tmp_path, oracle_lib):
+    exe = _compile(tmp_path, os.path.join(ROOT, "tests", "cpp", "host_cpu_test.cpp"), "host_cpu_test")
+    cfg = tmp_path / "c.cfg"
+    cfg.write_text("# comment\nspacing 0.05\ntau 1.5\n\ndt 8e-6\nConditions: inlet\nu = 1\nEquation\n")
+    out = subprocess.run([exe, str(cfg)], capture_output=True, text=True, check=True).stdout.split("\n")
+    kv = [l.split() for l in out if l]
+    assert ["config_ok", "0"] in kv  # "Conditions: inlet" is not numeric -> the read fails, as the reference's
+    cfg.write_text("# comment\nspacing 0.05\ntau 1.5\n\ndt 8e-6\n")
+    out = subprocess.run([exe, str(cfg)], capture_output=True, text=True, check=True).stdout.split("\n")
+    kv = [l.split() for l in out if l]
+    conf = {k[1]: float(k[2]) for k in kv if k[0] == "config"}
+    assert conf == {"spacing": 0.05, "tau": 1.5, "dt": 8e-6}
+    for Q in (19, 27):
+        c, w, opp = oracle_lib.lattice(Q)
+        rows = [k for k in kv if k[0] == "lattice" and int(k[1]) == Q]
+        assert len(rows) == Q
+        for r in rows:
+            q = int(r[2])
+            assert [int(r[3]), int(r[4]), int(r[5])] == list(c[q])
+            assert float(r[6]) == w[q] and int(r[7]) == opp[q]
+        assert [int(k[2]) for k in kv if k[0] == "unknowns" and int(k[1]) == Q] == [5 if Q == 19 else 9] * 6
+    d = load(os.path.join(GOLDEN, "pulse.npz"))
+    pulse = {int(k[1]): float(k[2]) for k in kv if k[0] == "pulse"}
+    got = np.array([pulse[int(i)] for i in d["idx"]])
+    np.testing.assert_allclose(got, d["v"], rtol=1e-14, atol=1e-15)
+
+
+@pytest.mark.gpu
+def test_lbm_run_end_to_end_vs_oracle(tmp_path, gpu_lib, oracle_lib):
+    """lbm_run (the reference's driver on the GPU engine) on a golden elbow:
+    FP64 parity with a velocity inlet and a density outlet; the CSV output
+    matches the oracle run with the same inlet table."""
+    from pv_dec_original_gb300 import build, geometry as G, waveform
+    from helpers import classify
+    build.build()
+    d = load(fixtures("sim")[0])
+    tri = d["tri12"]
+    stl = str(tmp_path / "e.stl")
+    G.write_stl_ascii(stl, G.Surface(tri[:, :9].reshape(-1, 3, 3).copy(), tri[:, 9:].copy()))
+    dt, end = 8e-6, 8e-6 * 30.5   # 31 iterations (t = 0 .. 30 dt)
+    cfg = tmp_path / "run.cfg"
+    cfg.write_text(f"stl {stl}\nspacing 1.0\ntau 0.8\ndt {dt!r}\nend_time {end!r}\noutput_every 30\n"
+                   f"output_dir {tmp_path}\nprecision 0\nmode 0\ninlet_face 0\ninlet_plane -1\n"
+                   f"outlet_face 4\noutlet_plane -1\n")
+    r = subprocess.run([os.path.join(BUILD, "lbm_run"), str(cfg)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "steps 31" in r.stdout
+    csv = np.loadtxt(str(tmp_path / "FlowHemodynamics" / "30_FlowHemodynamics.csv"), delimiter=",", skiprows=1)
+    assert (tmp_path / "Fluid_Variables" / "30.vtu").exists()
+    mask, bb, dims = oracle_lib.voxelize(tri, 1.0)
+    fl = np.argwhere(mask > 0)
+    kin, kout = int(fl[:, 2].min()), int(fl[:, 0].min())
+    bcs = [dict(kind=oracle_lib.BC_VELOCITY, face=0, plane=kin, value=1.0),
+           dict(kind=oracle_lib.BC_PRESSURE, face=4, plane=kout, value=1.0)]
+    cls = classify(mask, [(0, kin), (2, kout)])
+    o = oracle_lib.Sim(19, oracle_lib.PARITY, cls, (bb[0], bb[2], bb[4]), 1.0, 0.8, bcs)
+    o.set_amplitude(waveform.reference_table(dt, 31))
+    o.set_wss(1060.0 * (dt * dt) / ((1.0 * 1.0) * 1e-6), 0.9)
+    o.compute_normals(tri)
+    o.step(31)
+    nw = o.nw()
+    assert len(csv) == len(nw["pt"])
+    np.testing.assert_allclose(csv[:, 3], nw["wss"], rtol=2e-5, atol=1e-12)
+    np.testing.assert_allclose(csv[:, 5], nw["tawss"], rtol=2e-5, atol=1e-12)
