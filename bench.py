@@ -284,6 +284,7 @@ def run_ours(args):
     flush = cr.malloc(L2_FLUSH_BYTES)
 
     s.step(args.warmup)
+    tuned = s.autotune(10) if not args.no_tune else (0, [])
     if dist is not None:
         dist.barrier()
     cr.ck(cr.L.cudaStreamSynchronize(C.c_void_p(stream)), "sync")
@@ -306,6 +307,8 @@ def run_ours(args):
     if args.precision == "f32" and not args.quick:
         s16, _ = make_solver(capi, mask, surf, tri, args.Q, "f16", origin, local)
         s16.step(args.warmup)
+        if not args.no_tune:
+            s16.autotune(10)
         ms16 = time_steps(cr, s16, args.steps, flush, s16.stream())
         m16 = sum(ms16) / len(ms16)
         extra["f16_store"] = {"mlups": active / (m16 * 1e-3) / 1e6,
@@ -383,6 +386,8 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h,
                     "step": f"{B} LBM steps per call batch + WSS/OSI/TAWSS and rho/u read-back (pinned host buffers)"},
             "gpu_launches": launches,
+            "autotune": {"variant": tuned[0], "ms_per_step_by_variant": tuned[1],
+                         "variants": "(block, min blocks/SM): (256,1) (256,4) (128,8) (512,2) (128,1)"},
             "clocks": clk.summary(),
             "extra": extra,
         }
@@ -448,6 +453,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the secondary FP16 measurement")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

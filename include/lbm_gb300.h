@@ -228,6 +228,16 @@ lbm_status lbm_get_launch_count(lbm_handle* h, int64_t* launches);
 /* Steps per captured CUDA graph (0 = launch kernels directly). */
 lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph);
 
+/* Launch-shape variants of the step kernel (block size x minimum resident
+ * blocks per SM).  lbm_autotune times each variant for trial_steps steps on a
+ * snapshot of the current state, restores the state, keeps the fastest and
+ * reports it (and, if ms_per_step is not NULL, the time of every variant:
+ * LBM_NUM_VARIANTS floats).  No reference counterpart (the reference has a
+ * single serial loop). */
+#define LBM_NUM_VARIANTS 5
+lbm_status lbm_autotune(lbm_handle* h, int trial_steps, int* best, float* ms_per_step);
+lbm_status lbm_set_variant(lbm_handle* h, int variant);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,9 @@ UNITS = [
     ("voxelize.cu", False),
     ("setup.cu", False),
     ("step_f64.cu", False),
+    ("step_f32.cu", True),
+    ("step_f16.cu", True),
+    ("step_bf16.cu", True),
     ("step_fast.cu", True),
     ("capi.cu", False),
 ]

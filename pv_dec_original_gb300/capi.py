@@ -61,8 +61,9 @@ EXPORTS = [
     "lbm_set_geometry", "lbm_set_normals_from_surface", "lbm_set_inlet_table", "lbm_init_equilibrium",
     "lbm_init_from_macro", "lbm_step", "lbm_step_async", "lbm_check_status", "lbm_sync", "lbm_get_counts", "lbm_get_classes", "lbm_get_distributions",
     "lbm_set_distributions", "lbm_get_macro", "lbm_get_wss", "lbm_get_conservation", "lbm_save", "lbm_load",
-    "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps",
+    "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_autotune", "lbm_set_variant",
 ]
+NUM_VARIANTS = 5
 
 
 def lib_path() -> str:
@@ -113,6 +114,8 @@ def load(build_if_missing: bool = True):
     L.lbm_get_stream.argtypes = [P, C.POINTER(P)]
     L.lbm_get_launch_count.argtypes = [P, C.POINTER(C.c_int64)]
     L.lbm_set_graph_steps.argtypes = [P, C.c_int]
+    L.lbm_autotune.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+    L.lbm_set_variant.argtypes = [P, C.c_int]
     _lib = L
     return L
 
@@ -242,6 +245,16 @@ class Solver:
 
     def set_graph_steps(self, n):
         self._c(load().lbm_set_graph_steps(self.h, int(n)))
+
+    def autotune(self, trial_steps=10):
+        """Time every launch variant on a snapshot of the state; keep the fastest."""
+        best = C.c_int()
+        ms = (C.c_float * NUM_VARIANTS)()
+        self._c(load().lbm_autotune(self.h, int(trial_steps), C.byref(best), ms))
+        return best.value, list(ms)
+
+    def set_variant(self, v):
+        self._c(load().lbm_set_variant(self.h, int(v)))
 
     def counts(self) -> dict:
         c = Counts()

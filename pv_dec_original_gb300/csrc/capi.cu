@@ -59,6 +59,7 @@ struct lbm_handle {
     cudaGraphExec_t gexec = nullptr;
     int gexec_parity = -1;
     int gexec_cur = -1;
+    int variant = 0;            // launch shape of the step kernel (lbm_autotune)
     size_t geo_bytes = 0;
     lbm_counts counts{};
 };
@@ -191,8 +192,12 @@ StepParams make_params(lbm_handle* h, int kind) {
 
 cudaError_t launch(lbm_handle* h, int kind, const StepParams& p) {
     h->launches++;
-    if (h->d.precision == LBM_F64) return launch_step_f64(h->d.Q, h->d.mode, kind, p, h->st);
-    return launch_step_fast(h->d.Q, h->d.precision, h->d.mode, kind, p, h->st);
+    switch (h->d.precision) {
+        case LBM_F64: return launch_step_f64(h->d.Q, h->d.mode, kind, h->variant, p, h->st);
+        case LBM_F32: return launch_step_f32(h->d.Q, h->d.mode, kind, h->variant, p, h->st);
+        case LBM_F16: return launch_step_f16(h->d.Q, h->d.mode, kind, h->variant, p, h->st);
+        default: return launch_step_bf16(h->d.Q, h->d.mode, kind, h->variant, p, h->st);
+    }
 }
 
 // buf[0] holds f^N at each point's own index: collide it into buf[1].
@@ -853,6 +858,98 @@ lbm_status lbm_load(lbm_handle* h, const char* path) {
     }
     h->steps = sz[2];
     return lbm_set_distributions(h, f.data());
+}
+
+lbm_status lbm_set_variant(lbm_handle* h, int variant) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, variant >= 0 && variant < kNumVariants, LBM_ERR_ARG, "variant out of range");
+    drop_graph(h);
+    h->variant = variant;
+    return LBM_OK;
+}
+
+lbm_status lbm_autotune(lbm_handle* h, int trial_steps, int* best, float* ms_per_step) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state: set the geometry first");
+    REQUIRE(h, trial_steps > 0, LBM_ERR_ARG, "trial_steps must be > 0");
+    CK(h, cudaSetDevice(h->d.device));
+    CK(h, cudaStreamSynchronize(h->st));
+    // snapshot of everything a step writes, restored after every trial
+    const size_t fbytes = (size_t)elem_size(h->d.precision) * h->d.Q * h->stride;
+    const size_t rs = real_size(h->d.precision);
+    struct Item { void* live; size_t bytes; void* copy; };
+    std::vector<Item> items = {
+        {h->buf[0], fbytes, nullptr}, {h->buf[1], fbytes, nullptr}, {h->slots, 2 * sizeof(int64_t), nullptr},
+        {h->flags, sizeof(unsigned), nullptr},
+        {h->nw_acc, sizeof(double) * 3 * (h->g.nnw + 1), nullptr},
+        {h->nw_accm, sizeof(double) * (h->g.nnw + 1), nullptr},
+        {h->nw_wss, sizeof(double) * (h->g.nnw + 1), nullptr}};
+    if (h->stale) items.push_back({h->stale, rs * h->d.Q * (h->g.nsp + 1), nullptr});
+    if (h->nw_prev) items.push_back({h->nw_prev, rs * 4 * (h->g.nnw + 1), nullptr});
+    auto release = [&]() {
+        for (Item& it : items)
+            if (it.copy) cudaFree(it.copy);
+    };
+    for (Item& it : items) {
+        cudaError_t e = cudaMalloc(&it.copy, it.bytes);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(it.copy, it.live, it.bytes, cudaMemcpyDeviceToDevice, h->st);
+        if (e != cudaSuccess) {
+            release();
+            return fail(h, LBM_ERR_ALLOC, std::string("autotune snapshot: ") + cudaGetErrorString(e));
+        }
+    }
+    const int64_t steps0 = h->steps, since0 = h->since_start, launches0 = h->launches;
+    const int cur0 = h->cur, v0 = h->variant;
+    auto restore = [&]() -> cudaError_t {
+        for (Item& it : items) {
+            cudaError_t e = cudaMemcpyAsync(it.live, it.copy, it.bytes, cudaMemcpyDeviceToDevice, h->st);
+            if (e != cudaSuccess) return e;
+        }
+        h->steps = steps0; h->since_start = since0; h->cur = cur0;
+        return cudaSuccess;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = 1e30f;
+    int best_v = v0;
+    cudaError_t err = cudaSuccess;
+    for (int v = 0; v < kNumVariants && err == cudaSuccess; ++v) {
+        err = restore();
+        if (err != cudaSuccess) break;
+        h->variant = v;
+        for (int k = 0; k < 2 && err == cudaSuccess; ++k) {  // warm-up
+            err = launch(h, 0, make_params(h, 0));
+            h->cur ^= 1;
+            h->steps++;
+        }
+        if (err != cudaSuccess) break;
+        cudaEventRecord(e0, h->st);
+        for (int k = 0; k < trial_steps && err == cudaSuccess; ++k) {
+            err = launch(h, 0, make_params(h, 0));
+            h->cur ^= 1;
+            h->steps++;
+        }
+        cudaEventRecord(e1, h->st);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)trial_steps;
+        if (ms_per_step) ms_per_step[v] = ms;
+        if (err == cudaSuccess && ms < best_ms) { best_ms = ms; best_v = v; }
+    }
+    cudaError_t e2 = restore();
+    if (err == cudaSuccess) err = e2;
+    if (err == cudaSuccess) err = cudaStreamSynchronize(h->st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    release();
+    h->launches = launches0;
+    h->variant = best_v;
+    drop_graph(h);
+    if (err != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(err));
+    if (best) *best = best_v;
+    return LBM_OK;
 }
 
 lbm_status lbm_get_stream(lbm_handle* h, void** stream) {

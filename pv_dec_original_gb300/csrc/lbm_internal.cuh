@@ -71,8 +71,11 @@ constexpr int kStepThreads = 256;
 
 // Launchers (one per translation unit family).  kind: 0 step, 1 prologue
 // (collide the initial state), 2 materialize (post-boundary f + sums).
-cudaError_t launch_step_f64(int Q, int mode, int kind, const StepParams& p, cudaStream_t s);
-cudaError_t launch_step_fast(int Q, int precision, int mode, int kind, const StepParams& p, cudaStream_t s);
+constexpr int kNumVariants = 5;  // launch-shape variants of the step kernel (step_kernels.cuh)
+cudaError_t launch_step_f64(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
+cudaError_t launch_step_f32(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
+cudaError_t launch_step_f16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
+cudaError_t launch_step_bf16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 
 // State initialisation: what = 0 fills f = w on every point, what = 1
 // scatters fa[a*Q + q] (FP64, per active node) into the planes.

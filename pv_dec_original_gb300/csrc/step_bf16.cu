@@ -1,0 +1,10 @@
+// BF16 storage of relative offsets, FP32 arithmetic, FMA contraction on.
+#include "step_kernels.cuh"
+
+namespace lbm {
+
+cudaError_t launch_step_bf16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t st) {
+    return launch_typed<__nv_bfloat16>(Q, mode, kind, variant, p, st);
+}
+
+}  // namespace lbm

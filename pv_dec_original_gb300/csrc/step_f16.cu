@@ -1,0 +1,10 @@
+// FP16 storage of scaled relative offsets, FP32 arithmetic, FMA contraction on.
+#include "step_kernels.cuh"
+
+namespace lbm {
+
+cudaError_t launch_step_f16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t st) {
+    return launch_typed<__half>(Q, mode, kind, variant, p, st);
+}
+
+}  // namespace lbm

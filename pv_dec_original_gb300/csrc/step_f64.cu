@@ -7,8 +7,8 @@
 
 namespace lbm {
 
-cudaError_t launch_step_f64(int Q, int mode, int kind, const StepParams& p, cudaStream_t st) {
-    return launch_typed<double>(Q, mode, kind, p, st);
+cudaError_t launch_step_f64(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t st) {
+    return launch_typed<double>(Q, mode, kind, variant, p, st);
 }
 
 cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,

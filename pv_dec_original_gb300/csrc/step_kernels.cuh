@@ -274,17 +274,23 @@ __device__ __forceinline__ void wss_reference(const double (&f)[Q], const double
     }
 }
 
-// Same quantity, factored: tau_i = C sum_a f_ne (c.n)(c_i - (c.n) n_i).
-template <int Q, typename R>
-__device__ __forceinline__ void wss_fast(const R (&f)[Q], const R (&feq)[Q], const R n[3], R C, R tau_i[3]) {
+// Same quantity, factored: tau_i = C sum_a f_ne (c.n)(c_i - (c.n) n_i), with
+// the equilibrium of moments (r, u) evaluated inside the loop.
+template <int Q, typename R, bool OFF>
+__device__ __forceinline__ void wss_fast(const R (&f)[Q], R r, R ux, R uy, R uz, const R n[3], R C, R tau_i[3]) {
+    const R usqr = ux * ux + uy * uy + uz * uz;
     R a0 = R(0), a1 = R(0), a2 = R(0);
 #pragma unroll
     for (int al = 0; al < Q; ++al) {
-        const R cn = (R)Lat<Q>::cx(al) * n[0] + (R)Lat<Q>::cy(al) * n[1] + (R)Lat<Q>::cz(al) * n[2];
-        const R k = (f[al] - feq[al]) * cn;
-        a0 += k * ((R)Lat<Q>::cx(al) - cn * n[0]);
-        a1 += k * ((R)Lat<Q>::cy(al) - cn * n[1]);
-        a2 += k * ((R)Lat<Q>::cz(al) - cn * n[2]);
+        const R cx = (R)Lat<Q>::cx(al), cy = (R)Lat<Q>::cy(al), cz = (R)Lat<Q>::cz(al);
+        const R du = ux * cx + uy * cy + uz * cz;
+        const R e = OFF ? (R)Lat<Q>::w(al) * (r + (R(1) + r) * (R(3.0) * du + R(4.5) * du * du - R(1.5) * usqr))
+                        : (R)Lat<Q>::w(al) * r * (R(1.0) + R(3.0) * du + R(4.5) * du * du - R(1.5) * usqr);
+        const R cn = cx * n[0] + cy * n[1] + cz * n[2];
+        const R k = (f[al] - e) * cn;
+        a0 += k * (cx - cn * n[0]);
+        a1 += k * (cy - cn * n[1]);
+        a2 += k * (cz - cn * n[2]);
     }
     tau_i[0] = C * a0; tau_i[1] = C * a1; tau_i[2] = C * a2;
 }
@@ -292,8 +298,9 @@ __device__ __forceinline__ void wss_fast(const R (&f)[Q], const R (&feq)[Q], con
 // ---------------------------------------------------------------------------
 // Block reduction of the read-out sums (rho - 1, momentum, per-BC flux).
 
+template <int BT>
 __device__ __forceinline__ void block_partials(double (&v)[kPartialStride], double* __restrict__ out) {
-    __shared__ double red[kStepThreads / 32][kPartialStride];
+    __shared__ double red[BT / 32][kPartialStride];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < kPartialStride; ++k) {
@@ -305,7 +312,7 @@ __device__ __forceinline__ void block_partials(double (&v)[kPartialStride], doub
     __syncthreads();
     if (threadIdx.x < kPartialStride) {
         double s = 0.0;
-        for (int w = 0; w < kStepThreads / 32; ++w) s += red[w][threadIdx.x];
+        for (int w = 0; w < BT / 32; ++w) s += red[w][threadIdx.x];
         out[(int64_t)blockIdx.x * kPartialStride + threadIdx.x] = s;
     }
 }
@@ -335,8 +342,8 @@ __device__ __forceinline__ bool word_special(uint64_t w) { return (w >> 31) & 1u
 __device__ __forceinline__ uint32_t word_miss(uint64_t w) { return (uint32_t)((w >> 32) & 0x7ffffffull); }
 __device__ __forceinline__ int word_class(uint64_t w) { return (int)((w >> 59) & 0xfull); }
 
-template <int Q, typename S, int MODE, int KIND>
-__global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) {
+template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1>
+__global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
     using R = typename Store<S>::real;
     constexpr bool OFF = Store<S>::offset;
     const S* __restrict__ fin = static_cast<const S*>(P.fin);
@@ -347,7 +354,7 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
 #pragma unroll
         for (int k = 0; k < kPartialStride; ++k) part[k] = 0.0;
     }
-    const int64_t a = (int64_t)blockIdx.x * kStepThreads + threadIdx.x;
+    const int64_t a = (int64_t)blockIdx.x * BT + threadIdx.x;
     const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
     constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
 
@@ -425,25 +432,25 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
                     const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
                     if constexpr (MODE == MODE_PARITY) {
                         // equilibrium of the previous collision (time-lagged, as the reference)
-                        R e[Q];
-                        feq_all<Q, R, OFF>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
-                                           prev[3 * P.nnw + nw]);
                         if constexpr (!OFF) {
+                            double e[Q];
+                            feq_all<Q, double, false>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
+                                                      prev[3 * P.nnw + nw]);
                             wss_reference<Q>(g, e, nn, P.wss_C, t);
                         } else {
                             const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
                             R tr[3];
-                            wss_fast<Q, R>(g, e, nr, (R)P.wss_C, tr);
+                            wss_fast<Q, R, OFF>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
+                                                prev[3 * P.nnw + nw], nr, (R)P.wss_C, tr);
                             t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
                         }
                     } else {
                         // stress of the same post-boundary f, with the (1 - 1/2tau) factor
-                        R e[Q], r, ux, uy, uz;
+                        R r, ux, uy, uz;
                         moments<Q, R, OFF>(g, r, ux, uy, uz);
-                        feq_all<Q, R, OFF>(e, r, ux, uy, uz);
                         const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
                         R tr[3];
-                        wss_fast<Q, R>(g, e, nr, (R)(-(1.0 - 0.5 / P.tau) * P.wss_C), tr);
+                        wss_fast<Q, R, OFF>(g, r, ux, uy, uz, nr, (R)(-(1.0 - 0.5 / P.tau) * P.wss_C), tr);
                         t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
                     }
                     const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
@@ -493,32 +500,58 @@ __global__ void __launch_bounds__(kStepThreads) step_kernel(const StepParams P) 
     if constexpr (KIND == KIND_STEP) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
     }
-    if constexpr (KIND == KIND_READOUT) block_partials(part, P.partials);
+    if constexpr (KIND == KIND_READOUT) block_partials<BT>(part, P.partials);
+}
+
+// Launch-shape variants of the step kernel, picked by the autotuner
+// (lbm_autotune): block size and the minimum resident blocks per SM, which
+// caps registers per thread (65536 / (BT * MINB)) to trade per-thread
+// registers for more warps in flight on this latency-bound stencil.
+struct Variant {
+    int bt, minb;
+};
+constexpr Variant kVariants[kNumVariants] = {{256, 1}, {256, 4}, {128, 8}, {512, 2}, {128, 1}};
+
+template <int Q, typename S, int MODE, int V>
+cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
+    constexpr int BT = kVariants[V].bt, MB = kVariants[V].minb;
+    const int64_t nblocks = ceil_div(p.nact, BT);
+    if (nblocks <= 0) return cudaSuccess;
+    if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    step_kernel<Q, S, MODE, KIND_STEP, BT, MB><<<(unsigned)nblocks, BT, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 template <int Q, typename S, int MODE>
-cudaError_t launch_family(int kind, const StepParams& p, cudaStream_t st) {
+cudaError_t launch_family(int kind, int variant, const StepParams& p, cudaStream_t st) {
+    if (kind == KIND_STEP) {
+        switch (variant) {
+            case 1: return launch_step_variant<Q, S, MODE, 1>(p, st);
+            case 2: return launch_step_variant<Q, S, MODE, 2>(p, st);
+            case 3: return launch_step_variant<Q, S, MODE, 3>(p, st);
+            case 4: return launch_step_variant<Q, S, MODE, 4>(p, st);
+            default: return launch_step_variant<Q, S, MODE, 0>(p, st);
+        }
+    }
+    // prologue and read-out: default shape (the read-out's partial sums are per 256-thread block)
     const int64_t nblocks = ceil_div(p.nact, kStepThreads);
     if (nblocks <= 0) return cudaSuccess;
     if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    switch (kind) {
-        case KIND_STEP: step_kernel<Q, S, MODE, KIND_STEP><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p); break;
-        case KIND_PROLOGUE:
-            step_kernel<Q, S, MODE, KIND_PROLOGUE><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p);
-            break;
-        default: step_kernel<Q, S, MODE, KIND_READOUT><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p); break;
-    }
+    if (kind == KIND_PROLOGUE)
+        step_kernel<Q, S, MODE, KIND_PROLOGUE><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p);
+    else
+        step_kernel<Q, S, MODE, KIND_READOUT><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 
 template <typename S>
-cudaError_t launch_typed(int Q, int mode, int kind, const StepParams& p, cudaStream_t st) {
+cudaError_t launch_typed(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t st) {
     if (Q == 19) {
-        return mode == MODE_PARITY ? launch_family<19, S, MODE_PARITY>(kind, p, st)
-                                   : launch_family<19, S, MODE_PHYSICS>(kind, p, st);
+        return mode == MODE_PARITY ? launch_family<19, S, MODE_PARITY>(kind, variant, p, st)
+                                   : launch_family<19, S, MODE_PHYSICS>(kind, variant, p, st);
     }
-    return mode == MODE_PARITY ? launch_family<27, S, MODE_PARITY>(kind, p, st)
-                               : launch_family<27, S, MODE_PHYSICS>(kind, p, st);
+    return mode == MODE_PARITY ? launch_family<27, S, MODE_PARITY>(kind, variant, p, st)
+                               : launch_family<27, S, MODE_PHYSICS>(kind, variant, p, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,82 @@
+"""Synthetic geometry generators: closed surfaces, outward normals, lattice
+sizing through bbox anchors."""
+import numpy as np
+import pytest
+
+from pv_dec_original_gb300 import geometry as G
+
+
+def _edges_closed(surf):
+    """Every directed edge (a->b) of a closed, consistently oriented surface
+    appears reversed (b->a) exactly once."""
+    v = np.round(surf.v, 9)
+    keys = {}
+    for t in range(surf.ntri):
+        for k in range(3):
+            a, b = tuple(v[t, k]), tuple(v[t, (k + 1) % 3])
+            keys[(a, b)] = keys.get((a, b), 0) + 1
+    return all(keys.get((b, a), 0) == n for (a, b), n in keys.items())
+
+
+def _enclosed_volume(surf):
+    v = surf.v
+    return float(np.einsum("ij,ij->i", v[:, 0], np.cross(v[:, 1], v[:, 2])).sum() / 6.0)
+
+
+@pytest.mark.parametrize("maker", [
+    lambda: G.capped_cylinder(10.0, 100.0, 48),
+    lambda: G.elbow(radius=4.0, leg=12.0, h=1.5, exit="z-"),
+    lambda: G.elbow(radius=4.0, leg=12.0, h=1.5, exit="y+"),
+    lambda: G.stenosed_tube(5.0, 30.0, 0.5, 0.2, h=1.2),
+    lambda: G.y_bifurcation(6.0, 4.25, 30.0, z_in=1.3, z_out=60.6, z_split=38.0, h=1.5),
+], ids=["cylinder", "elbow_z", "elbow_y", "stenosis", "bifurcation"])
+def test_surfaces_closed_and_outward(maker):
+    s = maker()
+    assert s.ntri > 0
+    assert _edges_closed(s)
+    assert _enclosed_volume(s) > 0  # outward orientation
+    # file normals agree with the vertex winding
+    n = np.cross(s.v[:, 1] - s.v[:, 0], s.v[:, 2] - s.v[:, 0])
+    assert np.all((n * s.n).sum(axis=1) > 0)
+
+
+def test_cylinder_volume_close_to_analytic():
+    s = G.capped_cylinder(10.0, 100.0, 48)
+    vol = _enclosed_volume(s)
+    poly = 0.5 * 48 * 10.0 ** 2 * np.sin(2 * np.pi / 48) * 100.0
+    assert abs(vol - poly) < 1e-6 * poly
+
+
+def test_stenosis_removes_requested_area():
+    s = G.stenosed_tube(10.0, 80.0, 0.5, 0.0, h=0.8)
+    # the SDF throat radius is r (1 - k) with k = 1 - sqrt(1 - severity)
+    z = s.v[..., 2]
+    throat = s.v[np.abs(z - 40.0) < 0.5]
+    r = np.hypot(throat[:, 0], throat[:, 1]).max()
+    assert abs(r - 10.0 * np.sqrt(0.5)) < 0.8
+
+
+@pytest.mark.parametrize("cfg,dims", [(G.config_c1_cylinder, (24, 24, 104))])
+def test_anchor_lattice(cfg, dims):
+    s = cfg()
+    bb, d = G.reference_lattice_dims(s.tri12(), 1.0)
+    assert d == dims
+
+
+def test_c2_lattice_and_stl_round_trip(tmp_path):
+    s = G.config_c2_bifurcation()
+    _, d = G.reference_lattice_dims(s.tri12(), 1.0)
+    assert d == (256, 192, 512)
+    p = str(tmp_path / "c2.stl")
+    G.write_stl_ascii(p, s)
+    assert np.array_equal(G.read_stl_ascii(p), s.tri12())
+
+
+def test_ensemble_members_seeded():
+    a = G.config_c4_ensemble(3, seed=7)
+    b = G.config_c4_ensemble(3, seed=7)
+    for x, y in zip(a, b):
+        assert np.array_equal(x["surface"].v, y["surface"].v)
+        assert 8 <= x["radius"] <= 20 and 120 <= x["length"] <= 400
+        assert 0.2 <= x["severity"] <= 0.7 and 0 <= x["eccentricity"] <= 0.3
+        assert 2000 <= x["period"] <= 6000 and 0.01 <= x["inlet_mean"] <= 0.04

@@ -171,3 +171,25 @@ def test_gpu_divergence_reports_status(gpu_lib):
         for _ in range(50):
             s.step(20)
     assert e.value.code == -4
+
+
+def test_gpu_autotune_restores_state(gpu_lib):
+    """Autotuning times every launch variant on a snapshot and restores the
+    state: FP64 parity results are bit-identical with or without it, and every
+    variant computes the same step."""
+    d = load(fixtures("sim")[0])
+    a, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64)
+    b, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64, split=10)  # 10 steps, then the rest
+    fa = a.distributions()
+    # rerun b from scratch with an autotune after 10 steps
+    c, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64, split=None)
+    best, ms = c.autotune(3)
+    assert 0 <= best < gpu_lib.NUM_VARIANTS and all(m > 0 for m in ms)
+    assert np.array_equal(c.distributions(), fa)
+    for v in range(gpu_lib.NUM_VARIANTS):
+        e, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64, split=5)
+        e.set_variant(v)
+        e.step(5)
+        r, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64, split=5)
+        r.step(5)
+        assert np.array_equal(e.distributions(), r.distributions()), v
