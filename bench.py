@@ -284,7 +284,11 @@ def run_ours(args):
     flush = cr.malloc(L2_FLUSH_BYTES)
 
     s.step(args.warmup)
-    tuned = s.autotune(10) if not args.no_tune else (0, [])
+    if args.variant is not None:
+        s.set_variant(args.variant)
+        tuned = (args.variant, [])
+    else:
+        tuned = s.autotune(10) if not args.no_tune else (0, [])
     if dist is not None:
         dist.barrier()
     cr.ck(cr.L.cudaStreamSynchronize(C.c_void_p(stream)), "sync")
@@ -307,7 +311,9 @@ def run_ours(args):
     if args.precision == "f32" and not args.quick:
         s16, _ = make_solver(capi, mask, surf, tri, args.Q, "f16", origin, local)
         s16.step(args.warmup)
-        if not args.no_tune:
+        if args.variant is not None:
+            s16.set_variant(args.variant)
+        elif not args.no_tune:
             s16.autotune(10)
         ms16 = time_steps(cr, s16, args.steps, flush, s16.stream())
         m16 = sum(ms16) / len(ms16)
@@ -454,6 +460,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the secondary FP16 measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--variant", type=int, default=None, help="force a launch shape (skips the autotuner)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

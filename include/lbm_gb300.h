@@ -192,7 +192,7 @@ typedef struct {
     int64_t bc[LBM_MAX_BC]; /* nodes per boundary condition */
     int64_t next_to_wall;
     int64_t special;  /* boundary + next-to-wall nodes (the boundary list) */
-    int64_t segments; /* warps of the step kernel (32 active nodes each) */
+    int64_t segments; /* pull segments (stretches of active nodes sharing neighbour offsets) */
     int64_t steps;    /* steps taken */
     int64_t device_bytes; /* device memory held by the handle */
 } lbm_counts;

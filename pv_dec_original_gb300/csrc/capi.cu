@@ -32,6 +32,8 @@ struct lbm_handle {
     std::string err;
     int nx = 0, ny = 0, nz = 0;
     int64_t npts = 0, stride = 0;
+    int32_t* seg_delta = nullptr;  // per pull segment: Q offsets in active-index space
+    int64_t nseg = 0;
     GeometryLists g;
     bool has_geo = false;
     bool has_state = false;
@@ -132,12 +134,14 @@ void free_geometry(lbm_handle* h) {
     void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_prof, g.nw_pt, g.act_word, g.sp_of_act,
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
-                    h->partials, h->sums, h->out_f, h->macro};
+                    h->partials, h->sums, h->out_f, h->macro, h->seg_delta};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     g = GeometryLists();
     h->buf[0] = h->buf[1] = h->stale = h->nw_prev = nullptr;
     h->nw_n = h->nw_wss = h->nw_acc = h->nw_accm = h->partials = h->sums = h->out_f = h->macro = nullptr;
+    h->seg_delta = nullptr;
+    h->nseg = 0;
     drop_graph(h);
     h->has_geo = h->has_state = false;
     h->geo_bytes = 0;
@@ -157,9 +161,7 @@ StepParams make_params(lbm_handle* h, int kind) {
         p.direct = h->since_start == 0 ? 1 : 0;
     }
     p.stride = h->stride;
-    p.nx = h->nx;
-    p.ny = h->ny;
-    p.nxy = (int64_t)h->nx * h->ny;
+    p.seg_delta = h->seg_delta;
     p.nact = h->g.nact;
     p.act_word = h->g.act_word;
     p.sp_of_act = h->g.sp_of_act;
@@ -366,6 +368,62 @@ void reference_bbox(const double* t, int64_t ntri, double spacing, double* bb, i
     dims[2] = (int)std::ceil((mxz - mnz) / spacing);
 }
 
+// Pull segments.  With populations stored by active index a, the source of
+// population q at node a is the active index of point x_a - c_q.  Along an
+// x-run that index is a + delta_q with delta_q constant; a segment is a
+// maximal stretch of consecutive active nodes whose valid (non-missing)
+// offsets agree for every q.  Output: per active node its segment, per
+// segment Q offsets (0 where no node of the segment has that source).
+template <int Q>
+void build_segments_q(const uint8_t* mask, int nx, int ny, int nz, int64_t& nact, std::vector<int32_t>& seg_of,
+                      std::vector<int32_t>& delta) {
+    const int64_t nxy = (int64_t)nx * ny, npts = nxy * nz;
+    std::vector<int32_t> aidx((size_t)npts);
+    int64_t a = 0;
+    for (int64_t n = 0; n < npts; ++n) aidx[n] = mask[n] ? (int32_t)a++ : -1;
+    nact = a;
+    seg_of.assign((size_t)nact, 0);
+    delta.clear();
+    int32_t cur[Q];
+    bool has[Q];
+    int64_t seg = -1;
+    auto flush = [&]() {
+        for (int q = 0; q < Q; ++q) delta.push_back(has[q] ? cur[q] : 0);
+    };
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const int64_t n = (int64_t)k * nxy + (int64_t)j * nx + i;
+                if (!mask[n]) continue;
+                const int32_t an = aidx[n];
+                int32_t d[Q];
+                bool v[Q];
+                bool fresh = seg < 0;
+                for (int q = 0; q < Q; ++q) {
+                    const int x = i - Lat<Q>::cx(q), y = j - Lat<Q>::cy(q), z = k - Lat<Q>::cz(q);
+                    v[q] = x >= 0 && x < nx && y >= 0 && y < ny && z >= 0 && z < nz &&
+                           mask[(int64_t)z * nxy + (int64_t)y * nx + x];
+                    d[q] = v[q] ? aidx[(int64_t)z * nxy + (int64_t)y * nx + x] - an : 0;
+                    if (!fresh && v[q] && has[q] && d[q] != cur[q]) fresh = true;
+                }
+                if (fresh) {
+                    if (seg >= 0) flush();
+                    ++seg;
+                    for (int q = 0; q < Q; ++q) has[q] = false;
+                }
+                for (int q = 0; q < Q; ++q)
+                    if (v[q] && !has[q]) { cur[q] = d[q]; has[q] = true; }
+                seg_of[an] = (int32_t)seg;
+            }
+    if (seg >= 0) flush();
+}
+
+void build_segments(int Q, const uint8_t* mask, int nx, int ny, int nz, int64_t& nact, std::vector<int32_t>& seg_of,
+                    std::vector<int32_t>& delta) {
+    if (Q == 19) build_segments_q<19>(mask, nx, ny, nz, nact, seg_of, delta);
+    else build_segments_q<27>(mask, nx, ny, nz, nact, seg_of, delta);
+}
+
 const uint32_t kCkptMagic = 0x4c424d43;  // "CMBL"
 const uint32_t kCkptVersion = 1;
 
@@ -501,14 +559,28 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     free_geometry(h);
     h->nx = dims[0]; h->ny = dims[1]; h->nz = dims[2];
     h->npts = npts;
-    h->stride = ceil_div(npts, 128) * 128;
+    int64_t nact = 0;
+    std::vector<int32_t> seg_of, delta;
+    build_segments(h->d.Q, mask, h->nx, h->ny, h->nz, nact, seg_of, delta);
+    REQUIRE(h, nact < (int64_t)1 << 31, LBM_ERR_ARG, "too many active nodes");
+    h->nseg = (int64_t)delta.size() / h->d.Q;
+    h->stride = ceil_div(nact > 0 ? nact : 1, 128) * 128;
+    CK(h, dalloc(h, &h->seg_delta, sizeof(int32_t) * (delta.size() + 1)));
+    if (!delta.empty())
+        CK(h, cudaMemcpyAsync(h->seg_delta, delta.data(), sizeof(int32_t) * delta.size(), cudaMemcpyHostToDevice, h->st));
     uint8_t* d_mask = nullptr;
+    int32_t* d_seg = nullptr;
     CK(h, cudaMalloc(&d_mask, npts));
-    cudaError_t e = cudaMemcpyAsync(d_mask, mask, npts, cudaMemcpyHostToDevice, h->st);
+    cudaError_t e = cudaMalloc(&d_seg, sizeof(int32_t) * (nact + 1));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_mask, mask, npts, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && nact)
+        e = cudaMemcpyAsync(d_seg, seg_of.data(), sizeof(int32_t) * nact, cudaMemcpyHostToDevice, h->st);
     std::string err;
     if (e == cudaSuccess)
-        e = build_geometry(h->d.Q, d_mask, h->nx, h->ny, h->nz, bc, nbc, h->d.origin, h->d.spacing, h->g, h->st, err);
+        e = build_geometry(h->d.Q, d_mask, h->nx, h->ny, h->nz, bc, nbc, h->d.origin, h->d.spacing, d_seg, h->g,
+                           h->st, err);
     cudaFree(d_mask);
+    if (d_seg) cudaFree(d_seg);
     if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, "set_geometry: " + (err.empty() ? cudaGetErrorString(e) : err));
     REQUIRE(h, h->g.nact < (int64_t)1 << 31, LBM_ERR_ARG, "too many active nodes");
     h->nbc = nbc;
@@ -542,7 +614,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     h->nblocks = ceil_div(h->g.nact, kStepThreads);
     CK(h, dalloc(h, &h->partials, sizeof(double) * kPartialStride * (h->nblocks + 1)));
     CK(h, dalloc(h, &h->sums, sizeof(double) * kPartialStride));
-    h->geo_bytes += h->npts * 5 + h->g.nsp * 25 + h->g.nact * 16;  // lists from setup
+    h->geo_bytes += h->npts * 5 + h->g.nsp * 25 + h->g.nact * 28;  // lists from setup
     h->has_geo = true;
     // counts
     std::vector<uint8_t> spc(h->g.nsp);
@@ -553,7 +625,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     c.active = h->g.nact;
     c.next_to_wall = h->g.nnw;
     c.special = h->g.nsp;
-    c.segments = ceil_div(h->g.nact, 32);
+    c.segments = h->nseg;
     int64_t bnd = 0;
     for (uint8_t v : spc) {
         if (v == CLS_WALL) c.wall++;
@@ -604,7 +676,7 @@ lbm_status lbm_init_equilibrium(lbm_handle* h) {
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
     CK(h, cudaSetDevice(h->d.device));
-    CK(h, init_state(h->d.precision, h->d.Q, 0, h->buf[0], h->stride, h->npts, nullptr, nullptr, 0, h->st));
+    CK(h, init_state(h->d.precision, h->d.Q, 0, h->buf[0], h->stride, nullptr, h->g.nact, h->st));
     return start_state(h, true);
 }
 
@@ -616,7 +688,7 @@ lbm_status lbm_set_distributions(lbm_handle* h, const double* f) {
     const size_t bytes = sizeof(double) * h->g.nact * h->d.Q;
     if (!h->out_f) CK(h, dalloc(h, &h->out_f, bytes));
     CK(h, cudaMemcpyAsync(h->out_f, f, bytes, cudaMemcpyHostToDevice, h->st));
-    CK(h, init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->npts, h->out_f, h->g.act_pt, h->g.nact, h->st));
+    CK(h, init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->out_f, h->g.nact, h->st));
     return start_state(h, false);
 }
 
@@ -636,7 +708,7 @@ lbm_status lbm_init_from_macro(lbm_handle* h, const float* rho, const float* u, 
         e = warm_start_f(h->d.Q, d_rho, d_u, h->g.act_idx, h->g.act_pt, na, h->nx, h->ny, h->nz, h->d.tau,
                          regularized, h->out_f, h->st);
     if (e == cudaSuccess)
-        e = init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->npts, h->out_f, h->g.act_pt, na, h->st);
+        e = init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->out_f, na, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     cudaFree(d_rho);
     if (d_u) cudaFree(d_u);

@@ -27,9 +27,8 @@ struct BCDev {
 struct StepParams {
     const void* fin;
     void* fout;
-    int64_t stride;        // elements per population plane
-    int nx, ny;
-    int64_t nxy;
+    int64_t stride;            // elements per population plane (active nodes, padded)
+    const int32_t* seg_delta;  // per pull segment, Q source offsets in active-index space
     // one thread per active node; packed word layout in step_kernels.cuh
     int64_t nact;
     const uint64_t* act_word;
@@ -77,14 +76,13 @@ cudaError_t launch_step_f32(int Q, int mode, int kind, int variant, const StepPa
 cudaError_t launch_step_f16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 cudaError_t launch_step_bf16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 
-// State initialisation: what = 0 fills f = w on every point, what = 1
-// scatters fa[a*Q + q] (FP64, per active node) into the planes.
-cudaError_t init_state(int precision, int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
-                       const int64_t* act_pt, int64_t nact, cudaStream_t s);
-cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
-                           const int64_t* act_pt, int64_t nact, cudaStream_t s);
-cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t stride, int64_t npts,
-                            const double* fa, const int64_t* act_pt, int64_t nact, cudaStream_t s);
+// State initialisation: what = 0 fills f = w on every active node, what = 1
+// stores fa[a*Q + q] (FP64, per active node) into the planes.
+cudaError_t init_state(int precision, int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact,
+                       cudaStream_t s);
+cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact, cudaStream_t s);
+cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact,
+                            cudaStream_t s);
 
 // Read-out helpers (step_f64.cu): ordered FP64 sum of per-block partials,
 // and rho/u from read-out distributions.

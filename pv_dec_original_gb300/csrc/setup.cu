@@ -158,12 +158,13 @@ __global__ void k_active_flags(const uint8_t* __restrict__ cls, int64_t npts, in
 }
 
 // Per active node: index maps and the step kernel's packed word
-// (n | special << 31 | missing mask << 32 | class << 59 | next-to-wall << 63).
+// (segment | special << 31 | missing mask << 32 | class << 59 | next-to-wall << 63).
 template <int Q>
 __global__ void k_active_index(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos,
                                const int64_t* __restrict__ spflag, const int64_t* __restrict__ sppos,
                                const uint8_t* __restrict__ cls, int nx, int ny, int nz,
-                               int32_t* __restrict__ act_idx, int64_t* __restrict__ act_pt,
+                               const int32_t* __restrict__ seg_of_act, int32_t* __restrict__ act_idx,
+                               int64_t* __restrict__ act_pt,
                                uint64_t* __restrict__ act_word, int32_t* __restrict__ sp_of_act) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t npts = (int64_t)nx * ny * nz;
@@ -186,7 +187,8 @@ __global__ void k_active_index(const int64_t* __restrict__ flag, const int64_t* 
     }
     const uint8_t c = cls[n];
     const bool sp = spflag[n] != 0;
-    act_word[a] = (uint64_t)n | ((uint64_t)sp << 31) | (miss << 32) | ((uint64_t)(c & CLS_MASK & 0xf) << 59) |
+    act_word[a] = (uint64_t)(uint32_t)seg_of_act[a] | ((uint64_t)sp << 31) | (miss << 32) |
+                  ((uint64_t)(c & CLS_MASK & 0xf) << 59) |
                   ((uint64_t)((c & CLS_NW_BIT) ? 1 : 0) << 63);
     sp_of_act[a] = sp ? (int32_t)sppos[n] : -1;
 }
@@ -265,8 +267,8 @@ inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)ceil_div(n > 0
     } while (0)
 
 cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz, const lbm_bc_spec* bc, int nbc,
-                           const double origin[3], double spacing, GeometryLists& out, cudaStream_t st,
-                           std::string& err) {
+                           const double origin[3], double spacing, const int32_t* d_seg_of_act, GeometryLists& out,
+                           cudaStream_t st, std::string& err) {
     const int64_t npts = (int64_t)nx * ny * nz;
     out.npts = npts;
     // padded to whole 32-point segments: the bulk kernel reads the class
@@ -360,11 +362,11 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     SETUP_CHECK(cudaMallocAsync(&out.act_word, sizeof(uint64_t) * (out.nact + 1), st));
     SETUP_CHECK(cudaMallocAsync(&out.sp_of_act, sizeof(int32_t) * (out.nact + 1), st));
     if (Q == 19)
-        k_active_index<19><<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, out.cls, nx, ny, nz, out.act_idx,
-                                                         out.act_pt, out.act_word, out.sp_of_act);
+        k_active_index<19><<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, out.cls, nx, ny, nz, d_seg_of_act,
+                                                         out.act_idx, out.act_pt, out.act_word, out.sp_of_act);
     else
-        k_active_index<27><<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, out.cls, nx, ny, nz, out.act_idx,
-                                                         out.act_pt, out.act_word, out.sp_of_act);
+        k_active_index<27><<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, out.cls, nx, ny, nz, d_seg_of_act,
+                                                         out.act_idx, out.act_pt, out.act_word, out.sp_of_act);
     SETUP_CHECK(cudaGetLastError());
     cudaFreeAsync(aflag, st);
     cudaFreeAsync(apos, st);

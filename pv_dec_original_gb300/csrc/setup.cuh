@@ -33,8 +33,9 @@ struct GeometryLists {
     int plane[LBM_MAX_BC] = {0};
 };
 
+// d_seg_of_act: per active node, its pull segment (see capi.cu build_segments).
 cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz, const lbm_bc_spec* bc, int nbc,
-                           const double origin[3], double spacing, GeometryLists& out, cudaStream_t st,
-                           std::string& err);
+                           const double origin[3], double spacing, const int32_t* d_seg_of_act, GeometryLists& out,
+                           cudaStream_t st, std::string& err);
 
 }  // namespace lbm

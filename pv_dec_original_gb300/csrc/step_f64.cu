@@ -11,15 +11,15 @@ cudaError_t launch_step_f64(int Q, int mode, int kind, int variant, const StepPa
     return launch_typed<double>(Q, mode, kind, variant, p, st);
 }
 
-cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
-                           const int64_t* act_pt, int64_t nact, cudaStream_t st) {
-    return init_typed<double>(Q, what, f, stride, npts, fa, act_pt, nact, st);
+cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact,
+                           cudaStream_t st) {
+    return init_typed<double>(Q, what, f, stride, fa, nact, st);
 }
 
-cudaError_t init_state(int precision, int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
-                       const int64_t* act_pt, int64_t nact, cudaStream_t st) {
-    if (precision == P_F64) return init_state_f64(Q, what, f, stride, npts, fa, act_pt, nact, st);
-    return init_state_fast(precision, Q, what, f, stride, npts, fa, act_pt, nact, st);
+cudaError_t init_state(int precision, int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact,
+                       cudaStream_t st) {
+    if (precision == P_F64) return init_state_f64(Q, what, f, stride, fa, nact, st);
+    return init_state_fast(precision, Q, what, f, stride, fa, nact, st);
 }
 
 namespace {

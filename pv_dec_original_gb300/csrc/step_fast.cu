@@ -3,12 +3,12 @@
 
 namespace lbm {
 
-cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t stride, int64_t npts,
-                            const double* fa, const int64_t* act_pt, int64_t nact, cudaStream_t st) {
+cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t stride, const double* fa,
+                            int64_t nact, cudaStream_t st) {
     switch (precision) {
-        case P_F32: return init_typed<float>(Q, what, f, stride, npts, fa, act_pt, nact, st);
-        case P_F16: return init_typed<__half>(Q, what, f, stride, npts, fa, act_pt, nact, st);
-        case P_BF16: return init_typed<__nv_bfloat16>(Q, what, f, stride, npts, fa, act_pt, nact, st);
+        case P_F32: return init_typed<float>(Q, what, f, stride, fa, nact, st);
+        case P_F16: return init_typed<__half>(Q, what, f, stride, fa, nact, st);
+        case P_BF16: return init_typed<__nv_bfloat16>(Q, what, f, stride, fa, nact, st);
         default: return cudaErrorInvalidValue;
     }
 }

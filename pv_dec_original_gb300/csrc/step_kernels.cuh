@@ -6,7 +6,12 @@
 //
 // One launch advances the lattice by one reference step.  Populations are
 // stored post-collision, structure of arrays, one plane per population over
-// the dense box (plane q holds entry n = (k*ny + j)*nx + i).  Launch k:
+// the active nodes only (plane q holds entry a, the a-th non-solid point in
+// increasing n = (k*ny + j)*nx + i).  The source of the pull for population q
+// is node a + delta[seg(a)][q], where a segment is a stretch of consecutive
+// active nodes whose 18 neighbour offsets in active-index space agree (in
+// practice an x-run of a row), so loads of a warp are contiguous and stores
+// are exactly contiguous.  Launch k:
 //   1. pulls f*_q(x - c_q) from the input planes        (Streaming, Simulation.cpp:264-290)
 //   2. applies Zou-He / the wall rule on boundary nodes (Simulation.cpp:614-863)
 //   3. accumulates wall shear stress on next-to-wall nodes (Simulation.cpp:880-898)
@@ -37,11 +42,6 @@ namespace lbm {
 constexpr int MODE_PARITY = LBM_PARITY;
 constexpr int MODE_PHYSICS = LBM_PHYSICS;
 constexpr int KIND_STEP = 0, KIND_PROLOGUE = 1, KIND_READOUT = 2;
-
-template <int Q>
-__device__ __forceinline__ int64_t nb_off(int q, int64_t nx, int64_t nxy) {
-    return (int64_t)Lat<Q>::cx(q) + (int64_t)Lat<Q>::cy(q) * nx + (int64_t)Lat<Q>::cz(q) * nxy;
-}
 
 // Momentum sums with the reference's explicit index lists (Simulation.cpp:122-228);
 // the same lists apply to offsets because sum_q w_q c_q = 0.
@@ -332,12 +332,12 @@ __device__ __forceinline__ bool is_exact_zero(R v, int q) {
 // The kernel.
 
 // Packed per-node word (built by setup.cu):
-//   bits  0-30  lattice point n
+//   bits  0-30  segment id: the pull source of population q is node a + delta[seg][q]
 //   bit   31    boundary-list node (needs the long path)
 //   bits 32-58  missing-link mask: bit q set when x + c_q is solid / outside
 //   bits 59-62  class (1 fluid, 2 wall, 3+b boundary condition b)
 //   bit   63    next-to-wall node (accumulates wall shear stress)
-__device__ __forceinline__ int64_t word_point(uint64_t w) { return (int64_t)(w & 0x7fffffffull); }
+__device__ __forceinline__ int64_t word_segment(uint64_t w) { return (int64_t)(w & 0x7fffffffull); }
 __device__ __forceinline__ bool word_special(uint64_t w) { return (w >> 31) & 1ull; }
 __device__ __forceinline__ uint32_t word_miss(uint64_t w) { return (uint32_t)((w >> 32) & 0x7ffffffull); }
 __device__ __forceinline__ int word_class(uint64_t w) { return (int)((w >> 59) & 0xfull); }
@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
 
     if (a < P.nact) {
         const uint64_t word = __ldg(P.act_word + a);
-        const int64_t n = word_point(word);
+        const int32_t* __restrict__ delta = P.seg_delta + word_segment(word) * Q;
         const uint32_t miss = word_miss(word);  // zero on interior nodes
 
         // ---- stream: one load per population, issued by every lane together.
@@ -372,13 +372,12 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
         for (int q = 0; q < Q; ++q) {
             const bool src_missing = !direct && ((miss >> Lat<Q>::opp(q)) & 1u);
             const S* p;
-            if (direct) {
-                p = fin + q * P.stride + n;
+            if (direct || q == Lat<Q>::REST) {
+                p = fin + q * P.stride + a;
             } else if (MODE == MODE_PHYSICS) {
-                p = src_missing ? fin + Lat<Q>::opp(q) * P.stride + n
-                                : fin + q * P.stride + n - nb_off<Q>(q, P.nx, P.nxy);
+                p = src_missing ? fin + Lat<Q>::opp(q) * P.stride + a : fin + q * P.stride + a + __ldg(delta + q);
             } else {
-                p = fin + q * P.stride + (src_missing ? n : n - nb_off<Q>(q, P.nx, P.nxy));
+                p = fin + q * P.stride + (src_missing ? a : a + __ldg(delta + q));
             }
             g[q] = Store<S>::template load<Q>(p, q);  // w_opp(q) == w_q: same decode
         }
@@ -494,7 +493,7 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
             collide<Q, R, OFF>(g, inv_tau, r, ux, uy, uz);
             if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
 #pragma unroll
-            for (int q = 0; q < Q; ++q) fout[q * P.stride + n] = Store<S>::template pack<Q>(g[q], q);
+            for (int q = 0; q < Q; ++q) fout[q * P.stride + a] = Store<S>::template pack<Q>(g[q], q);
         }
     }
     if constexpr (KIND == KIND_STEP) {
@@ -564,37 +563,33 @@ __device__ __forceinline__ S encode_full(double f, int q) {
     else return Store<S>::template pack<Q>((R)f, q);
 }
 
-// Every plane entry := f = w (Node.cpp:30-37).
+// Every plane entry of every active node := f = w (Node.cpp:30-37).
 template <int Q, typename S>
-__global__ void k_fill_weights(S* __restrict__ f, int64_t stride, int64_t npts) {
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= npts) return;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) f[q * stride + n] = encode_full<Q, S>(Lat<Q>::w(q), q);
-}
-
-// fa[a*Q + q] (FP64 f, per active node) scattered into the planes.
-template <int Q, typename S>
-__global__ void k_scatter_f(const double* __restrict__ fa, const int64_t* __restrict__ act_pt, int64_t nact,
-                            S* __restrict__ f, int64_t stride) {
+__global__ void k_fill_weights(S* __restrict__ f, int64_t stride, int64_t nact) {
     const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nact) return;
-    const int64_t n = act_pt[a];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) f[q * stride + n] = encode_full<Q, S>(fa[a * Q + q], q);
+    for (int q = 0; q < Q; ++q) f[q * stride + a] = encode_full<Q, S>(Lat<Q>::w(q), q);
+}
+
+// fa[a*Q + q] (FP64 f, per active node) into the planes.
+template <int Q, typename S>
+__global__ void k_scatter_f(const double* __restrict__ fa, int64_t nact, S* __restrict__ f, int64_t stride) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nact) return;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q * stride + a] = encode_full<Q, S>(fa[a * Q + q], q);
 }
 
 template <typename S>
-cudaError_t init_typed(int Q, int what, void* f, int64_t stride, int64_t npts, const double* fa,
-                       const int64_t* act_pt, int64_t nact, cudaStream_t st) {
+cudaError_t init_typed(int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact, cudaStream_t st) {
+    const unsigned g = (unsigned)ceil_div(nact > 0 ? nact : 1, 256);
     if (what == 0) {
-        const unsigned g = (unsigned)ceil_div(npts > 0 ? npts : 1, 256);
-        if (Q == 19) k_fill_weights<19, S><<<g, 256, 0, st>>>(static_cast<S*>(f), stride, npts);
-        else k_fill_weights<27, S><<<g, 256, 0, st>>>(static_cast<S*>(f), stride, npts);
+        if (Q == 19) k_fill_weights<19, S><<<g, 256, 0, st>>>(static_cast<S*>(f), stride, nact);
+        else k_fill_weights<27, S><<<g, 256, 0, st>>>(static_cast<S*>(f), stride, nact);
     } else {
-        const unsigned g = (unsigned)ceil_div(nact > 0 ? nact : 1, 256);
-        if (Q == 19) k_scatter_f<19, S><<<g, 256, 0, st>>>(fa, act_pt, nact, static_cast<S*>(f), stride);
-        else k_scatter_f<27, S><<<g, 256, 0, st>>>(fa, act_pt, nact, static_cast<S*>(f), stride);
+        if (Q == 19) k_scatter_f<19, S><<<g, 256, 0, st>>>(fa, nact, static_cast<S*>(f), stride);
+        else k_scatter_f<27, S><<<g, 256, 0, st>>>(fa, nact, static_cast<S*>(f), stride);
     }
     return cudaGetLastError();
 }
