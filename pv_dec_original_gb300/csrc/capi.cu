@@ -42,6 +42,8 @@ struct lbm_handle {
     void* stale = nullptr;
     void* nw_prev = nullptr;
     double *nw_n = nullptr, *nw_wss = nullptr, *nw_acc = nullptr, *nw_accm = nullptr;
+    float *nw_nf = nullptr, *nw_wssf = nullptr;  // FP32-arithmetic formats
+    float2* nw_accf = nullptr;
     double* amp = nullptr;
     int64_t namp = 0;
     std::vector<double> amp_host;
@@ -134,7 +136,7 @@ void free_geometry(lbm_handle* h) {
     void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_prof, g.nw_pt, g.act_word, g.sp_of_act,
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
-                    h->partials, h->sums, h->out_f, h->macro, h->seg_delta};
+                    h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     g = GeometryLists();
@@ -142,6 +144,8 @@ void free_geometry(lbm_handle* h) {
     h->nw_n = h->nw_wss = h->nw_acc = h->nw_accm = h->partials = h->sums = h->out_f = h->macro = nullptr;
     h->seg_delta = nullptr;
     h->nseg = 0;
+    h->nw_nf = h->nw_wssf = nullptr;
+    h->nw_accf = nullptr;
     drop_graph(h);
     h->has_geo = h->has_state = false;
     h->geo_bytes = 0;
@@ -176,9 +180,17 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.nw_wss = h->nw_wss;
     p.nw_acc = h->nw_acc;
     p.nw_accm = h->nw_accm;
+    p.nw_nf = h->nw_nf;
+    p.nw_wssf = h->nw_wssf;
+    p.nw_accf = h->nw_accf;
     p.nw_prev = h->nw_prev;
     p.tau = h->d.tau;
     p.wss_C = h->d.wss_scale;
+    p.inv_tau = 1.0 / h->d.tau;
+    p.inv_tau_f = (float)p.inv_tau;
+    p.wss_C_f = (float)h->d.wss_scale;
+    p.wss_phys = -(1.0 - 0.5 / h->d.tau) * h->d.wss_scale;
+    p.wss_phys_f = (float)p.wss_phys;
     p.amp = h->amp;
     p.namp = h->namp;
     p.step_base = h->slots + parity;
@@ -208,6 +220,8 @@ int start_state(lbm_handle* h, bool reset) {
         CK(h, cudaMemsetAsync(h->nw_acc, 0, sizeof(double) * 3 * (h->g.nnw + 1), h->st));
         CK(h, cudaMemsetAsync(h->nw_accm, 0, sizeof(double) * (h->g.nnw + 1), h->st));
         CK(h, cudaMemsetAsync(h->nw_wss, 0, sizeof(double) * (h->g.nnw + 1), h->st));
+        CK(h, cudaMemsetAsync(h->nw_accf, 0, sizeof(float2) * 4 * (h->g.nnw + 1), h->st));
+        CK(h, cudaMemsetAsync(h->nw_wssf, 0, sizeof(float) * (h->g.nnw + 1), h->st));
         h->steps = 0;
     }
     int64_t sl[2] = {h->steps, h->steps};
@@ -611,6 +625,10 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     CK(h, dalloc(h, &h->nw_wss, sizeof(double) * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_acc, sizeof(double) * 3 * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_accm, sizeof(double) * (h->g.nnw + 1)));
+    CK(h, dalloc(h, &h->nw_nf, sizeof(float) * 3 * (h->g.nnw + 1)));
+    CK(h, cudaMemsetAsync(h->nw_nf, 0, sizeof(float) * 3 * (h->g.nnw + 1), h->st));
+    CK(h, dalloc(h, &h->nw_wssf, sizeof(float) * (h->g.nnw + 1)));
+    CK(h, dalloc(h, &h->nw_accf, sizeof(float2) * 4 * (h->g.nnw + 1)));
     h->nblocks = ceil_div(h->g.nact, kStepThreads);
     CK(h, dalloc(h, &h->partials, sizeof(double) * kPartialStride * (h->nblocks + 1)));
     CK(h, dalloc(h, &h->sums, sizeof(double) * kPartialStride));
@@ -648,6 +666,15 @@ lbm_status lbm_set_normals_from_surface(lbm_handle* h, const double* tri12, int6
     if (ntri > 0) e = cudaMemcpyAsync(d_tri, tri12, sizeof(double) * 12 * ntri, cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess)
         e = surface_normals(d_tri, ntri, h->g.nw_pt, h->g.nnw, h->nx, h->ny, h->d.origin, h->d.spacing, h->nw_n, h->st);
+    if (e == cudaSuccess && h->g.nnw > 0) {
+        // FP32 copy for the FP32-arithmetic formats
+        std::vector<double> nd(3 * h->g.nnw);
+        std::vector<float> nf(3 * h->g.nnw);
+        e = cudaMemcpyAsync(nd.data(), h->nw_n, sizeof(double) * nd.size(), cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        for (size_t k = 0; k < nd.size(); ++k) nf[k] = (float)nd[k];
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h->nw_nf, nf.data(), sizeof(float) * nf.size(), cudaMemcpyHostToDevice, h->st);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     cudaFree(d_tri);
     if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("normals: ") + cudaGetErrorString(e));
@@ -818,17 +845,74 @@ lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3) {
     return LBM_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Next-to-wall accumulators as doubles: |tau| (n), tau (3n, [3][n]), |tau| sum (n).
+int read_accumulators(lbm_handle* h, std::vector<double>& w, std::vector<double>& a, std::vector<double>& am) {
+    const int64_t n = h->g.nnw;
+    w.assign(n, 0.0); a.assign(3 * n, 0.0); am.assign(n, 0.0);
+    if (!n) return LBM_OK;
+    if (h->d.precision == LBM_F64) {
+        CK(h, cudaMemcpyAsync(w.data(), h->nw_wss, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(a.data(), h->nw_acc, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(am.data(), h->nw_accm, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaStreamSynchronize(h->st));
+        return LBM_OK;
+    }
+    std::vector<float> wf(n);
+    std::vector<float2> af(4 * n);
+    CK(h, cudaMemcpyAsync(wf.data(), h->nw_wssf, sizeof(float) * n, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaMemcpyAsync(af.data(), h->nw_accf, sizeof(float2) * 4 * n, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    for (int64_t p = 0; p < n; ++p) {
+        w[p] = wf[p];
+        for (int c = 0; c < 3; ++c) a[c * n + p] = (double)af[c * n + p].x + (double)af[c * n + p].y;
+        am[p] = (double)af[3 * n + p].x + (double)af[3 * n + p].y;
+    }
+    return LBM_OK;
+}
+
+int write_accumulators(lbm_handle* h, const std::vector<double>& w, const std::vector<double>& a,
+                       const std::vector<double>& am) {
+    const int64_t n = h->g.nnw;
+    if (!n) return LBM_OK;
+    if (h->d.precision == LBM_F64) {
+        CK(h, cudaMemcpyAsync(h->nw_wss, w.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
+        CK(h, cudaMemcpyAsync(h->nw_acc, a.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->st));
+        CK(h, cudaMemcpyAsync(h->nw_accm, am.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
+        CK(h, cudaStreamSynchronize(h->st));
+        return LBM_OK;
+    }
+    std::vector<float> wf(n);
+    std::vector<float2> af(4 * n);
+    auto split = [](double v) { float hi = (float)v; return make_float2(hi, (float)(v - (double)hi)); };
+    for (int64_t p = 0; p < n; ++p) {
+        wf[p] = (float)w[p];
+        for (int c = 0; c < 3; ++c) af[c * n + p] = split(a[c * n + p]);
+        af[3 * n + p] = split(am[p]);
+    }
+    CK(h, cudaMemcpyAsync(h->nw_wssf, wf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaMemcpyAsync(h->nw_accf, af.data(), sizeof(float2) * 4 * n, cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3, double* acc_mag,
                        double* osi, double* tawss) {
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
     const int64_t n = h->g.nnw;
-    std::vector<double> nn(3 * n), w(n), a(3 * n), am(n);
+    std::vector<double> nn(3 * n), w, a, am;
+    int rc = read_accumulators(h, w, a, am);
+    if (rc) return rc;
     if (n) {
         CK(h, cudaMemcpyAsync(nn.data(), h->nw_n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
-        CK(h, cudaMemcpyAsync(w.data(), h->nw_wss, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
-        CK(h, cudaMemcpyAsync(a.data(), h->nw_acc, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
-        CK(h, cudaMemcpyAsync(am.data(), h->nw_accm, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
         if (pt) CK(h, cudaMemcpyAsync(pt, h->g.nw_pt, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, h->st));
     }
     CK(h, cudaStreamSynchronize(h->st));
@@ -867,15 +951,11 @@ lbm_status lbm_save(lbm_handle* h, const char* path) {
     if (!h || !path) return fail(h, LBM_ERR_ARG, "null handle or path");
     REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state to save");
     const int64_t na = h->g.nact, nn = h->g.nnw;
-    std::vector<double> f(na * h->d.Q), acc(3 * nn), accm(nn), wss(nn);
+    std::vector<double> f(na * h->d.Q), acc, accm, wss;
     int rc = lbm_get_distributions(h, f.data());
     if (rc) return rc;
-    if (nn) {
-        CK(h, cudaMemcpyAsync(acc.data(), h->nw_acc, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, h->st));
-        CK(h, cudaMemcpyAsync(accm.data(), h->nw_accm, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->st));
-        CK(h, cudaMemcpyAsync(wss.data(), h->nw_wss, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->st));
-    }
-    CK(h, cudaStreamSynchronize(h->st));
+    rc = read_accumulators(h, wss, acc, accm);
+    if (rc) return rc;
     std::FILE* fp = std::fopen(path, "wb");
     REQUIRE(h, fp, LBM_ERR_IO, std::string("cannot write ") + path);
     const uint32_t head[2] = {kCkptMagic, kCkptVersion};
@@ -923,11 +1003,8 @@ lbm_status lbm_load(lbm_handle* h, const char* path) {
     REQUIRE(h, ok, LBM_ERR_IO, std::string("truncated checkpoint ") + path);
     int rc = lbm_set_inlet_table(h, amp.data(), (int64_t)amp.size());
     if (rc) return rc;
-    if (nn) {
-        CK(h, cudaMemcpyAsync(h->nw_acc, acc.data(), sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, h->st));
-        CK(h, cudaMemcpyAsync(h->nw_accm, accm.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, h->st));
-        CK(h, cudaMemcpyAsync(h->nw_wss, wss.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, h->st));
-    }
+    rc = write_accumulators(h, wss, acc, accm);
+    if (rc) return rc;
     h->steps = sz[2];
     return lbm_set_distributions(h, f.data());
 }
@@ -955,7 +1032,9 @@ lbm_status lbm_autotune(lbm_handle* h, int trial_steps, int* best, float* ms_per
         {h->flags, sizeof(unsigned), nullptr},
         {h->nw_acc, sizeof(double) * 3 * (h->g.nnw + 1), nullptr},
         {h->nw_accm, sizeof(double) * (h->g.nnw + 1), nullptr},
-        {h->nw_wss, sizeof(double) * (h->g.nnw + 1), nullptr}};
+        {h->nw_wss, sizeof(double) * (h->g.nnw + 1), nullptr},
+        {h->nw_accf, sizeof(float2) * 4 * (h->g.nnw + 1), nullptr},
+        {h->nw_wssf, sizeof(float) * (h->g.nnw + 1), nullptr}};
     if (h->stale) items.push_back({h->stale, rs * h->d.Q * (h->g.nsp + 1), nullptr});
     if (h->nw_prev) items.push_back({h->nw_prev, rs * 4 * (h->g.nnw + 1), nullptr});
     auto release = [&]() {

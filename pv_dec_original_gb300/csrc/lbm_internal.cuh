@@ -46,9 +46,22 @@ struct StepParams {
     double* nw_wss;
     double* nw_acc;           // [3][nnw]
     double* nw_accm;
+    // FP32-arithmetic formats keep their next-to-wall data in FP32 (GB300's
+    // FP64 rate is a small fraction of FP32): normals, the current |tau|, and
+    // compensated two-float accumulators (hi, lo) for tau_x, tau_y, tau_z, |tau|
+    const float* nw_nf;       // [3][nnw]
+    float* nw_wssf;
+    float2* nw_accf;          // [4][nnw]
     void* nw_prev;            // parity: rho, ux, uy, uz of the previous collision, [4][nnw]
     double tau;
     double wss_C;
+    // scalars derived on the host: FP64 arithmetic is slow on GB300, so no
+    // thread recomputes them
+    double inv_tau;            // 1/tau (the reference's (1.0 / m_relaxation))
+    float inv_tau_f;
+    float wss_C_f;             // C in FP32 (parity stress)
+    float wss_phys_f;          // -(1 - 1/(2 tau)) C in FP32 (physics stress)
+    double wss_phys;           // the same in FP64
     // inlet amplitude table: step index = *step_base + step_off
     const double* amp;
     int64_t namp;

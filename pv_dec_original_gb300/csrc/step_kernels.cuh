@@ -72,7 +72,7 @@ __device__ __forceinline__ void moments(const R (&f)[Q], R& r, R& ux, R& uy, R& 
     R px, py, pz;
     momentum<Q, R>(f, px, py, pz);
     if constexpr (OFF) {
-        const R inv = R(1) / (R(1) + d);
+        const R inv = __frcp_rn(R(1) + d);
         ux = px * inv; uy = py * inv; uz = pz * inv;
     } else {
         ux = px / d; uy = py / d; uz = pz / d;
@@ -232,7 +232,10 @@ __device__ __forceinline__ void zou_he(R (&m)[Q], int face, bool pressure, R val
 // (FP64, full f); elsewhere the reference kinds use the equivalent face form.
 template <int Q, typename R, bool OFF>
 __device__ __forceinline__ void apply_bc(R (&m)[Q], const BCDev& b, double amp, double prof) {
-    const R vel = (R)(amp * prof * b.value);
+    // FP64 keeps the reference's product (amplitude * profile); FP32 multiplies in FP32
+    R vel;
+    if constexpr (OFF) vel = (R)amp * (R)prof * (R)b.value;
+    else vel = amp * prof * b.value;
     if constexpr (Q == 19 && !OFF) {
         if (b.kind == LBM_BC_REF_INLET) { ref_inlet_q19(m, vel); return; }
         if (b.kind == LBM_BC_REF_OUTLET_YMAX) { ref_outlet_ymax_q19(m); return; }
@@ -295,6 +298,15 @@ __device__ __forceinline__ void wss_fast(const R (&f)[Q], R r, R ux, R uy, R uz,
     tau_i[0] = C * a0; tau_i[1] = C * a1; tau_i[2] = C * a2;
 }
 
+// Compensated accumulation in two floats (Neumaier): acc.x carries the sum,
+// acc.y the rounding errors; the value is (double)acc.x + acc.y.
+__device__ __forceinline__ void comp_add(float2& acc, float v) {
+    const float s = acc.x + v;
+    const float c = fabsf(acc.x) >= fabsf(v) ? (acc.x - s) + v : (v - s) + acc.x;
+    acc.x = s;
+    acc.y += c;
+}
+
 // ---------------------------------------------------------------------------
 // Block reduction of the read-out sums (rho - 1, momentum, per-BC flux).
 
@@ -348,7 +360,9 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
     constexpr bool OFF = Store<S>::offset;
     const S* __restrict__ fin = static_cast<const S*>(P.fin);
     S* __restrict__ fout = static_cast<S*>(P.fout);
-    const R inv_tau = (R)(1.0 / P.tau);
+    R inv_tau;
+    if constexpr (OFF) inv_tau = P.inv_tau_f;
+    else inv_tau = P.inv_tau;
     double part[kPartialStride];
     if constexpr (KIND == KIND_READOUT) {
 #pragma unroll
@@ -427,37 +441,46 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
                 const int nw = __ldg(P.sp_nw + s);
                 R* __restrict__ prev = static_cast<R*>(P.nw_prev);
                 if (KIND == KIND_STEP && nw >= 0) {
-                    double t[3];
-                    const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
-                    if constexpr (MODE == MODE_PARITY) {
-                        // equilibrium of the previous collision (time-lagged, as the reference)
-                        if constexpr (!OFF) {
+                    if constexpr (!OFF) {
+                        // FP64: the reference's arithmetic
+                        double t[3];
+                        const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
+                        if constexpr (MODE == MODE_PARITY) {
+                            // equilibrium of the previous collision (time-lagged, as the reference)
                             double e[Q];
                             feq_all<Q, double, false>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
                                                       prev[3 * P.nnw + nw]);
                             wss_reference<Q>(g, e, nn, P.wss_C, t);
                         } else {
-                            const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
-                            R tr[3];
-                            wss_fast<Q, R, OFF>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
-                                                prev[3 * P.nnw + nw], nr, (R)P.wss_C, tr);
-                            t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
+                            double r, ux, uy, uz;
+                            moments<Q, double, false>(g, r, ux, uy, uz);
+                            wss_fast<Q, double, false>(g, r, ux, uy, uz, nn, P.wss_phys, t);
                         }
+                        const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                        P.nw_wss[nw] = W;
+                        P.nw_acc[nw] += t[0];
+                        P.nw_acc[P.nnw + nw] += t[1];
+                        P.nw_acc[2 * P.nnw + nw] += t[2];
+                        P.nw_accm[nw] += W;
                     } else {
-                        // stress of the same post-boundary f, with the (1 - 1/2tau) factor
-                        R r, ux, uy, uz;
-                        moments<Q, R, OFF>(g, r, ux, uy, uz);
-                        const R nr[3] = {(R)nn[0], (R)nn[1], (R)nn[2]};
-                        R tr[3];
-                        wss_fast<Q, R, OFF>(g, r, ux, uy, uz, nr, (R)(-(1.0 - 0.5 / P.tau) * P.wss_C), tr);
-                        t[0] = tr[0]; t[1] = tr[1]; t[2] = tr[2];
+                        // FP32 arithmetic end to end
+                        const float nr[3] = {P.nw_nf[nw], P.nw_nf[P.nnw + nw], P.nw_nf[2 * P.nnw + nw]};
+                        float t[3];
+                        if constexpr (MODE == MODE_PARITY) {
+                            wss_fast<Q, float, true>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
+                                                     prev[3 * P.nnw + nw], nr, P.wss_C_f, t);
+                        } else {
+                            float r, ux, uy, uz;
+                            moments<Q, float, true>(g, r, ux, uy, uz);
+                            wss_fast<Q, float, true>(g, r, ux, uy, uz, nr, P.wss_phys_f, t);
+                        }
+                        const float W = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                        P.nw_wssf[nw] = W;
+                        comp_add(P.nw_accf[nw], t[0]);
+                        comp_add(P.nw_accf[P.nnw + nw], t[1]);
+                        comp_add(P.nw_accf[2 * P.nnw + nw], t[2]);
+                        comp_add(P.nw_accf[3 * P.nnw + nw], W);
                     }
-                    const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-                    P.nw_wss[nw] = W;
-                    P.nw_acc[nw] += t[0];
-                    P.nw_acc[P.nnw + nw] += t[1];
-                    P.nw_acc[2 * P.nnw + nw] += t[2];
-                    P.nw_accm[nw] += W;
                 }
                 if constexpr (MODE == MODE_PARITY) {
 #pragma unroll
