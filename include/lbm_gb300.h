@@ -238,6 +238,22 @@ lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph);
 lbm_status lbm_autotune(lbm_handle* h, int trial_steps, int* best, float* ms_per_step);
 lbm_status lbm_set_variant(lbm_handle* h, int variant);
 
+/* ---------------------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (code running during CUDA graph capture, real-time loops with
+ * memory fixed up-front, frameworks whose pool allocator owns the device):
+ * FP64 sums over caller-owned device memory with no allocation at all.
+ *   d_f:   device array of nact*Q doubles, distributions per node [a*Q + q]
+ *   d_out: device array of 4 doubles <- mass, momentum x, y, z
+ * Runs on `stream` (a cudaStream_t, NULL = default stream) and returns
+ * without waiting.  The per-block scratch is a fixed 512 KiB device array
+ * inside the library (held by every GPU that loads it until exit), so nact
+ * is limited to 4,194,304; larger inputs get LBM_ERR_ARG.  The first call on
+ * a device looks the array up with that device current: make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race; serialise them.  Errors: lbm_last_global_error(). */
+lbm_status lbm_moment_sums_noalloc(const double* d_f, int64_t nact, int Q, double* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

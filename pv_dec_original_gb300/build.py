@@ -34,6 +34,7 @@ UNITS = [
     ("step_bf16.cu", True),
     ("step_fast.cu", True),
     ("capi.cu", False),
+    ("noalloc.cu", False),
 ]
 HOST_UNITS = ["host/LatticeModel.cpp", "host/GeometryReader.cpp", "host/ComplexGeometry.cpp",
               "host/Subdomain.cpp", "host/Simulation.cpp", "host/Boundary.cpp", "host/ConfigReader.cpp",

@@ -62,6 +62,7 @@ EXPORTS = [
     "lbm_init_from_macro", "lbm_step", "lbm_step_async", "lbm_check_status", "lbm_sync", "lbm_get_counts", "lbm_get_classes", "lbm_get_distributions",
     "lbm_set_distributions", "lbm_get_macro", "lbm_get_wss", "lbm_get_conservation", "lbm_save", "lbm_load",
     "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_autotune", "lbm_set_variant",
+    "lbm_moment_sums_noalloc",
 ]
 NUM_VARIANTS = 5
 
@@ -116,6 +117,7 @@ def load(build_if_missing: bool = True):
     L.lbm_set_graph_steps.argtypes = [P, C.c_int]
     L.lbm_autotune.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     L.lbm_set_variant.argtypes = [P, C.c_int]
+    L.lbm_moment_sums_noalloc.argtypes = [P, C.c_int64, C.c_int, P, P]
     _lib = L
     return L
 

@@ -443,6 +443,8 @@ const uint32_t kCkptVersion = 1;
 
 }  // namespace
 
+void lbm::set_last_global_error(const char* msg) { g_err = msg ? msg : ""; }
+
 // ===========================================================================
 
 extern "C" {

@@ -126,4 +126,7 @@ cudaError_t surface_normals(const double* d_tri, int64_t ntri, const int64_t* d_
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Message returned by lbm_last_global_error() (capi.cu).
+void set_last_global_error(const char* msg);
+
 }  // namespace lbm
