@@ -387,7 +387,9 @@ void reference_bbox(const double* t, int64_t ntri, double spacing, double* bb, i
 // x-run that index is a + delta_q with delta_q constant; a segment is a
 // maximal stretch of consecutive active nodes whose valid (non-missing)
 // offsets agree for every q.  Output: per active node its segment, per
-// segment Q offsets (0 where no node of the segment has that source).
+// segment Q offsets (0 where no node of the segment has that source), each
+// row padded with zeros to kDeltaRow<Q> entries so that the step kernel
+// reads it with 16-byte loads.
 template <int Q>
 void build_segments_q(const uint8_t* mask, int nx, int ny, int nz, int64_t& nact, std::vector<int32_t>& seg_of,
                       std::vector<int32_t>& delta) {
@@ -403,6 +405,7 @@ void build_segments_q(const uint8_t* mask, int nx, int ny, int nz, int64_t& nact
     int64_t seg = -1;
     auto flush = [&]() {
         for (int q = 0; q < Q; ++q) delta.push_back(has[q] ? cur[q] : 0);
+        for (int q = Q; q < kDeltaRow<Q>; ++q) delta.push_back(0);
     };
     for (int k = 0; k < nz; ++k)
         for (int j = 0; j < ny; ++j)
@@ -439,7 +442,7 @@ void build_segments(int Q, const uint8_t* mask, int nx, int ny, int nz, int64_t&
 }
 
 const uint32_t kCkptMagic = 0x4c424d43;  // "CMBL"
-const uint32_t kCkptVersion = 1;
+const uint32_t kCkptVersion = 2;  // 2: boundary list ordered next-to-wall first
 
 }  // namespace
 
@@ -579,7 +582,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     std::vector<int32_t> seg_of, delta;
     build_segments(h->d.Q, mask, h->nx, h->ny, h->nz, nact, seg_of, delta);
     REQUIRE(h, nact < (int64_t)1 << 31, LBM_ERR_ARG, "too many active nodes");
-    h->nseg = (int64_t)delta.size() / h->d.Q;
+    h->nseg = (int64_t)delta.size() / (h->d.Q == 19 ? kDeltaRow<19> : kDeltaRow<27>);
     h->stride = ceil_div(nact > 0 ? nact : 1, 128) * 128;
     CK(h, dalloc(h, &h->seg_delta, sizeof(int32_t) * (delta.size() + 1)));
     if (!delta.empty())

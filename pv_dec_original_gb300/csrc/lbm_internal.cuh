@@ -28,7 +28,7 @@ struct StepParams {
     const void* fin;
     void* fout;
     int64_t stride;            // elements per population plane (active nodes, padded)
-    const int32_t* seg_delta;  // per pull segment, Q source offsets in active-index space
+    const int32_t* seg_delta;  // per pull segment, Q source offsets in active-index space (rows of kDeltaRow<Q>)
     // one thread per active node; packed word layout in step_kernels.cuh
     int64_t nact;
     const uint64_t* act_word;
@@ -125,6 +125,11 @@ cudaError_t surface_normals(const double* d_tri, int64_t ntri, const int64_t* d_
                             const double origin[3], double spacing, double* d_out, cudaStream_t s);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Entries per pull-segment row of the delta table: Q offsets padded to a
+// multiple of 4 (one 16-byte load per 4 offsets).
+template <int Q>
+constexpr int kDeltaRow = (Q + 3) / 4 * 4;
 
 // Message returned by lbm_last_global_error() (capi.cu).
 void set_last_global_error(const char* msg);

@@ -96,13 +96,32 @@ __global__ void k_next_to_wall(uint8_t* __restrict__ cls, int nx, int ny, int nz
     if (nw) cls[n] = CLS_FLUID | CLS_NW_BIT;
 }
 
-__global__ void k_flag_special(const uint8_t* __restrict__ cls, int64_t npts, int64_t* __restrict__ flag,
+// Boundary-list membership, split in two: next-to-wall nodes (nwflag) and
+// the other boundary-list nodes (wall and boundary-condition nodes, oflag).
+__global__ void k_flag_special(const uint8_t* __restrict__ cls, int64_t npts, int64_t* __restrict__ oflag,
                                int64_t* __restrict__ nwflag) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= npts) return;
     const uint8_t c = cls[n];
-    flag[n] = ((c & CLS_MASK) >= CLS_WALL || (c & CLS_NW_BIT)) ? 1 : 0;
-    nwflag[n] = (c & CLS_NW_BIT) ? 1 : 0;
+    const bool nw = (c & CLS_NW_BIT) != 0;
+    oflag[n] = (!nw && (c & CLS_MASK) >= CLS_WALL) ? 1 : 0;
+    nwflag[n] = nw ? 1 : 0;
+}
+
+// Boundary-list position: next-to-wall nodes first, in point order, so that
+// a next-to-wall node's list entry s is also its wall-shear-stress index;
+// then the other boundary-list nodes in point order.
+__global__ void k_special_pos(int64_t* __restrict__ flag, int64_t* __restrict__ pos,
+                              const int64_t* __restrict__ nwflag, const int64_t* __restrict__ nwpos, int64_t nnw,
+                              int64_t npts) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts) return;
+    if (nwflag[n]) {
+        flag[n] = 1;
+        pos[n] = nwpos[n];
+    } else if (flag[n]) {
+        pos[n] = nnw + pos[n];
+    }
 }
 
 __global__ void k_scatter(const int64_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t npts,
@@ -321,8 +340,12 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     SETUP_CHECK(cudaMallocAsync(&nwflag, sizeof(int64_t) * npts, st));
     SETUP_CHECK(cudaMallocAsync(&nwpos, sizeof(int64_t) * npts, st));
     k_flag_special<<<blocks(npts), 256, 0, st>>>(out.cls, npts, flag, nwflag);
-    SETUP_CHECK(exclusive_scan_i64(flag, pos, npts, &out.nsp, st));
+    int64_t nother = 0;
+    SETUP_CHECK(exclusive_scan_i64(flag, pos, npts, &nother, st));
     SETUP_CHECK(exclusive_scan_i64(nwflag, nwpos, npts, &out.nnw, st));
+    out.nsp = out.nnw + nother;
+    k_special_pos<<<blocks(npts), 256, 0, st>>>(flag, pos, nwflag, nwpos, out.nnw, npts);
+    SETUP_CHECK(cudaGetLastError());
     SETUP_CHECK(cudaMallocAsync(&out.sp_pt, sizeof(int64_t) * (out.nsp + 1), st));
     SETUP_CHECK(cudaMallocAsync(&out.nw_pt, sizeof(int64_t) * (out.nnw + 1), st));
     k_scatter<<<blocks(npts), 256, 0, st>>>(flag, pos, npts, out.sp_pt);

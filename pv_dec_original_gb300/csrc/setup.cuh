@@ -17,7 +17,8 @@ struct ProfileSpec {
 struct GeometryLists {
     int64_t npts = 0;
     uint8_t* cls = nullptr;      // per point
-    int64_t nsp = 0;             // boundary + next-to-wall nodes
+    int64_t nsp = 0;             // boundary + next-to-wall nodes; next-to-wall first (entry s < nnw is
+                                 // next-to-wall node s)
     int64_t* sp_pt = nullptr;
     uint32_t* sp_miss = nullptr;
     uint8_t* sp_cls = nullptr;

@@ -35,6 +35,8 @@
 // nodes, which keep no previous value, the event is flagged instead
 // (FLAG_EXACT_ZERO) -- it needs a post-collision population of exactly zero.
 #pragma once
+#include <type_traits>
+
 #include "lbm_internal.cuh"
 
 namespace lbm {
@@ -111,12 +113,99 @@ __device__ __forceinline__ void feq_all(R (&e)[Q], R r, R ux, R uy, R uz) {
     }
 }
 
-// BGK collision in place; returns the moments (r as in `moments`).
-template <int Q, typename R, bool OFF>
-__device__ __forceinline__ void collide(R (&f)[Q], R inv_tau, R& r, R& ux, R& uy, R& uz) {
-    moments<Q, R, OFF>(f, r, ux, uy, uz);
-    const R usqr = ux * ux + uy * uy + uz * uz;
-    relax_all<Q, R, OFF>(f, r, ux, uy, uz, usqr, inv_tau);
+
+// ---------------------------------------------------------------------------
+// FP32 arithmetic on offsets, with the lattice constants folded by hand:
+// IEEE rules forbid the compiler to drop x * 0.0f or 0.0f + x, so products
+// with c_q components are written as signed additions.
+
+template <int c, typename R>
+__device__ __forceinline__ R cadd(R s, R v) {
+    if constexpr (c > 0) return s + v;
+    else if constexpr (c < 0) return s - v;
+    else return s;
+}
+
+// c_q . (x, y, z)
+template <int Q, int q, typename R>
+__device__ __forceinline__ R cdot(R x, R y, R z) {
+    constexpr int cx = Lat<Q>::cx(q), cy = Lat<Q>::cy(q), cz = Lat<Q>::cz(q);
+    if constexpr (cx != 0) {
+        return cadd<cz>(cadd<cy>(cx > 0 ? x : -x, y), z);
+    } else if constexpr (cy != 0) {
+        return cadd<cz>(cy > 0 ? y : -y, z);
+    } else if constexpr (cz != 0) {
+        return cz > 0 ? z : -z;
+    } else {
+        return R(0);
+    }
+}
+
+// BGK relaxation of offsets d = f - w, direction pairs (q, opp q) sharing
+// the even part of the equilibrium.  With A = 1 + r, B = r - 1.5 A u^2 and
+// du = c_q . u:  feq_{q|opp} - w_q = w_q (B + 4.5 A du^2 +|- 3 A du), and
+// d* = (1 - omega) d + omega (feq - w).
+template <int Q, int q = 0>
+__device__ __forceinline__ void relax_pairs(float (&f)[Q], float A, float B, float ux, float uy, float uz, float om,
+                                            float om1) {
+    if constexpr (q < Q) {
+        constexpr int o = Lat<Q>::opp(q);
+        if constexpr (q == Lat<Q>::REST) {
+            f[q] = om1 * f[q] + (om * (float)Lat<Q>::w(q)) * B;
+        } else if constexpr (q < o) {
+            const float du = cdot<Q, q, float>(ux, uy, uz);
+            const float ow = om * (float)Lat<Q>::w(q);
+            const float t = A * du;
+            const float sym = ow * ((4.5f * t) * du + B);
+            const float anti = (3.0f * ow) * t;
+            f[q] = om1 * f[q] + (sym + anti);
+            f[o] = om1 * f[o] + (sym - anti);
+        }
+        relax_pairs<Q, q + 1>(f, A, B, ux, uy, uz, om, om1);
+    }
+}
+
+// Second moments sum_q d_q c_qa c_qb (xx, yy, zz, xy, xz, yz) from the
+// pair sums d_q + d_opp(q): c c^T is even in c.
+template <int Q, int q = 0>
+__device__ __forceinline__ void second_moments(const float (&d)[Q], float (&m)[6]) {
+    if constexpr (q < Q) {
+        constexpr int o = Lat<Q>::opp(q);
+        if constexpr (q < o) {
+            constexpr int cx = Lat<Q>::cx(q), cy = Lat<Q>::cy(q), cz = Lat<Q>::cz(q);
+            const float p = d[q] + d[o];
+            m[0] = cadd<cx * cx>(m[0], p);
+            m[1] = cadd<cy * cy>(m[1], p);
+            m[2] = cadd<cz * cz>(m[2], p);
+            m[3] = cadd<cx * cy>(m[3], p);
+            m[4] = cadd<cx * cz>(m[4], p);
+            m[5] = cadd<cy * cz>(m[5], p);
+        }
+        second_moments<Q, q + 1>(d, m);
+    }
+}
+
+// Wall shear stress from the non-equilibrium stress tensor
+//   Pi = sum_q (f_q - feq_q) c_q c_q^T,
+// using sum_q (feq_q - w_q) c_q c_q^T = r/3 I + (1 + r) u u^T (exact for the
+// second-order equilibrium on D3Q19 and D3Q27): tau = C (Pi n - (n.Pi n) n),
+// the per-direction sum of Simulation.cpp:880-898 regrouped.  (r, u) are the
+// moments the equilibrium is taken at.
+template <int Q>
+__device__ __forceinline__ void wss_stress(const float (&d)[Q], float r, float ux, float uy, float uz,
+                                           const float n[3], float C, float t[3]) {
+    float m[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    second_moments<Q>(d, m);
+    const float A = 1.0f + r, r3 = r * (1.0f / 3.0f);
+    const float Axx = m[0] - (r3 + A * ux * ux), Ayy = m[1] - (r3 + A * uy * uy), Azz = m[2] - (r3 + A * uz * uz);
+    const float Axy = m[3] - A * ux * uy, Axz = m[4] - A * ux * uz, Ayz = m[5] - A * uy * uz;
+    const float px = Axx * n[0] + Axy * n[1] + Axz * n[2];
+    const float py = Axy * n[0] + Ayy * n[1] + Ayz * n[2];
+    const float pz = Axz * n[0] + Ayz * n[1] + Azz * n[2];
+    const float nn = px * n[0] + py * n[1] + pz * n[2];
+    t[0] = C * (px - nn * n[0]);
+    t[1] = C * (py - nn * n[1]);
+    t[2] = C * (pz - nn * n[2]);
 }
 
 // ---------------------------------------------------------------------------
@@ -343,6 +432,10 @@ __device__ __forceinline__ bool is_exact_zero(R v, int q) {
 // ---------------------------------------------------------------------------
 // The kernel.
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Packed per-node word (built by setup.cu):
 //   bits  0-30  segment id: the pull source of population q is node a + delta[seg][q]
 //   bit   31    boundary-list node (needs the long path)
@@ -353,16 +446,18 @@ __device__ __forceinline__ int64_t word_segment(uint64_t w) { return (int64_t)(w
 __device__ __forceinline__ bool word_special(uint64_t w) { return (w >> 31) & 1ull; }
 __device__ __forceinline__ uint32_t word_miss(uint64_t w) { return (uint32_t)((w >> 32) & 0x7ffffffull); }
 __device__ __forceinline__ int word_class(uint64_t w) { return (int)((w >> 59) & 0xfull); }
+__device__ __forceinline__ bool word_nw(uint64_t w) { return (w >> 63) & 1ull; }
 
-template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1>
+// WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
+// lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
+template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1, bool WIDE = true>
 __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
+    using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
     using R = typename Store<S>::real;
     constexpr bool OFF = Store<S>::offset;
+    constexpr int DR = kDeltaRow<Q>;
     const S* __restrict__ fin = static_cast<const S*>(P.fin);
     S* __restrict__ fout = static_cast<S*>(P.fout);
-    R inv_tau;
-    if constexpr (OFF) inv_tau = P.inv_tau_f;
-    else inv_tau = P.inv_tau;
     double part[kPartialStride];
     if constexpr (KIND == KIND_READOUT) {
 #pragma unroll
@@ -373,33 +468,64 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
     constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
 
     if (a < P.nact) {
+        // the node's word and its boundary-list entry (-1 for most nodes),
+        // loaded side by side
         const uint64_t word = __ldg(P.act_word + a);
-        const int32_t* __restrict__ delta = P.seg_delta + word_segment(word) * Q;
+        const int32_t sp_entry = __ldg(P.sp_of_act + a);
         const uint32_t miss = word_miss(word);  // zero on interior nodes
+        const int c = word_class(word);
+        // Boundary-list work: in parity mode every boundary-list node (history
+        // of missing links, the wall rule); in physics mode only
+        // boundary-condition and next-to-wall nodes (bounce-back is folded
+        // into the loads).  The list entry is fetched before the loads.
+        const bool lng = MODE == MODE_PARITY ? word_special(word) : (c >= CLS_BC0 || word_nw(word));
+        const int64_t s = lng ? (int64_t)sp_entry : 0;
+        if (KIND == KIND_STEP && lng && s < P.nnw) {
+            // next-to-wall node: pull its normal and accumulators towards L2
+            // while the populations load
+            if constexpr (OFF) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) prefetch_l2(P.nw_accf + k * P.nnw + s);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) prefetch_l2(P.nw_nf + k * P.nnw + s);
+            }
+        }
 
         // ---- stream: one load per population, issued by every lane together.
         // A link whose source is missing reads, in physics mode, the node's
         // own opposite population (half-way bounce-back); in parity mode any
         // valid address -- the previous value replaces it below.
+        const I ai = (I)a, st = (I)P.stride;
         R g[Q];
+        if (direct) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const bool src_missing = !direct && ((miss >> Lat<Q>::opp(q)) & 1u);
-            const S* p;
-            if (direct || q == Lat<Q>::REST) {
-                p = fin + q * P.stride + a;
-            } else if (MODE == MODE_PHYSICS) {
-                p = src_missing ? fin + Lat<Q>::opp(q) * P.stride + a : fin + q * P.stride + a + __ldg(delta + q);
-            } else {
-                p = fin + q * P.stride + (src_missing ? a : a + __ldg(delta + q));
+            for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin + (q * st + ai), q);
+        } else {
+            int32_t dl[DR];
+            const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
+#pragma unroll
+            for (int k = 0; k < DR / 4; ++k) {
+                const int4 v = __ldg(drow + k);
+                dl[4 * k] = v.x; dl[4 * k + 1] = v.y; dl[4 * k + 2] = v.z; dl[4 * k + 3] = v.w;
             }
-            g[q] = Store<S>::template load<Q>(p, q);  // w_opp(q) == w_q: same decode
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const bool src_missing = (miss >> Lat<Q>::opp(q)) & 1u;
+                I idx;
+                if (q == Lat<Q>::REST) {
+                    idx = q * st + ai;
+                } else if (MODE == MODE_PHYSICS) {
+                    idx = src_missing ? Lat<Q>::opp(q) * st + ai : q * st + ai + dl[q];
+                } else {
+                    idx = q * st + (src_missing ? ai : ai + dl[q]);
+                }
+                g[q] = Store<S>::template load<Q>(fin + idx, q);  // w_opp(q) == w_q: same decode
+            }
         }
 
-        if (word_special(word)) {
-            // ---- boundary-list node: history, boundary rules, wall shear stress
-            const int64_t s = __ldg(P.sp_of_act + a);
-            const int c = word_class(word);
+        int nw = -1;  // next-to-wall index: boundary-list entries below nnw
+        if (lng) {
+            // ---- boundary-list node: history, boundary rules
             R* __restrict__ stale = static_cast<R*>(P.stale);
             if constexpr (MODE == MODE_PARITY) {
                 if (parity_readout) {
@@ -437,62 +563,8 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
                     const double j[3] = {rho * ux, rho * uy, rho * uz};
                     part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
                 }
-            } else {
-                const int nw = __ldg(P.sp_nw + s);
-                R* __restrict__ prev = static_cast<R*>(P.nw_prev);
-                if (KIND == KIND_STEP && nw >= 0) {
-                    if constexpr (!OFF) {
-                        // FP64: the reference's arithmetic
-                        double t[3];
-                        const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
-                        if constexpr (MODE == MODE_PARITY) {
-                            // equilibrium of the previous collision (time-lagged, as the reference)
-                            double e[Q];
-                            feq_all<Q, double, false>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
-                                                      prev[3 * P.nnw + nw]);
-                            wss_reference<Q>(g, e, nn, P.wss_C, t);
-                        } else {
-                            double r, ux, uy, uz;
-                            moments<Q, double, false>(g, r, ux, uy, uz);
-                            wss_fast<Q, double, false>(g, r, ux, uy, uz, nn, P.wss_phys, t);
-                        }
-                        const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-                        P.nw_wss[nw] = W;
-                        P.nw_acc[nw] += t[0];
-                        P.nw_acc[P.nnw + nw] += t[1];
-                        P.nw_acc[2 * P.nnw + nw] += t[2];
-                        P.nw_accm[nw] += W;
-                    } else {
-                        // FP32 arithmetic end to end
-                        const float nr[3] = {P.nw_nf[nw], P.nw_nf[P.nnw + nw], P.nw_nf[2 * P.nnw + nw]};
-                        float t[3];
-                        if constexpr (MODE == MODE_PARITY) {
-                            wss_fast<Q, float, true>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
-                                                     prev[3 * P.nnw + nw], nr, P.wss_C_f, t);
-                        } else {
-                            float r, ux, uy, uz;
-                            moments<Q, float, true>(g, r, ux, uy, uz);
-                            wss_fast<Q, float, true>(g, r, ux, uy, uz, nr, P.wss_phys_f, t);
-                        }
-                        const float W = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-                        P.nw_wssf[nw] = W;
-                        comp_add(P.nw_accf[nw], t[0]);
-                        comp_add(P.nw_accf[P.nnw + nw], t[1]);
-                        comp_add(P.nw_accf[2 * P.nnw + nw], t[2]);
-                        comp_add(P.nw_accf[3 * P.nnw + nw], W);
-                    }
-                }
-                if constexpr (MODE == MODE_PARITY) {
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) stale[q * P.nsp + s] = g[q];
-                    if (nw >= 0) {
-                        // moments of this step's collision, for the next step's lagged stress
-                        R r, ux, uy, uz;
-                        moments<Q, R, OFF>(g, r, ux, uy, uz);
-                        prev[nw] = r; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
-                    }
-                }
             }
+            if (s < P.nnw) nw = (int)s;
         } else if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
             bool zero = false;
 #pragma unroll
@@ -500,7 +572,6 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
             if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
         }
 
-        // ---- collide and store (every lane), or read out
         if constexpr (KIND == KIND_READOUT) {
             R r, ux, uy, uz;
             moments<Q, R, OFF>(g, r, ux, uy, uz);
@@ -512,11 +583,73 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
                 for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
             }
         } else {
+            // ---- moments of the post-boundary populations: they serve the
+            // wall shear stress (physics), the next step's lagged stress
+            // (parity) and the collision
             R r, ux, uy, uz;
-            collide<Q, R, OFF>(g, inv_tau, r, ux, uy, uz);
+            moments<Q, R, OFF>(g, r, ux, uy, uz);
+            R* __restrict__ prev = static_cast<R*>(P.nw_prev);
+            if (KIND == KIND_STEP && nw >= 0) {
+                if constexpr (!OFF) {
+                    // FP64: the reference's arithmetic
+                    double t[3];
+                    const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
+                    if constexpr (MODE == MODE_PARITY) {
+                        // equilibrium of the previous collision (time-lagged, as the reference)
+                        double e[Q];
+                        feq_all<Q, double, false>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
+                                                  prev[3 * P.nnw + nw]);
+                        wss_reference<Q>(g, e, nn, P.wss_C, t);
+                    } else {
+                        wss_fast<Q, double, false>(g, r, ux, uy, uz, nn, P.wss_phys, t);
+                    }
+                    const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                    P.nw_wss[nw] = W;
+                    P.nw_acc[nw] += t[0];
+                    P.nw_acc[P.nnw + nw] += t[1];
+                    P.nw_acc[2 * P.nnw + nw] += t[2];
+                    P.nw_accm[nw] += W;
+                } else {
+                    // FP32 arithmetic end to end
+                    const float nr[3] = {P.nw_nf[nw], P.nw_nf[P.nnw + nw], P.nw_nf[2 * P.nnw + nw]};
+                    float t[3];
+                    if constexpr (MODE == MODE_PARITY) {
+                        wss_stress<Q>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw], prev[3 * P.nnw + nw], nr,
+                                      P.wss_C_f, t);
+                    } else {
+                        wss_stress<Q>(g, r, ux, uy, uz, nr, P.wss_phys_f, t);
+                    }
+                    const float W = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                    P.nw_wssf[nw] = W;
+                    comp_add(P.nw_accf[nw], t[0]);
+                    comp_add(P.nw_accf[P.nnw + nw], t[1]);
+                    comp_add(P.nw_accf[2 * P.nnw + nw], t[2]);
+                    comp_add(P.nw_accf[3 * P.nnw + nw], W);
+                }
+            }
+            if constexpr (MODE == MODE_PARITY) {
+                if (lng) {
+                    R* __restrict__ stale = static_cast<R*>(P.stale);
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) stale[q * P.nsp + s] = g[q];
+                    if (nw >= 0) {
+                        // moments of this step's collision, for the next step's lagged stress
+                        prev[nw] = r; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
+                    }
+                }
+            }
+            // ---- collide and store (every lane)
+            if constexpr (OFF) {
+                const float om = P.inv_tau_f;
+                const float A = 1.0f + r;
+                const float B = r - 1.5f * A * (ux * ux + uy * uy + uz * uz);
+                relax_pairs<Q>(g, A, B, ux, uy, uz, om, 1.0f - om);
+            } else {
+                relax_all<Q, R, OFF>(g, r, ux, uy, uz, ux * ux + uy * uy + uz * uz, (R)P.inv_tau);
+            }
             if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
 #pragma unroll
-            for (int q = 0; q < Q; ++q) fout[q * P.stride + a] = Store<S>::template pack<Q>(g[q], q);
+            for (int q = 0; q < Q; ++q) fout[q * st + ai] = Store<S>::template pack<Q>(g[q], q);
         }
     }
     if constexpr (KIND == KIND_STEP) {
@@ -532,7 +665,7 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
 struct Variant {
     int bt, minb;
 };
-constexpr Variant kVariants[kNumVariants] = {{256, 1}, {256, 4}, {128, 8}, {512, 2}, {128, 1}};
+constexpr Variant kVariants[kNumVariants] = {{256, 1}, {256, 4}, {128, 8}, {128, 10}, {128, 12}};
 
 template <int Q, typename S, int MODE, int V>
 cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
@@ -540,7 +673,11 @@ cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
     const int64_t nblocks = ceil_div(p.nact, BT);
     if (nblocks <= 0) return cudaSuccess;
     if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    step_kernel<Q, S, MODE, KIND_STEP, BT, MB><<<(unsigned)nblocks, BT, 0, st>>>(p);
+    if ((int64_t)Q * p.stride < ((int64_t)1 << 31))
+        step_kernel<Q, S, MODE, KIND_STEP, BT, MB, false><<<(unsigned)nblocks, BT, 0, st>>>(p);
+    else  // beyond 32-bit offsets: one 64-bit shape for every variant
+        step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true>
+            <<<(unsigned)ceil_div(p.nact, kStepThreads), kStepThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 
