@@ -415,7 +415,7 @@ def run_ours(args):
                     "step": f"{B} LBM steps per call batch + WSS/OSI/TAWSS and rho/u read-back (pinned host buffers)"},
             "gpu_launches": launches,
             "autotune": {"variant": tuned[0], "ms_per_step_by_variant": tuned[1],
-                         "variants": "(block, min blocks/SM): (256,1) (256,4) (128,8) (128,10) (128,12)"},
+                         "variants": "(block, min blocks/SM): (128,12) (128,10) (128,8) (256,3) (256,1)"},
             "clocks": clk.summary(),
             "extra": extra,
         }

@@ -229,7 +229,8 @@ lbm_status lbm_get_launch_count(lbm_handle* h, int64_t* launches);
 lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph);
 
 /* Launch-shape variants of the step kernel (block size x minimum resident
- * blocks per SM).  lbm_autotune times each variant for trial_steps steps on a
+ * blocks per SM): (128,12) (128,10) (128,8) (256,3) (256,1); a new handle
+ * starts on variant 0, FP64 on variant 4.  lbm_autotune times each variant for trial_steps steps on a
  * snapshot of the current state, restores the state, keeps the fastest and
  * reports it (and, if ms_per_step is not NULL, the time of every variant:
  * LBM_NUM_VARIANTS floats).  No reference counterpart (the reference has a

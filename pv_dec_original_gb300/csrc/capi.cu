@@ -43,7 +43,10 @@ struct lbm_handle {
     void* nw_prev = nullptr;
     double *nw_n = nullptr, *nw_wss = nullptr, *nw_acc = nullptr, *nw_accm = nullptr;
     float *nw_nf = nullptr, *nw_wssf = nullptr;  // FP32-arithmetic formats
+    float* nw_ring = nullptr;                      // [kRingSlots][4][nnw]
+    double* nw_out = nullptr;                      // read-out staging, [5][nnw]
     float2* nw_accf = nullptr;
+    bool wss_from_ckpt = false;  // |tau| of the last step comes from a checkpoint (nw_wssf), not the ring
     double* amp = nullptr;
     int64_t namp = 0;
     std::vector<double> amp_host;
@@ -136,7 +139,8 @@ void free_geometry(lbm_handle* h) {
     void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_prof, g.nw_pt, g.act_word, g.sp_of_act,
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
-                    h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf};
+                    h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf,
+                    h->nw_ring, h->nw_out};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     g = GeometryLists();
@@ -146,6 +150,8 @@ void free_geometry(lbm_handle* h) {
     h->nseg = 0;
     h->nw_nf = h->nw_wssf = nullptr;
     h->nw_accf = nullptr;
+    h->nw_ring = nullptr;
+    h->nw_out = nullptr;
     drop_graph(h);
     h->has_geo = h->has_state = false;
     h->geo_bytes = 0;
@@ -181,7 +187,7 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.nw_acc = h->nw_acc;
     p.nw_accm = h->nw_accm;
     p.nw_nf = h->nw_nf;
-    p.nw_wssf = h->nw_wssf;
+    p.nw_ring = h->nw_ring;
     p.nw_accf = h->nw_accf;
     p.nw_prev = h->nw_prev;
     p.tau = h->d.tau;
@@ -222,6 +228,8 @@ int start_state(lbm_handle* h, bool reset) {
         CK(h, cudaMemsetAsync(h->nw_wss, 0, sizeof(double) * (h->g.nnw + 1), h->st));
         CK(h, cudaMemsetAsync(h->nw_accf, 0, sizeof(float2) * 4 * (h->g.nnw + 1), h->st));
         CK(h, cudaMemsetAsync(h->nw_wssf, 0, sizeof(float) * (h->g.nnw + 1), h->st));
+        CK(h, cudaMemsetAsync(h->nw_ring, 0, sizeof(float) * kRingSlots * 4 * (h->g.nnw + 1), h->st));
+        h->wss_from_ckpt = false;
         h->steps = 0;
     }
     int64_t sl[2] = {h->steps, h->steps};
@@ -530,6 +538,9 @@ lbm_status lbm_create(const lbm_desc* desc, lbm_handle** out) {
     lbm_handle* h = new lbm_handle();
     h->d = *desc;
     if (h->d.tawss_div == 0.0) h->d.tawss_div = 0.9;
+    // FP64 keeps every population in two registers: start it on the
+    // unconstrained shape, the FP32-arithmetic formats on the 40-register one
+    h->variant = h->d.precision == LBM_F64 ? kNumVariants - 1 : 0;
     e = cudaSetDevice(desc->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->slots, 2 * sizeof(int64_t));
@@ -634,6 +645,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     CK(h, cudaMemsetAsync(h->nw_nf, 0, sizeof(float) * 3 * (h->g.nnw + 1), h->st));
     CK(h, dalloc(h, &h->nw_wssf, sizeof(float) * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_accf, sizeof(float2) * 4 * (h->g.nnw + 1)));
+    CK(h, dalloc(h, &h->nw_ring, sizeof(float) * kRingSlots * 4 * (h->g.nnw + 1)));
     h->nblocks = ceil_div(h->g.nact, kStepThreads);
     CK(h, dalloc(h, &h->partials, sizeof(double) * kPartialStride * (h->nblocks + 1)));
     CK(h, dalloc(h, &h->sums, sizeof(double) * kPartialStride));
@@ -765,6 +777,7 @@ lbm_status lbm_step_async(lbm_handle* h, int nsteps) {
     REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state: set the geometry first");
     REQUIRE(h, nsteps >= 0, LBM_ERR_ARG, "negative step count");
     CK(h, cudaSetDevice(h->d.device));
+    if (nsteps > 0) h->wss_from_ckpt = false;
     int left = nsteps;
     // Graph replay: a captured graph bakes the buffer roles (cur) and the
     // counter slot (step parity); both flip every step, so a graph built at
@@ -866,16 +879,17 @@ int read_accumulators(lbm_handle* h, std::vector<double>& w, std::vector<double>
         CK(h, cudaStreamSynchronize(h->st));
         return LBM_OK;
     }
-    std::vector<float> wf(n);
-    std::vector<float2> af(4 * n);
-    CK(h, cudaMemcpyAsync(wf.data(), h->nw_wssf, sizeof(float) * n, cudaMemcpyDeviceToHost, h->st));
-    CK(h, cudaMemcpyAsync(af.data(), h->nw_accf, sizeof(float2) * 4 * n, cudaMemcpyDeviceToHost, h->st));
+    // folded steps (accumulators) + the steps since the last fold (ring
+    // slots 0 .. steps % kRingSlots - 1); |tau| of the last step from its slot
+    const int pending = (int)(h->steps % kRingSlots);
+    const int last = h->steps == 0 ? -1 : (int)((h->steps - 1) % kRingSlots);
+    if (!h->nw_out) CK(h, dalloc(h, &h->nw_out, sizeof(double) * 5 * n));
+    CK(h, nw_readout_f32(h->nw_accf, h->nw_ring, n, pending, last, h->wss_from_ckpt ? h->nw_wssf : nullptr,
+                         h->nw_out, h->st));
+    CK(h, cudaMemcpyAsync(w.data(), h->nw_out, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaMemcpyAsync(a.data(), h->nw_out + n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaMemcpyAsync(am.data(), h->nw_out + 4 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
-    for (int64_t p = 0; p < n; ++p) {
-        w[p] = wf[p];
-        for (int c = 0; c < 3; ++c) a[c * n + p] = (double)af[c * n + p].x + (double)af[c * n + p].y;
-        am[p] = (double)af[3 * n + p].x + (double)af[3 * n + p].y;
-    }
     return LBM_OK;
 }
 
@@ -900,6 +914,9 @@ int write_accumulators(lbm_handle* h, const std::vector<double>& w, const std::v
     }
     CK(h, cudaMemcpyAsync(h->nw_wssf, wf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, h->st));
     CK(h, cudaMemcpyAsync(h->nw_accf, af.data(), sizeof(float2) * 4 * n, cudaMemcpyHostToDevice, h->st));
+    // the accumulators hold every step so far: no ring slot is pending
+    CK(h, cudaMemsetAsync(h->nw_ring, 0, sizeof(float) * kRingSlots * 4 * (n + 1), h->st));
+    h->wss_from_ckpt = true;
     CK(h, cudaStreamSynchronize(h->st));
     return LBM_OK;
 }
@@ -1039,7 +1056,8 @@ lbm_status lbm_autotune(lbm_handle* h, int trial_steps, int* best, float* ms_per
         {h->nw_accm, sizeof(double) * (h->g.nnw + 1), nullptr},
         {h->nw_wss, sizeof(double) * (h->g.nnw + 1), nullptr},
         {h->nw_accf, sizeof(float2) * 4 * (h->g.nnw + 1), nullptr},
-        {h->nw_wssf, sizeof(float) * (h->g.nnw + 1), nullptr}};
+        {h->nw_wssf, sizeof(float) * (h->g.nnw + 1), nullptr},
+        {h->nw_ring, sizeof(float) * kRingSlots * 4 * (h->g.nnw + 1), nullptr}};
     if (h->stale) items.push_back({h->stale, rs * h->d.Q * (h->g.nsp + 1), nullptr});
     if (h->nw_prev) items.push_back({h->nw_prev, rs * 4 * (h->g.nnw + 1), nullptr});
     auto release = [&]() {

@@ -13,4 +13,31 @@ cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t str
     }
 }
 
+namespace {
+
+// Next-to-wall read-out of the FP32 formats, as doubles: out[0] = |tau| of
+// the last step, out[1..3] = sum tau, out[4] = sum |tau| (each [nnw]); the
+// sums are the folded accumulators plus the ring slots 0 .. pending-1.
+__global__ void k_nw_readout(const float2* __restrict__ accf, const float* __restrict__ ring, int64_t nnw,
+                             int pending, int last, const float* __restrict__ wss_ckpt, double* __restrict__ out) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nnw) return;
+    out[p] = last < 0 ? 0.0 : wss_ckpt ? (double)wss_ckpt[p] : (double)ring[((int64_t)last * 4 + 3) * nnw + p];
+    for (int k = 0; k < 4; ++k) {
+        const float2 a = accf[k * nnw + p];
+        double v = (double)a.x + (double)a.y;
+        for (int j = 0; j < pending; ++j) v += (double)ring[((int64_t)j * 4 + k) * nnw + p];
+        out[(1 + k) * nnw + p] = v;
+    }
+}
+
+}  // namespace
+
+cudaError_t nw_readout_f32(const float2* accf, const float* ring, int64_t nnw, int pending, int last,
+                           const float* wss_ckpt, double* out, cudaStream_t st) {
+    if (nnw <= 0) return cudaSuccess;
+    k_nw_readout<<<(unsigned)ceil_div(nnw, 256), 256, 0, st>>>(accf, ring, nnw, pending, last, wss_ckpt, out);
+    return cudaGetLastError();
+}
+
 }  // namespace lbm

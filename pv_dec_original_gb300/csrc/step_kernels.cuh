@@ -396,6 +396,19 @@ __device__ __forceinline__ void comp_add(float2& acc, float v) {
     acc.y += c;
 }
 
+// Every kRingSlots-th step: add the ring's slots 0 .. kRingSlots-2 and this
+// step's stresses t, in step order, to next-to-wall node nw's accumulators.
+static __device__ __noinline__ void fold_ring(const StepParams& P, int nw, const float (&t)[4]) {
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        float2 acc = P.nw_accf[k * P.nnw + nw];
+#pragma unroll 5
+        for (int j = 0; j < kRingSlots - 1; ++j) comp_add(acc, P.nw_ring[((int64_t)j * 4 + k) * P.nnw + nw]);
+        comp_add(acc, t[k]);
+        P.nw_accf[k * P.nnw + nw] = acc;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Block reduction of the read-out sums (rho - 1, momentum, per-BC flux).
 
@@ -432,9 +445,7 @@ __device__ __forceinline__ bool is_exact_zero(R v, int q) {
 // ---------------------------------------------------------------------------
 // The kernel.
 
-__device__ __forceinline__ void prefetch_l2(const void* p) {
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
+
 
 // Packed per-node word (built by setup.cu):
 //   bits  0-30  segment id: the pull source of population q is node a + delta[seg][q]
@@ -448,209 +459,219 @@ __device__ __forceinline__ uint32_t word_miss(uint64_t w) { return (uint32_t)((w
 __device__ __forceinline__ int word_class(uint64_t w) { return (int)((w >> 59) & 0xfull); }
 __device__ __forceinline__ bool word_nw(uint64_t w) { return (w >> 63) & 1ull; }
 
-// WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
-// lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
-template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1, bool WIDE = true>
-__global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
+// One node's update: pull, boundary rules, wall shear stress, collision and
+// store (or the read-out sums).
+template <int Q, typename S, int MODE, int KIND, bool WIDE>
+__device__ __forceinline__ void node_update(const StepParams& P, const int64_t a, const uint64_t word,
+                                            const int32_t sp_entry, double (&part)[kPartialStride]) {
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
     using R = typename Store<S>::real;
     constexpr bool OFF = Store<S>::offset;
     constexpr int DR = kDeltaRow<Q>;
     const S* __restrict__ fin = static_cast<const S*>(P.fin);
     S* __restrict__ fout = static_cast<S*>(P.fout);
+    const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
+    constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
+    const uint32_t miss = word_miss(word);  // zero on interior nodes
+    const int c = word_class(word);
+    // Boundary-list work: in parity mode every boundary-list node (history
+    // of missing links, the wall rule); in physics mode only
+    // boundary-condition and next-to-wall nodes (bounce-back is folded
+    // into the loads).  The list entry is fetched before the loads.
+    const bool lng = MODE == MODE_PARITY ? word_special(word) : (c >= CLS_BC0 || word_nw(word));
+    const int64_t s = lng ? (int64_t)sp_entry : 0;
+    // FP32 formats: a next-to-wall node loads its normal now, beside the
+    // populations, so the stress below waits on nothing
+    float nr[3] = {0.f, 0.f, 0.f};
+    int slot = 0;
+    if constexpr (OFF && KIND == KIND_STEP) {
+        if (lng && s < P.nnw) {
+            nr[0] = __ldg(P.nw_nf + s);
+            nr[1] = __ldg(P.nw_nf + P.nnw + s);
+            nr[2] = __ldg(P.nw_nf + 2 * P.nnw + s);
+            slot = (int)(*P.step_base % kRingSlots);
+        }
+    }
+
+    // ---- stream: one load per population, issued by every lane together.
+    // A link whose source is missing reads, in physics mode, the node's
+    // own opposite population (half-way bounce-back); in parity mode any
+    // valid address -- the previous value replaces it below.
+    const I ai = (I)a, st = (I)P.stride;
+    R g[Q];
+    if (direct) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin + (q * st + ai), q);
+    } else {
+        int32_t dl[DR];
+        const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
+#pragma unroll
+        for (int k = 0; k < DR / 4; ++k) {
+            const int4 v = __ldg(drow + k);
+            dl[4 * k] = v.x; dl[4 * k + 1] = v.y; dl[4 * k + 2] = v.z; dl[4 * k + 3] = v.w;
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const bool src_missing = (miss >> Lat<Q>::opp(q)) & 1u;
+            I idx;
+            if (q == Lat<Q>::REST) {
+                idx = q * st + ai;
+            } else if (MODE == MODE_PHYSICS) {
+                idx = src_missing ? Lat<Q>::opp(q) * st + ai : q * st + ai + dl[q];
+            } else {
+                idx = q * st + (src_missing ? ai : ai + dl[q]);
+            }
+            g[q] = Store<S>::template load<Q>(fin + idx, q);  // w_opp(q) == w_q: same decode
+        }
+    }
+
+    int nw = -1;  // next-to-wall index: boundary-list entries below nnw
+    if (lng) {
+        // ---- boundary-list node: history, boundary rules
+        R* __restrict__ stale = static_cast<R*>(P.stale);
+        if constexpr (MODE == MODE_PARITY) {
+            if (parity_readout) {
+                // the boundary list keeps the exact post-boundary f of the last step
+#pragma unroll
+                for (int q = 0; q < Q; ++q) g[q] = stale[q * P.nsp + s];
+            } else if (!direct) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q)
+                    if (((miss >> Lat<Q>::opp(q)) & 1u) || is_exact_zero<Q, R, OFF>(g[q], q))
+                        g[q] = stale[q * P.nsp + s];
+            }
+        }
+        if (!direct && !parity_readout) {
+            if (c >= CLS_BC0) {
+                double amp = 0.0;
+                if (P.namp > 0) {
+                    int64_t t = (*P.step_base + P.step_off) % P.namp;
+                    if (t < 0) t += P.namp;
+                    amp = __ldg(P.amp + t);
+                }
+                apply_bc<Q, R, OFF>(g, P.bc[c - CLS_BC0], amp, __ldg(P.sp_prof + s));
+            } else if (MODE == MODE_PARITY && c == CLS_WALL) {
+                // ApplyWallBc: in place, direction order (Simulation.cpp:846-861)
+#pragma unroll
+                for (int q = 0; q < Q; ++q)
+                    if ((miss >> q) & 1u) g[Lat<Q>::opp(q)] = g[q];
+            }
+        }
+        if constexpr (KIND == KIND_READOUT) {
+            if (c >= CLS_BC0) {
+                R r, ux, uy, uz;
+                moments<Q, R, OFF>(g, r, ux, uy, uz);
+                const double rho = OFF ? 1.0 + (double)r : (double)r;
+                const double j[3] = {rho * ux, rho * uy, rho * uz};
+                part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
+            }
+        }
+        if (s < P.nnw) nw = (int)s;
+    } else if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
+        bool zero = false;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) zero |= is_exact_zero<Q, R, OFF>(g[q], q);
+        if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
+    }
+
+    if constexpr (KIND == KIND_READOUT) {
+        R r, ux, uy, uz;
+        moments<Q, R, OFF>(g, r, ux, uy, uz);
+        const double rho = OFF ? 1.0 + (double)r : (double)r;
+        part[0] = OFF ? (double)r : rho - 1.0;
+        part[1] = rho * ux; part[2] = rho * uy; part[3] = rho * uz;
+        if (P.out_f) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
+        }
+    } else {
+        // ---- moments of the post-boundary populations: they serve the
+        // wall shear stress (physics), the next step's lagged stress
+        // (parity) and the collision
+        R r, ux, uy, uz;
+        moments<Q, R, OFF>(g, r, ux, uy, uz);
+        R* __restrict__ prev = static_cast<R*>(P.nw_prev);
+        if (KIND == KIND_STEP && nw >= 0) {
+            if constexpr (!OFF) {
+                // FP64: the reference's arithmetic
+                double t[3];
+                const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
+                if constexpr (MODE == MODE_PARITY) {
+                    // equilibrium of the previous collision (time-lagged, as the reference)
+                    double e[Q];
+                    feq_all<Q, double, false>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
+                                              prev[3 * P.nnw + nw]);
+                    wss_reference<Q>(g, e, nn, P.wss_C, t);
+                } else {
+                    wss_fast<Q, double, false>(g, r, ux, uy, uz, nn, P.wss_phys, t);
+                }
+                const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                P.nw_wss[nw] = W;
+                P.nw_acc[nw] += t[0];
+                P.nw_acc[P.nnw + nw] += t[1];
+                P.nw_acc[2 * P.nnw + nw] += t[2];
+                P.nw_accm[nw] += W;
+            } else {
+                // FP32 arithmetic end to end
+                float t[4];
+                if constexpr (MODE == MODE_PARITY) {
+                    wss_stress<Q>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw], prev[3 * P.nnw + nw], nr,
+                                  P.wss_C_f, t);
+                } else {
+                    wss_stress<Q>(g, r, ux, uy, uz, nr, P.wss_phys_f, t);
+                }
+                t[3] = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                // this step's slot of the ring; the ring's last slot folds
+                // all kRingSlots steps, in step order, into the accumulators
+                float* __restrict__ ring = P.nw_ring + (int64_t)slot * 4 * P.nnw + nw;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) ring[k * P.nnw] = t[k];
+                if (slot == kRingSlots - 1) fold_ring(P, nw, t);
+            }
+        }
+        if constexpr (MODE == MODE_PARITY) {
+            if (lng) {
+                R* __restrict__ stale = static_cast<R*>(P.stale);
+#pragma unroll
+                for (int q = 0; q < Q; ++q) stale[q * P.nsp + s] = g[q];
+                if (nw >= 0) {
+                    // moments of this step's collision, for the next step's lagged stress
+                    prev[nw] = r; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
+                }
+            }
+        }
+        // ---- collide and store (every lane)
+        if constexpr (OFF) {
+            const float om = P.inv_tau_f;
+            const float A = 1.0f + r;
+            const float B = r - 1.5f * A * (ux * ux + uy * uy + uz * uz);
+            relax_pairs<Q>(g, A, B, ux, uy, uz, om, 1.0f - om);
+        } else {
+            relax_all<Q, R, OFF>(g, r, ux, uy, uz, ux * ux + uy * uy + uz * uz, (R)P.inv_tau);
+        }
+        if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) fout[q * st + ai] = Store<S>::template pack<Q>(g[q], q);
+    }
+}
+
+// WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
+// lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
+// One thread per active node.
+template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1, bool WIDE = true>
+__global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
     double part[kPartialStride];
     if constexpr (KIND == KIND_READOUT) {
 #pragma unroll
         for (int k = 0; k < kPartialStride; ++k) part[k] = 0.0;
     }
     const int64_t a = (int64_t)blockIdx.x * BT + threadIdx.x;
-    const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
-    constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
-
     if (a < P.nact) {
         // the node's word and its boundary-list entry (-1 for most nodes),
         // loaded side by side
         const uint64_t word = __ldg(P.act_word + a);
         const int32_t sp_entry = __ldg(P.sp_of_act + a);
-        const uint32_t miss = word_miss(word);  // zero on interior nodes
-        const int c = word_class(word);
-        // Boundary-list work: in parity mode every boundary-list node (history
-        // of missing links, the wall rule); in physics mode only
-        // boundary-condition and next-to-wall nodes (bounce-back is folded
-        // into the loads).  The list entry is fetched before the loads.
-        const bool lng = MODE == MODE_PARITY ? word_special(word) : (c >= CLS_BC0 || word_nw(word));
-        const int64_t s = lng ? (int64_t)sp_entry : 0;
-        if (KIND == KIND_STEP && lng && s < P.nnw) {
-            // next-to-wall node: pull its normal and accumulators towards L2
-            // while the populations load
-            if constexpr (OFF) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) prefetch_l2(P.nw_accf + k * P.nnw + s);
-#pragma unroll
-                for (int k = 0; k < 3; ++k) prefetch_l2(P.nw_nf + k * P.nnw + s);
-            }
-        }
-
-        // ---- stream: one load per population, issued by every lane together.
-        // A link whose source is missing reads, in physics mode, the node's
-        // own opposite population (half-way bounce-back); in parity mode any
-        // valid address -- the previous value replaces it below.
-        const I ai = (I)a, st = (I)P.stride;
-        R g[Q];
-        if (direct) {
-#pragma unroll
-            for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin + (q * st + ai), q);
-        } else {
-            int32_t dl[DR];
-            const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
-#pragma unroll
-            for (int k = 0; k < DR / 4; ++k) {
-                const int4 v = __ldg(drow + k);
-                dl[4 * k] = v.x; dl[4 * k + 1] = v.y; dl[4 * k + 2] = v.z; dl[4 * k + 3] = v.w;
-            }
-#pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                const bool src_missing = (miss >> Lat<Q>::opp(q)) & 1u;
-                I idx;
-                if (q == Lat<Q>::REST) {
-                    idx = q * st + ai;
-                } else if (MODE == MODE_PHYSICS) {
-                    idx = src_missing ? Lat<Q>::opp(q) * st + ai : q * st + ai + dl[q];
-                } else {
-                    idx = q * st + (src_missing ? ai : ai + dl[q]);
-                }
-                g[q] = Store<S>::template load<Q>(fin + idx, q);  // w_opp(q) == w_q: same decode
-            }
-        }
-
-        int nw = -1;  // next-to-wall index: boundary-list entries below nnw
-        if (lng) {
-            // ---- boundary-list node: history, boundary rules
-            R* __restrict__ stale = static_cast<R*>(P.stale);
-            if constexpr (MODE == MODE_PARITY) {
-                if (parity_readout) {
-                    // the boundary list keeps the exact post-boundary f of the last step
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) g[q] = stale[q * P.nsp + s];
-                } else if (!direct) {
-#pragma unroll
-                    for (int q = 0; q < Q; ++q)
-                        if (((miss >> Lat<Q>::opp(q)) & 1u) || is_exact_zero<Q, R, OFF>(g[q], q))
-                            g[q] = stale[q * P.nsp + s];
-                }
-            }
-            if (!direct && !parity_readout) {
-                if (c >= CLS_BC0) {
-                    double amp = 0.0;
-                    if (P.namp > 0) {
-                        int64_t t = (*P.step_base + P.step_off) % P.namp;
-                        if (t < 0) t += P.namp;
-                        amp = __ldg(P.amp + t);
-                    }
-                    apply_bc<Q, R, OFF>(g, P.bc[c - CLS_BC0], amp, __ldg(P.sp_prof + s));
-                } else if (MODE == MODE_PARITY && c == CLS_WALL) {
-                    // ApplyWallBc: in place, direction order (Simulation.cpp:846-861)
-#pragma unroll
-                    for (int q = 0; q < Q; ++q)
-                        if ((miss >> q) & 1u) g[Lat<Q>::opp(q)] = g[q];
-                }
-            }
-            if constexpr (KIND == KIND_READOUT) {
-                if (c >= CLS_BC0) {
-                    R r, ux, uy, uz;
-                    moments<Q, R, OFF>(g, r, ux, uy, uz);
-                    const double rho = OFF ? 1.0 + (double)r : (double)r;
-                    const double j[3] = {rho * ux, rho * uy, rho * uz};
-                    part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
-                }
-            }
-            if (s < P.nnw) nw = (int)s;
-        } else if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
-            bool zero = false;
-#pragma unroll
-            for (int q = 0; q < Q; ++q) zero |= is_exact_zero<Q, R, OFF>(g[q], q);
-            if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
-        }
-
-        if constexpr (KIND == KIND_READOUT) {
-            R r, ux, uy, uz;
-            moments<Q, R, OFF>(g, r, ux, uy, uz);
-            const double rho = OFF ? 1.0 + (double)r : (double)r;
-            part[0] = OFF ? (double)r : rho - 1.0;
-            part[1] = rho * ux; part[2] = rho * uy; part[3] = rho * uz;
-            if (P.out_f) {
-#pragma unroll
-                for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
-            }
-        } else {
-            // ---- moments of the post-boundary populations: they serve the
-            // wall shear stress (physics), the next step's lagged stress
-            // (parity) and the collision
-            R r, ux, uy, uz;
-            moments<Q, R, OFF>(g, r, ux, uy, uz);
-            R* __restrict__ prev = static_cast<R*>(P.nw_prev);
-            if (KIND == KIND_STEP && nw >= 0) {
-                if constexpr (!OFF) {
-                    // FP64: the reference's arithmetic
-                    double t[3];
-                    const double nn[3] = {P.nw_n[nw], P.nw_n[P.nnw + nw], P.nw_n[2 * P.nnw + nw]};
-                    if constexpr (MODE == MODE_PARITY) {
-                        // equilibrium of the previous collision (time-lagged, as the reference)
-                        double e[Q];
-                        feq_all<Q, double, false>(e, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw],
-                                                  prev[3 * P.nnw + nw]);
-                        wss_reference<Q>(g, e, nn, P.wss_C, t);
-                    } else {
-                        wss_fast<Q, double, false>(g, r, ux, uy, uz, nn, P.wss_phys, t);
-                    }
-                    const double W = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-                    P.nw_wss[nw] = W;
-                    P.nw_acc[nw] += t[0];
-                    P.nw_acc[P.nnw + nw] += t[1];
-                    P.nw_acc[2 * P.nnw + nw] += t[2];
-                    P.nw_accm[nw] += W;
-                } else {
-                    // FP32 arithmetic end to end
-                    const float nr[3] = {P.nw_nf[nw], P.nw_nf[P.nnw + nw], P.nw_nf[2 * P.nnw + nw]};
-                    float t[3];
-                    if constexpr (MODE == MODE_PARITY) {
-                        wss_stress<Q>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw], prev[3 * P.nnw + nw], nr,
-                                      P.wss_C_f, t);
-                    } else {
-                        wss_stress<Q>(g, r, ux, uy, uz, nr, P.wss_phys_f, t);
-                    }
-                    const float W = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-                    P.nw_wssf[nw] = W;
-                    comp_add(P.nw_accf[nw], t[0]);
-                    comp_add(P.nw_accf[P.nnw + nw], t[1]);
-                    comp_add(P.nw_accf[2 * P.nnw + nw], t[2]);
-                    comp_add(P.nw_accf[3 * P.nnw + nw], W);
-                }
-            }
-            if constexpr (MODE == MODE_PARITY) {
-                if (lng) {
-                    R* __restrict__ stale = static_cast<R*>(P.stale);
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) stale[q * P.nsp + s] = g[q];
-                    if (nw >= 0) {
-                        // moments of this step's collision, for the next step's lagged stress
-                        prev[nw] = r; prev[P.nnw + nw] = ux; prev[2 * P.nnw + nw] = uy; prev[3 * P.nnw + nw] = uz;
-                    }
-                }
-            }
-            // ---- collide and store (every lane)
-            if constexpr (OFF) {
-                const float om = P.inv_tau_f;
-                const float A = 1.0f + r;
-                const float B = r - 1.5f * A * (ux * ux + uy * uy + uz * uz);
-                relax_pairs<Q>(g, A, B, ux, uy, uz, om, 1.0f - om);
-            } else {
-                relax_all<Q, R, OFF>(g, r, ux, uy, uz, ux * ux + uy * uy + uz * uz, (R)P.inv_tau);
-            }
-            if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
-#pragma unroll
-            for (int q = 0; q < Q; ++q) fout[q * st + ai] = Store<S>::template pack<Q>(g[q], q);
-        }
+        node_update<Q, S, MODE, KIND, WIDE>(P, a, word, sp_entry, part);
     }
     if constexpr (KIND == KIND_STEP) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
@@ -660,12 +681,13 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
 
 // Launch-shape variants of the step kernel, picked by the autotuner
 // (lbm_autotune): block size and the minimum resident blocks per SM, which
-// caps registers per thread (65536 / (BT * MINB)) to trade per-thread
-// registers for more warps in flight on this latency-bound stencil.
+// caps registers per thread at 65536 / (BT * MINB) -- more warps in flight
+// on this latency-bound stencil against fewer registers (FP32 D3Q19 fits
+// 40; D3Q27 and FP64 want more).
 struct Variant {
     int bt, minb;
 };
-constexpr Variant kVariants[kNumVariants] = {{256, 1}, {256, 4}, {128, 8}, {128, 10}, {128, 12}};
+constexpr Variant kVariants[kNumVariants] = {{128, 12}, {128, 10}, {128, 8}, {256, 3}, {256, 1}};
 
 template <int Q, typename S, int MODE, int V>
 cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
