@@ -215,6 +215,69 @@ def time_steps(cr, s, steps, flush, stream):
     return ms
 
 
+def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
+    """Aggregate MLUPS of the C4 ensemble packed into one lattice (captured
+    graph, one step-kernel launch per step) against the same members as
+    separate lattices advanced together (each its own stream and graph).
+    The members' populations (FP16, about 1 GB) exceed the L2, so
+    consecutive steps are timed without a flush."""
+    from pv_dec_original_gb300 import geometry as G
+    from pv_dec_original_gb300 import waveform
+    from pv_dec_original_gb300.ensemble import Ensemble
+    members = G.config_c4_ensemble(nmem, seed=0)
+    t0 = time.perf_counter()
+    ens = Ensemble(members, Q, "f16", TAU, device=device)
+    setup_s = time.perf_counter() - t0
+    ens.solver.autotune(5)
+    ens.solver.set_graph_steps(32)
+    st = ens.solver.stream()
+    ens.step(64)
+    a, b = cr.event(), cr.event()
+    cr.record(a, st)
+    ens.step_async(steps)
+    cr.record(b, st)
+    ms = cr.elapsed_ms(a, b)
+    ens.solver.check_status()
+    packed = ens.active * steps / (ms * 1e-3) / 1e6
+    # the same members as separate lattices
+    singles = []
+    for m in members:
+        tri = m["surface"].tri12()
+        mask, vd = capi.voxelize(tri, 1.0)
+        bb = np.array(vd.bbox[:])
+        fl = np.argwhere(mask > 0)
+        kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
+        s = capi.Solver(Q, "f16", capi.LBM_PHYSICS, TAU, 1.0, (bb[0], bb[2], bb[4]), 1.0, 1.0, device)
+        s.set_geometry(mask, [capi.bc_spec(capi.LBM_BC_VELOCITY, "z-", kin, 1.0, 1, m["center"][0], m["center"][1],
+                                           m["radius"]), capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)])
+        s.set_normals(tri)
+        s.set_inlet_table(waveform.sinusoid_table(m["inlet_mean"], m["period"]))
+        s.set_graph_steps(32)
+        s.step(64)
+        singles.append(s)
+    for s in singles:
+        s.sync()
+    t0 = time.perf_counter()
+    for s in singles:
+        s.step_async(steps)
+    for s in singles:
+        s.sync()
+    loop_s = time.perf_counter() - t0
+    active = sum(s.counts()["active"] for s in singles)
+    looped = active * steps / loop_s / 1e6
+    for s in singles:
+        s.close()
+    launches = ens.solver.launches()
+    ens.solver.close()
+    return {"members": nmem, "active_nodes": ens.active, "storage": "f16", "steps": steps,
+            "packed_mlups": packed, "packed_ms_per_step": ms / steps,
+            "packed_hbm_gbs": ens.active * BYTES_PER_LU[(Q, "f16")] / (ms / steps * 1e-3) / 1e9,
+            "looped_mlups": looped, "speedup_vs_looped": packed / looped, "setup_s": setup_s,
+            "timing": "packed: CUDA events around 64 graph-replayed steps; looped: host wall clock around "
+                      "64 steps of each of the 64 lattices issued on their own streams",
+            "l2": "not flushed (populations exceed L2)", "launches_total": launches}
+
+
 def read_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -343,6 +406,11 @@ def run_ours(args):
                               "hbm_gbs": active * BYTES_PER_LU[(args.Q, "f16")] / (m16 * 1e-3) / 1e9,
                               "ms_per_step": m16, "speedup_vs_f32": mean_ms / m16}
         s16.close()
+
+    # batched ensemble (64 seeded stenosed tubes, FP16 storage): one packed
+    # lattice, one launch per step, vs the same members as 64 lattices
+    if not args.quick and not args.no_ensemble:
+        extra["ensemble_c4"] = ensemble_extra(capi, cr, local, args.Q)
 
     # end to end through the C ABI: per e2e step, H2D of a 100-step inlet
     # table slice from pinned memory, 100 LBM steps (graph replay), D2H of
@@ -480,7 +548,8 @@ def main():
     ap.add_argument("--Q", type=int, default=19, choices=[19, 27])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--quick", action="store_true", help="skip the secondary FP16 measurement")
+    ap.add_argument("--quick", action="store_true", help="skip the secondary FP16 and ensemble measurements")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--variant", type=int, default=None, help="force a launch shape (skips the autotuner)")
     args = ap.parse_args()

@@ -78,7 +78,11 @@ typedef int lbm_status;
 #define LBM_FACE_ZMIN 4
 #define LBM_FACE_ZMAX 5
 
-#define LBM_MAX_BC 8
+/* Boundary-condition rules per handle (an ensemble packs one inlet and one
+ * outlet rule per member into one lattice). */
+#define LBM_MAX_BC 256
+/* Inlet waveforms per handle (lbm_set_waveform). */
+#define LBM_MAX_WAVES 256
 
 typedef struct lbm_handle lbm_handle;
 
@@ -150,6 +154,9 @@ typedef struct {
     int region;
     double coord, tol;
     double lo[2], hi[2];
+    /* Velocity kinds: the waveform (lbm_set_waveform) whose amplitude scales
+     * the velocity each step; 0 is the table of lbm_set_inlet_table. */
+    int wave;
 } lbm_bc_spec;
 
 /* mask: nx*ny*nz bytes (nonzero = Fluid).  Builds classes, boundary lists,
@@ -160,11 +167,20 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
 
 /* Wall / next-to-wall normals from the surface (Subdomain.cpp:224-370). */
 lbm_status lbm_set_normals_from_surface(lbm_handle* h, const double* tri12, int64_t ntri);
+/* The same for the next-to-wall nodes whose coordinates lie in the box
+ * lo <= x < hi only (one member of a packed ensemble and its own surface).
+ * No reference counterpart (the reference holds one vessel). */
+lbm_status lbm_set_normals_from_surface_box(lbm_handle* h, const double* tri12, int64_t ntri, const double lo[3],
+                                            const double hi[3]);
 
 /* Inlet amplitude per step: step s uses amp[s % n] (times the node's
  * profile factor and the spec's value).  Replaces InletVelocity_ =
  * getInletVelocity(t, 0.9) (Simulation.cpp:580). */
 lbm_status lbm_set_inlet_table(lbm_handle* h, const double* amp, int64_t n);
+/* Waveform `wave` (0 <= wave < LBM_MAX_WAVES; 0 is the inlet table above):
+ * a velocity rule with this wave uses amp[s % n] at step s.  No reference
+ * counterpart (the reference has one inlet waveform). */
+lbm_status lbm_set_waveform(lbm_handle* h, int wave, const double* amp, int64_t n);
 
 /* f = w_i, accumulators cleared, step counter 0 (Node.cpp:30-37,
  * Simulation.cpp:85-91). */

@@ -18,7 +18,8 @@ LBM_PARITY, LBM_PHYSICS = 0, 1
 LBM_BC_REF_INLET, LBM_BC_REF_OUTLET_YMAX, LBM_BC_REF_OUTLET_ZMIN, LBM_BC_VELOCITY, LBM_BC_PRESSURE = 1, 2, 3, 4, 5
 FACES = {"x-": 0, "x+": 1, "y-": 2, "y+": 3, "z-": 4, "z+": 5}
 PRECISIONS = {"f64": LBM_F64, "f32": LBM_F32, "f16": LBM_F16, "bf16": LBM_BF16}
-MAX_BC = 8
+MAX_BC = 256
+MAX_WAVES = 256
 
 ERRORS = {-1: "LBM_ERR_ARG", -2: "LBM_ERR_CUDA", -3: "LBM_ERR_STATE", -4: "LBM_ERR_NONFINITE",
           -5: "LBM_ERR_ALLOC", -6: "LBM_ERR_IO", -7: "LBM_ERR_UNSUPPORTED"}
@@ -46,7 +47,7 @@ class BCSpec(C.Structure):
     _fields_ = [("kind", C.c_int), ("face", C.c_int), ("plane", C.c_int), ("value", C.c_double),
                 ("profile", C.c_int), ("c1", C.c_double), ("c2", C.c_double), ("R", C.c_double),
                 ("region", C.c_int), ("coord", C.c_double), ("tol", C.c_double), ("lo", C.c_double * 2),
-                ("hi", C.c_double * 2)]
+                ("hi", C.c_double * 2), ("wave", C.c_int)]
 
 
 class Counts(C.Structure):
@@ -58,7 +59,8 @@ class Counts(C.Structure):
 _lib = None
 EXPORTS = [
     "lbm_voxelize", "lbm_read_stl_ascii", "lbm_create", "lbm_destroy", "lbm_last_error", "lbm_last_global_error",
-    "lbm_set_geometry", "lbm_set_normals_from_surface", "lbm_set_inlet_table", "lbm_init_equilibrium",
+    "lbm_set_geometry", "lbm_set_normals_from_surface", "lbm_set_normals_from_surface_box", "lbm_set_inlet_table",
+    "lbm_set_waveform", "lbm_init_equilibrium",
     "lbm_init_from_macro", "lbm_step", "lbm_step_async", "lbm_check_status", "lbm_sync", "lbm_get_counts", "lbm_get_classes", "lbm_get_distributions",
     "lbm_set_distributions", "lbm_get_macro", "lbm_get_wss", "lbm_get_conservation", "lbm_save", "lbm_load",
     "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_autotune", "lbm_set_variant",
@@ -97,6 +99,8 @@ def load(build_if_missing: bool = True):
     L.lbm_set_geometry.argtypes = [P, u8, C.POINTER(C.c_int), C.POINTER(BCSpec), C.c_int]
     L.lbm_set_normals_from_surface.argtypes = [P, dp, C.c_int64]
     L.lbm_set_inlet_table.argtypes = [P, dp, C.c_int64]
+    L.lbm_set_waveform.argtypes = [P, C.c_int, dp, C.c_int64]
+    L.lbm_set_normals_from_surface_box.argtypes = [P, dp, C.c_int64, dp, dp]
     L.lbm_init_equilibrium.argtypes = [P]
     L.lbm_init_from_macro.argtypes = [P, fp, fp, C.c_int]
     L.lbm_step.argtypes = [P, C.c_int]
@@ -163,12 +167,14 @@ def voxelize(tri12, spacing, bbox=None, origin=None, dims=None):
     return mask.reshape(nz, ny, nx), d
 
 
-def bc_spec(kind, face=0, plane=-1, value=1.0, profile=0, c1=0.0, c2=0.0, R=1.0, region=None):
+def bc_spec(kind, face=0, plane=-1, value=1.0, profile=0, c1=0.0, c2=0.0, R=1.0, region=None, wave=0):
     """Boundary rule.  region=(coord, tol, (lo1, hi1), (lo2, hi2)) selects
-    points by coordinates instead of a lattice plane."""
+    points by coordinates instead of a lattice plane; wave picks the inlet
+    waveform of a velocity rule (0: the inlet table)."""
     if isinstance(face, str):
         face = FACES[face]
     b = BCSpec(kind, face, plane, value, profile, c1, c2, R)
+    b.wave = wave
     if region is not None:
         coord, tol, (lo1, hi1), (lo2, hi2) = region
         b.region, b.coord, b.tol = 1, coord, tol
@@ -221,6 +227,16 @@ class Solver:
     def set_normals(self, tri12):
         t = np.ascontiguousarray(tri12, np.float64)
         self._c(load().lbm_set_normals_from_surface(self.h, t, len(t)))
+
+    def set_normals_box(self, tri12, lo, hi):
+        """Normals of the next-to-wall nodes inside lo <= x < hi from these triangles."""
+        t = np.ascontiguousarray(tri12, np.float64)
+        self._c(load().lbm_set_normals_from_surface_box(self.h, t, len(t), np.asarray(lo, np.float64),
+                                                        np.asarray(hi, np.float64)))
+
+    def set_waveform(self, wave, amp):
+        a = np.ascontiguousarray(amp, np.float64)
+        self._c(load().lbm_set_waveform(self.h, int(wave), a, len(a)))
 
     def set_inlet_table(self, amp):
         a = np.ascontiguousarray(np.atleast_1d(amp), np.float64)

@@ -47,14 +47,20 @@ struct lbm_handle {
     double* nw_out = nullptr;                      // read-out staging, [5][nnw]
     float2* nw_accf = nullptr;
     bool wss_from_ckpt = false;  // |tau| of the last step comes from a checkpoint (nw_wssf), not the ring
+    // inlet waveforms: host tables, device concatenation with per-wave offset / length
+    std::vector<std::vector<double>> waves;
     double* amp = nullptr;
-    int64_t namp = 0;
-    std::vector<double> amp_host;
+    int64_t amp_cap = 0;
+    int64_t* wave_off = nullptr;  // [LBM_MAX_WAVES]
+    int64_t* wave_len = nullptr;  // [LBM_MAX_WAVES]
     int64_t* slots = nullptr;   // step counter, two slots (even / odd launches)
     int64_t steps = 0;          // steps taken
     int64_t since_start = 0;    // steps since the last start
     unsigned* flags = nullptr;
-    BCDev bc[LBM_MAX_BC]{};
+    std::vector<BCDev> bc;          // boundary-condition rules (host copy)
+    BCDev* bct = nullptr;           // the same on the device
+    std::vector<int32_t> sp_bc;     // rule of each boundary-list entry (host copy)
+    double* sp_flux = nullptr;      // read-out: per-entry flux
     int nbc = 0;
     int64_t launches = 0;
     int64_t nblocks = 0;
@@ -134,9 +140,39 @@ void drop_graph(lbm_handle* h) {
     h->gexec_parity = -1;
 }
 
+// Concatenate the host waveforms into the device table; unset waveforms
+// have length 0 (amplitude 0).
+int upload_waves(lbm_handle* h) {
+    CK(h, cudaStreamSynchronize(h->st));
+    std::vector<int64_t> off(LBM_MAX_WAVES, 0), len(LBM_MAX_WAVES, 0);
+    int64_t total = 0;
+    for (size_t w = 0; w < h->waves.size(); ++w) {
+        off[w] = total;
+        len[w] = (int64_t)h->waves[w].size();
+        total += len[w];
+    }
+    if (total > h->amp_cap) {
+        drop_graph(h);  // the table pointer is baked into captured launches
+        if (h->amp) cudaFree(h->amp);
+        h->amp = nullptr;
+        h->amp_cap = 0;
+        CK(h, cudaMalloc(&h->amp, sizeof(double) * total));
+        h->amp_cap = total;
+    }
+    for (size_t w = 0; w < h->waves.size(); ++w)
+        if (len[w] > 0)
+            CK(h, cudaMemcpyAsync(h->amp + off[w], h->waves[w].data(), sizeof(double) * len[w],
+                                  cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaMemcpyAsync(h->wave_off, off.data(), sizeof(int64_t) * LBM_MAX_WAVES, cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaMemcpyAsync(h->wave_len, len.data(), sizeof(int64_t) * LBM_MAX_WAVES, cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
 void free_geometry(lbm_handle* h) {
     GeometryLists& g = h->g;
-    void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_prof, g.nw_pt, g.act_word, g.sp_of_act,
+    void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_bc, g.bcidx, g.sp_prof, g.nw_pt, g.act_word,
+                    g.sp_of_act, h->bct, h->sp_flux,
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
                     h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf,
@@ -148,6 +184,8 @@ void free_geometry(lbm_handle* h) {
     h->nw_n = h->nw_wss = h->nw_acc = h->nw_accm = h->partials = h->sums = h->out_f = h->macro = nullptr;
     h->seg_delta = nullptr;
     h->nseg = 0;
+    h->bct = nullptr;
+    h->sp_flux = nullptr;
     h->nw_nf = h->nw_wssf = nullptr;
     h->nw_accf = nullptr;
     h->nw_ring = nullptr;
@@ -198,12 +236,15 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.wss_phys = -(1.0 - 0.5 / h->d.tau) * h->d.wss_scale;
     p.wss_phys_f = (float)p.wss_phys;
     p.amp = h->amp;
-    p.namp = h->namp;
+    p.wave_off = h->wave_off;
+    p.wave_len = h->wave_len;
     p.step_base = h->slots + parity;
     p.step_next = h->slots + (1 - parity);
     p.step_off = kind == 2 ? -1 : 0;
-    for (int b = 0; b < LBM_MAX_BC; ++b) p.bc[b] = h->bc[b];
+    p.bct = h->bct;
     p.nbc = h->nbc;
+    p.sp_bc = h->g.sp_bc;
+    p.sp_flux = h->sp_flux;
     p.flags = h->flags;
     p.act_idx = h->g.act_idx;
     p.partials = h->partials;
@@ -450,7 +491,7 @@ void build_segments(int Q, const uint8_t* mask, int nx, int ny, int nz, int64_t&
 }
 
 const uint32_t kCkptMagic = 0x4c424d43;  // "CMBL"
-const uint32_t kCkptVersion = 2;  // 2: boundary list ordered next-to-wall first
+const uint32_t kCkptVersion = 3;  // 2: boundary list next-to-wall first; 3: every inlet waveform
 
 }  // namespace
 
@@ -545,15 +586,18 @@ lbm_status lbm_create(const lbm_desc* desc, lbm_handle** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->slots, 2 * sizeof(int64_t));
     if (e == cudaSuccess) e = cudaMalloc(&h->flags, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMalloc(&h->amp, sizeof(double));
-    if (e == cudaSuccess) e = cudaMemset(h->amp, 0, sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->wave_off, sizeof(int64_t) * LBM_MAX_WAVES);
+    if (e == cudaSuccess) e = cudaMalloc(&h->wave_len, sizeof(int64_t) * LBM_MAX_WAVES);
     if (e != cudaSuccess) {
         int rc = fail(nullptr, LBM_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
         lbm_destroy(h);
         return rc;
     }
-    h->namp = 1;
-    h->amp_host.assign(1, 0.0);
+    h->waves.assign(1, std::vector<double>(1, 0.0));
+    if (upload_waves(h) != LBM_OK) {
+        lbm_destroy(h);
+        return LBM_ERR_CUDA;
+    }
     *out = h;
     return LBM_OK;
 }
@@ -566,6 +610,8 @@ lbm_status lbm_destroy(lbm_handle* h) {
     if (h->slots) cudaFree(h->slots);
     if (h->flags) cudaFree(h->flags);
     if (h->amp) cudaFree(h->amp);
+    if (h->wave_off) cudaFree(h->wave_off);
+    if (h->wave_len) cudaFree(h->wave_len);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
     return LBM_OK;
@@ -575,7 +621,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     REQUIRE(h, mask && dims, LBM_ERR_ARG, "null mask or dims");
     REQUIRE(h, dims[0] > 0 && dims[1] > 0 && dims[2] > 0, LBM_ERR_ARG, "empty lattice");
-    REQUIRE(h, nbc >= 0 && nbc <= LBM_MAX_BC && (nbc == 0 || bc), LBM_ERR_ARG, "0..8 boundary conditions");
+    REQUIRE(h, nbc >= 0 && nbc <= LBM_MAX_BC && (nbc == 0 || bc), LBM_ERR_ARG, "0..256 boundary conditions");
     const int64_t npts = (int64_t)dims[0] * dims[1] * dims[2];
     REQUIRE(h, npts < (int64_t)1 << 31, LBM_ERR_ARG, "lattice too large (more than 2^31 points)");
     for (int b = 0; b < nbc; ++b) {
@@ -583,6 +629,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
         REQUIRE(h, bc[b].face >= 0 && bc[b].face <= 5, LBM_ERR_ARG, "face must be 0..5");
         REQUIRE(h, bc[b].kind != LBM_BC_PRESSURE || bc[b].value > 0, LBM_ERR_ARG, "pressure bc needs density > 0");
         REQUIRE(h, bc[b].profile == 0 || bc[b].R > 0, LBM_ERR_ARG, "profile radius must be > 0");
+        REQUIRE(h, bc[b].wave >= 0 && bc[b].wave < LBM_MAX_WAVES, LBM_ERR_ARG, "waveform index out of range");
     }
     CK(h, cudaSetDevice(h->d.device));
     CK(h, cudaStreamSynchronize(h->st));
@@ -614,18 +661,20 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, "set_geometry: " + (err.empty() ? cudaGetErrorString(e) : err));
     REQUIRE(h, h->g.nact < (int64_t)1 << 31, LBM_ERR_ARG, "too many active nodes");
     h->nbc = nbc;
-    for (int b = 0; b < LBM_MAX_BC; ++b) {
-        h->bc[b] = BCDev{};
-        if (b < nbc) {
-            h->bc[b].kind = bc[b].kind;
-            h->bc[b].face = bc[b].face;
-            h->bc[b].value = bc[b].value;
-            h->bc[b].profile = bc[b].profile;
-            h->bc[b].c1 = bc[b].c1;
-            h->bc[b].c2 = bc[b].c2;
-            h->bc[b].R = bc[b].R;
-        }
+    h->bc.assign(nbc, BCDev{});
+    for (int b = 0; b < nbc; ++b) {
+        h->bc[b].kind = bc[b].kind;
+        h->bc[b].face = bc[b].face;
+        h->bc[b].value = bc[b].value;
+        h->bc[b].profile = bc[b].profile;
+        h->bc[b].c1 = bc[b].c1;
+        h->bc[b].c2 = bc[b].c2;
+        h->bc[b].R = bc[b].R;
+        h->bc[b].wave = bc[b].wave;
     }
+    CK(h, dalloc(h, &h->bct, sizeof(BCDev) * (nbc + 1)));
+    if (nbc) CK(h, cudaMemcpyAsync(h->bct, h->bc.data(), sizeof(BCDev) * nbc, cudaMemcpyHostToDevice, h->st));
+    CK(h, dalloc(h, &h->sp_flux, sizeof(double) * (h->g.nsp + 1)));
     const int Q = h->d.Q;
     const size_t es = elem_size(h->d.precision), rs = real_size(h->d.precision);
     CK(h, dalloc(h, &h->buf[0], es * Q * h->stride));
@@ -653,7 +702,12 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     h->has_geo = true;
     // counts
     std::vector<uint8_t> spc(h->g.nsp);
-    if (h->g.nsp) CK(h, cudaMemcpyAsync(spc.data(), h->g.sp_cls, h->g.nsp, cudaMemcpyDeviceToHost, h->st));
+    h->sp_bc.assign(h->g.nsp, -1);
+    if (h->g.nsp) {
+        CK(h, cudaMemcpyAsync(spc.data(), h->g.sp_cls, h->g.nsp, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaMemcpyAsync(h->sp_bc.data(), h->g.sp_bc, sizeof(int32_t) * h->g.nsp, cudaMemcpyDeviceToHost,
+                              h->st));
+    }
     CK(h, cudaStreamSynchronize(h->st));
     lbm_counts c{};
     c.points = h->npts;
@@ -662,9 +716,10 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     c.special = h->g.nsp;
     c.segments = h->nseg;
     int64_t bnd = 0;
-    for (uint8_t v : spc) {
+    for (int64_t e = 0; e < h->g.nsp; ++e) {
+        const uint8_t v = spc[e];
         if (v == CLS_WALL) c.wall++;
-        else if (v >= CLS_BC0 && v - CLS_BC0 < LBM_MAX_BC) c.bc[v - CLS_BC0]++;
+        else if (v >= CLS_BC0 && h->sp_bc[e] >= 0 && h->sp_bc[e] < LBM_MAX_BC) c.bc[h->sp_bc[e]]++;
         if (v >= CLS_WALL) bnd++;
     }
     c.fluid = h->g.nact - bnd;
@@ -698,22 +753,76 @@ lbm_status lbm_set_normals_from_surface(lbm_handle* h, const double* tri12, int6
     return LBM_OK;
 }
 
+lbm_status lbm_set_normals_from_surface_box(lbm_handle* h, const double* tri12, int64_t ntri, const double lo[3],
+                                            const double hi[3]) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, ntri >= 0 && (ntri == 0 || tri12) && lo && hi, LBM_ERR_ARG, "null triangles or box");
+    CK(h, cudaSetDevice(h->d.device));
+    const int64_t nn = h->g.nnw;
+    if (nn == 0) return LBM_OK;
+    // next-to-wall points inside the box
+    std::vector<int64_t> pt(nn), sel_idx, sel_pt;
+    CK(h, cudaMemcpyAsync(pt.data(), h->g.nw_pt, sizeof(int64_t) * nn, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    const int64_t nxy = (int64_t)h->nx * h->ny;
+    for (int64_t p = 0; p < nn; ++p) {
+        const int64_t n = pt[p];
+        const int64_t idx[3] = {n % h->nx, (n / h->nx) % h->ny, n / nxy};
+        bool in = true;
+        for (int a = 0; a < 3; ++a) {
+            const double x = h->d.origin[a] + (double)idx[a] * h->d.spacing;
+            in = in && lo[a] <= x && x < hi[a];
+        }
+        if (in) {
+            sel_idx.push_back(p);
+            sel_pt.push_back(n);
+        }
+    }
+    const int64_t m = (int64_t)sel_pt.size();
+    if (m == 0) return LBM_OK;
+    double* d_tri = nullptr;
+    int64_t* d_pt = nullptr;
+    double* d_out = nullptr;
+    cudaError_t e = cudaMalloc(&d_tri, sizeof(double) * 12 * (ntri > 0 ? ntri : 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_pt, sizeof(int64_t) * m);
+    if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(double) * 3 * m);
+    if (e == cudaSuccess && ntri > 0)
+        e = cudaMemcpyAsync(d_tri, tri12, sizeof(double) * 12 * ntri, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_pt, sel_pt.data(), sizeof(int64_t) * m, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = surface_normals(d_tri, ntri, d_pt, m, h->nx, h->ny, h->d.origin, h->d.spacing, d_out, h->st);
+    std::vector<double> part(3 * m), nd(3 * nn);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), d_out, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nd.data(), h->nw_n, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    std::vector<float> nf(3 * nn);
+    if (e == cudaSuccess) {
+        for (int64_t k = 0; k < m; ++k)
+            for (int a = 0; a < 3; ++a) nd[a * nn + sel_idx[k]] = part[a * m + k];
+        for (int64_t k = 0; k < 3 * nn; ++k) nf[k] = (float)nd[k];
+        e = cudaMemcpyAsync(h->nw_n, nd.data(), sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, h->st);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->nw_nf, nf.data(), sizeof(float) * 3 * nn, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(d_tri);
+    cudaFree(d_pt);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("normals: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
 lbm_status lbm_set_inlet_table(lbm_handle* h, const double* amp, int64_t n) {
+    return lbm_set_waveform(h, 0, amp, n);
+}
+
+lbm_status lbm_set_waveform(lbm_handle* h, int wave, const double* amp, int64_t n) {
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     REQUIRE(h, amp && n > 0, LBM_ERR_ARG, "empty amplitude table");
+    REQUIRE(h, wave >= 0 && wave < LBM_MAX_WAVES, LBM_ERR_ARG, "waveform index out of range");
     CK(h, cudaSetDevice(h->d.device));
-    CK(h, cudaStreamSynchronize(h->st));
-    if (n != h->namp) {
-        drop_graph(h);  // the table pointer is baked into captured launches
-        cudaFree(h->amp);
-        h->amp = nullptr;
-        CK(h, cudaMalloc(&h->amp, sizeof(double) * n));
-    }
-    CK(h, cudaMemcpyAsync(h->amp, amp, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
-    CK(h, cudaStreamSynchronize(h->st));
-    h->namp = n;
-    h->amp_host.assign(amp, amp + n);
-    return LBM_OK;
+    if ((int)h->waves.size() <= wave) h->waves.resize(wave + 1);
+    h->waves[wave].assign(amp, amp + n);
+    return upload_waves(h);
 }
 
 lbm_status lbm_init_equilibrium(lbm_handle* h) {
@@ -964,8 +1073,16 @@ lbm_status lbm_get_conservation(lbm_handle* h, double* mass, double* mom3, doubl
     CK(h, cudaStreamSynchronize(h->st));
     if (mass) *mass = (double)h->g.nact + s[0];  // the kernel sums rho - 1
     if (mom3) { mom3[0] = s[1]; mom3[1] = s[2]; mom3[2] = s[3]; }
-    if (flux)
-        for (int b = 0; b < h->nbc; ++b) flux[b] = s[4 + b];
+    if (flux) {
+        // per-entry flux of the boundary-condition nodes, summed per rule in list order
+        std::vector<double> fx(h->g.nsp);
+        if (h->g.nsp) CK(h, cudaMemcpyAsync(fx.data(), h->sp_flux, sizeof(double) * h->g.nsp,
+                                            cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaStreamSynchronize(h->st));
+        for (int b = 0; b < h->nbc; ++b) flux[b] = 0.0;
+        for (int64_t e = 0; e < h->g.nsp; ++e)
+            if (h->sp_bc[e] >= 0 && h->sp_bc[e] < h->nbc) flux[h->sp_bc[e]] += fx[e];
+    }
     return LBM_OK;
 }
 
@@ -982,14 +1099,18 @@ lbm_status lbm_save(lbm_handle* h, const char* path) {
     REQUIRE(h, fp, LBM_ERR_IO, std::string("cannot write ") + path);
     const uint32_t head[2] = {kCkptMagic, kCkptVersion};
     const int32_t cfg[6] = {h->d.Q, h->d.precision, h->d.mode, h->nx, h->ny, h->nz};
-    const int64_t sz[4] = {na, nn, h->steps, h->namp};
+    const int64_t sz[4] = {na, nn, h->steps, (int64_t)h->waves.size()};
+    std::vector<int64_t> wl;
+    for (const auto& w : h->waves) wl.push_back((int64_t)w.size());
     bool ok = std::fwrite(head, sizeof(head), 1, fp) == 1 && std::fwrite(cfg, sizeof(cfg), 1, fp) == 1 &&
               std::fwrite(sz, sizeof(sz), 1, fp) == 1 &&
               std::fwrite(f.data(), sizeof(double), f.size(), fp) == f.size() &&
               std::fwrite(acc.data(), sizeof(double), acc.size(), fp) == acc.size() &&
               std::fwrite(accm.data(), sizeof(double), accm.size(), fp) == accm.size() &&
               std::fwrite(wss.data(), sizeof(double), wss.size(), fp) == wss.size() &&
-              std::fwrite(h->amp_host.data(), sizeof(double), h->amp_host.size(), fp) == h->amp_host.size();
+              std::fwrite(wl.data(), sizeof(int64_t), wl.size(), fp) == wl.size();
+    for (const auto& w : h->waves)
+        ok = ok && (w.empty() || std::fwrite(w.data(), sizeof(double), w.size(), fp) == w.size());
     ok = (std::fclose(fp) == 0) && ok;
     REQUIRE(h, ok, LBM_ERR_IO, std::string("short write to ") + path);
     return LBM_OK;
@@ -1010,20 +1131,31 @@ lbm_status lbm_load(lbm_handle* h, const char* path) {
         return fail(h, LBM_ERR_IO, "not a checkpoint of this version");
     }
     if (cfg[0] != h->d.Q || cfg[3] != h->nx || cfg[4] != h->ny || cfg[5] != h->nz || sz[0] != h->g.nact ||
-        sz[1] != h->g.nnw || sz[3] < 1) {
+        sz[1] != h->g.nnw || sz[3] < 1 || sz[3] > LBM_MAX_WAVES) {
         std::fclose(fp);
         return fail(h, LBM_ERR_ARG, "checkpoint lattice does not match this handle");
     }
     const int64_t na = sz[0], nn = sz[1];
-    std::vector<double> f(na * h->d.Q), acc(3 * nn), accm(nn), wss(nn), amp(sz[3]);
-    ok = std::fread(f.data(), sizeof(double), f.size(), fp) == f.size() &&
+    std::vector<double> f(na * h->d.Q), acc(3 * nn), accm(nn), wss(nn);
+    std::vector<int64_t> wl(sz[3] <= LBM_MAX_WAVES ? sz[3] : 0);
+    ok = sz[3] <= LBM_MAX_WAVES && std::fread(f.data(), sizeof(double), f.size(), fp) == f.size() &&
          std::fread(acc.data(), sizeof(double), acc.size(), fp) == acc.size() &&
          std::fread(accm.data(), sizeof(double), accm.size(), fp) == accm.size() &&
          std::fread(wss.data(), sizeof(double), wss.size(), fp) == wss.size() &&
-         std::fread(amp.data(), sizeof(double), amp.size(), fp) == amp.size();
+         std::fread(wl.data(), sizeof(int64_t), wl.size(), fp) == wl.size();
+    std::vector<std::vector<double>> waves(wl.size());
+    for (size_t w = 0; ok && w < wl.size(); ++w) {
+        ok = wl[w] >= 0 && wl[w] < ((int64_t)1 << 40);
+        if (ok) {
+            waves[w].resize(wl[w]);
+            ok = waves[w].empty() || std::fread(waves[w].data(), sizeof(double), wl[w], fp) == (size_t)wl[w];
+        }
+    }
     std::fclose(fp);
     REQUIRE(h, ok, LBM_ERR_IO, std::string("truncated checkpoint ") + path);
-    int rc = lbm_set_inlet_table(h, amp.data(), (int64_t)amp.size());
+    h->waves = waves;
+    if (h->waves.empty()) h->waves.assign(1, std::vector<double>(1, 0.0));
+    int rc = upload_waves(h);
     if (rc) return rc;
     rc = write_accumulators(h, wss, acc, accm);
     if (rc) return rc;

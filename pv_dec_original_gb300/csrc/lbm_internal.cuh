@@ -21,6 +21,7 @@ struct BCDev {
     double value;
     int profile;
     double c1, c2, R;
+    int wave;  // inlet waveform of a velocity rule
 };
 
 // Everything one stream-collide launch needs (passed by value).
@@ -39,6 +40,8 @@ struct StepParams {
     const uint8_t* sp_cls;
     const int32_t* sp_nw;     // next-to-wall index or -1
     const double* sp_prof;    // inlet profile factor
+    const int32_t* sp_bc;     // boundary-condition rule of a boundary-list entry (-1: none)
+    double* sp_flux;          // read-out: momentum along the rule's face axis, per entry
     void* stale;              // parity: previous post-boundary f, [q][nsp] in the arithmetic type
     // next-to-wall accumulators
     int64_t nnw;
@@ -64,23 +67,25 @@ struct StepParams {
     float wss_C_f;             // C in FP32 (parity stress)
     float wss_phys_f;          // -(1 - 1/(2 tau)) C in FP32 (physics stress)
     double wss_phys;           // the same in FP64
-    // inlet amplitude table: step index = *step_base + step_off
+    // inlet waveforms, concatenated: waveform w holds wave_len[w] entries
+    // from amp + wave_off[w]; step index = *step_base + step_off
     const double* amp;
-    int64_t namp;
+    const int64_t* wave_off;
+    const int64_t* wave_len;
     const int64_t* step_base;  // step counter slot read by this launch
     int64_t* step_next;        // the other slot: written with *step_base + 1
     int step_off;
     int direct;                // read-out of the initial state: no pull, no boundary rules
-    BCDev bc[LBM_MAX_BC];
+    const BCDev* bct;  // boundary-condition rules (device table)
     int nbc;
     unsigned* flags;
     // readout (materialize) outputs
     double* out_f;            // [a*Q + q] FP64, or null
     const int32_t* act_idx;   // per point active index (readout only)
-    double* partials;         // per block: mass, mom3, flux[LBM_MAX_BC]
+    double* partials;         // per block: mass - nact, mom3
 };
 
-constexpr int kPartialStride = 4 + LBM_MAX_BC;
+constexpr int kPartialStride = 4;
 constexpr int kStepThreads = 256;
 
 // Launchers (one per translation unit family).  kind: 0 step, 1 prologue

@@ -61,7 +61,9 @@ struct Rules {
 // Plane rules match a lattice index; region rules match coordinates the way
 // classifyBoundaryPoints does (ComplexGeometry.cpp:1380-1407; the reference
 // compares in long double, here in FP64).  First match wins.
-__global__ void k_classify(uint8_t* __restrict__ cls, int nx, int ny, int64_t npts, Rules R) {
+// The class byte records 3 + r (capped at 127 for r >= 124); bcidx holds r.
+__global__ void k_classify(uint8_t* __restrict__ cls, int16_t* __restrict__ bcidx, int nx, int ny, int64_t npts,
+                           Rules R) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= npts || cls[n] != CLS_WALL) return;
     const int idx[3] = {(int)(n % nx), (int)((n / nx) % ny), (int)(n / ((int64_t)nx * ny))};
@@ -76,7 +78,11 @@ __global__ void k_classify(uint8_t* __restrict__ cls, int nx, int ny, int64_t np
             hit = fabs(x[a] - R.coord[r]) <= R.tol[r] && R.lo[r][0] < x[t1] && x[t1] < R.hi[r][0] &&
                   R.lo[r][1] < x[t2] && x[t2] < R.hi[r][1];
         }
-        if (hit) { cls[n] = (uint8_t)(CLS_BC0 + r); return; }
+        if (hit) {
+            cls[n] = (uint8_t)(CLS_BC0 + (r < 124 ? r : 124));
+            bcidx[n] = (int16_t)r;
+            return;
+        }
     }
 }
 
@@ -134,7 +140,8 @@ __global__ void k_scatter(const int64_t* __restrict__ flag, const int64_t* __res
 template <int Q>
 __global__ void k_special_info(const int64_t* __restrict__ sp_pt, int64_t nsp, const uint8_t* __restrict__ cls,
                                const int64_t* __restrict__ nwpos, int nx, int ny, int nz,
-                               uint32_t* __restrict__ miss, uint8_t* __restrict__ spc, int32_t* __restrict__ spnw,
+                               const int16_t* __restrict__ bcidx, uint32_t* __restrict__ miss,
+                               uint8_t* __restrict__ spc, int32_t* __restrict__ spnw, int32_t* __restrict__ spbc,
                                double* __restrict__ prof, ProfileSpec ps) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsp) return;
@@ -152,9 +159,11 @@ __global__ void k_special_info(const int64_t* __restrict__ sp_pt, int64_t nsp, c
     const uint8_t c = cls[n];
     spc[s] = c & CLS_MASK;
     spnw[s] = (c & CLS_NW_BIT) ? (int32_t)nwpos[n] : -1;
+    const bool is_bc = (c & CLS_MASK) >= CLS_BC0;
+    const int b = is_bc ? (int)bcidx[n] : -1;
+    spbc[s] = b;
     double p = 0.0;
-    const int b = (c & CLS_MASK) - CLS_BC0;
-    if ((c & CLS_MASK) >= CLS_BC0 && b < ps.n) {
+    if (is_bc && b < ps.n) {
         if (ps.profile[b] == 0) {
             p = 1.0;
         } else {
@@ -207,7 +216,7 @@ __global__ void k_active_index(const int64_t* __restrict__ flag, const int64_t* 
     const uint8_t c = cls[n];
     const bool sp = spflag[n] != 0;
     act_word[a] = (uint64_t)(uint32_t)seg_of_act[a] | ((uint64_t)sp << 31) | (miss << 32) |
-                  ((uint64_t)(c & CLS_MASK & 0xf) << 59) |
+                  ((uint64_t)((c & CLS_MASK) < CLS_BC0 ? (c & CLS_MASK) : CLS_BC0) << 59) |
                   ((uint64_t)((c & CLS_NW_BIT) ? 1 : 0) << 63);
     sp_of_act[a] = sp ? (int32_t)sppos[n] : -1;
 }
@@ -327,7 +336,8 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
         for (int t = 0; t < 2; ++t) { R.lo[b][t] = bc[b].lo[t]; R.hi[b][t] = bc[b].hi[t]; }
         out.plane[b] = R.plane[b];
     }
-    k_classify<<<blocks(npts), 256, 0, st>>>(out.cls, nx, ny, npts, R);
+    SETUP_CHECK(cudaMallocAsync(&out.bcidx, sizeof(int16_t) * npad, st));
+    k_classify<<<blocks(npts), 256, 0, st>>>(out.cls, out.bcidx, nx, ny, npts, R);
     SETUP_CHECK(cudaGetLastError());
     if (Q == 19) k_next_to_wall<19><<<blocks(npts), 256, 0, st>>>(out.cls, nx, ny, nz);
     else k_next_to_wall<27><<<blocks(npts), 256, 0, st>>>(out.cls, nx, ny, nz);
@@ -354,6 +364,7 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     SETUP_CHECK(cudaMallocAsync(&out.sp_miss, sizeof(uint32_t) * (out.nsp + 1), st));
     SETUP_CHECK(cudaMallocAsync(&out.sp_cls, out.nsp + 1, st));
     SETUP_CHECK(cudaMallocAsync(&out.sp_nw, sizeof(int32_t) * (out.nsp + 1), st));
+    SETUP_CHECK(cudaMallocAsync(&out.sp_bc, sizeof(int32_t) * (out.nsp + 1), st));
     SETUP_CHECK(cudaMallocAsync(&out.sp_prof, sizeof(double) * (out.nsp + 1), st));
     ProfileSpec ps{};
     ps.n = nbc;
@@ -367,10 +378,12 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     if (out.nsp > 0) {
         if (Q == 19)
             k_special_info<19><<<blocks(out.nsp), 256, 0, st>>>(out.sp_pt, out.nsp, out.cls, nwpos, nx, ny, nz,
-                                                               out.sp_miss, out.sp_cls, out.sp_nw, out.sp_prof, ps);
+                                                               out.bcidx, out.sp_miss, out.sp_cls, out.sp_nw,
+                                                               out.sp_bc, out.sp_prof, ps);
         else
             k_special_info<27><<<blocks(out.nsp), 256, 0, st>>>(out.sp_pt, out.nsp, out.cls, nwpos, nx, ny, nz,
-                                                               out.sp_miss, out.sp_cls, out.sp_nw, out.sp_prof, ps);
+                                                               out.bcidx, out.sp_miss, out.sp_cls, out.sp_nw,
+                                                               out.sp_bc, out.sp_prof, ps);
         SETUP_CHECK(cudaGetLastError());
     }
 

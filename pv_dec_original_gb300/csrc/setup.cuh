@@ -23,6 +23,8 @@ struct GeometryLists {
     uint32_t* sp_miss = nullptr;
     uint8_t* sp_cls = nullptr;
     int32_t* sp_nw = nullptr;
+    int32_t* sp_bc = nullptr;    // boundary-condition rule of the entry, or -1
+    int16_t* bcidx = nullptr;    // per point: boundary-condition rule (valid where cls >= CLS_BC0)
     double* sp_prof = nullptr;
     int64_t nnw = 0;
     int64_t* nw_pt = nullptr;

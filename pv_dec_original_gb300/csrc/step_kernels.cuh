@@ -451,7 +451,7 @@ __device__ __forceinline__ bool is_exact_zero(R v, int q) {
 //   bits  0-30  segment id: the pull source of population q is node a + delta[seg][q]
 //   bit   31    boundary-list node (needs the long path)
 //   bits 32-58  missing-link mask: bit q set when x + c_q is solid / outside
-//   bits 59-62  class (1 fluid, 2 wall, 3+b boundary condition b)
+//   bits 59-62  class (1 fluid, 2 wall, 3 boundary condition: its rule is sp_bc of the entry)
 //   bit   63    next-to-wall node (accumulates wall shear stress)
 __device__ __forceinline__ int64_t word_segment(uint64_t w) { return (int64_t)(w & 0x7fffffffull); }
 __device__ __forceinline__ bool word_special(uint64_t w) { return (w >> 31) & 1ull; }
@@ -543,13 +543,15 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
         }
         if (!direct && !parity_readout) {
             if (c >= CLS_BC0) {
+                const BCDev& B = P.bct[__ldg(P.sp_bc + s)];
                 double amp = 0.0;
-                if (P.namp > 0) {
-                    int64_t t = (*P.step_base + P.step_off) % P.namp;
-                    if (t < 0) t += P.namp;
-                    amp = __ldg(P.amp + t);
+                const int64_t len = __ldg(P.wave_len + B.wave);
+                if (len > 0) {
+                    int64_t t = (*P.step_base + P.step_off) % len;
+                    if (t < 0) t += len;
+                    amp = __ldg(P.amp + __ldg(P.wave_off + B.wave) + t);
                 }
-                apply_bc<Q, R, OFF>(g, P.bc[c - CLS_BC0], amp, __ldg(P.sp_prof + s));
+                apply_bc<Q, R, OFF>(g, B, amp, __ldg(P.sp_prof + s));
             } else if (MODE == MODE_PARITY && c == CLS_WALL) {
                 // ApplyWallBc: in place, direction order (Simulation.cpp:846-861)
 #pragma unroll
@@ -563,7 +565,7 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
                 moments<Q, R, OFF>(g, r, ux, uy, uz);
                 const double rho = OFF ? 1.0 + (double)r : (double)r;
                 const double j[3] = {rho * ux, rho * uy, rho * uz};
-                part[4 + (c - CLS_BC0)] = j[bc_axis(P.bc[c - CLS_BC0])];
+                P.sp_flux[s] = j[bc_axis(P.bct[__ldg(P.sp_bc + s)])];
             }
         }
         if (s < P.nnw) nw = (int)s;

@@ -1,0 +1,69 @@
+"""C1 analytic pin (physics mode): steady Poiseuille flow in the capped
+cylinder (r=10 lu, L=100 lu) with a parabolic Zou-He velocity inlet
+(u_max=0.05), a density outlet (rho=1), half-way bounce-back walls and
+tau=0.8, 5000 steps in FP64.
+
+Analytic solution (nu = (tau - 1/2)/3, mu = rho nu):
+  u_z(r) = u_max (1 - r^2/R^2),   d rho/dz = -3 * 8 nu (u_max/2) / R^2,
+  shear stress magnitude tau(r) = 2 mu u_max r / R^2.
+A staircase wall with half-way bounce-back places the wall between the
+last fluid node and the first solid one, so the comparison allows a few
+per cent in the profile and the pressure gradient and more in the stress,
+which is sampled on next-to-wall nodes one spacing inside the wall."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gpu_c1_poiseuille(gpu_lib):
+    capi = gpu_lib
+    from pv_dec_original_gb300 import geometry as G
+    surf = G.config_c1_cylinder()
+    tri = surf.tri12()
+    mask, desc = capi.voxelize(tri, 1.0)
+    bb = np.array(desc.bbox[:])
+    org = (bb[0], bb[2], bb[4])
+    fl = np.argwhere(mask > 0)  # (k, j, i) in the solver's node order
+    kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
+    cx, cy = surf.meta["center"]
+    R, umax, tau = 10.0, 0.05, 0.8
+    nu = (tau - 0.5) / 3.0
+    s = capi.Solver(19, capi.LBM_F64, capi.LBM_PHYSICS, tau, 1.0, org, 1.0, 1.0)
+    s.set_geometry(mask, [capi.bc_spec(capi.LBM_BC_VELOCITY, "z-", kin, umax, 1, cx, cy, R),
+                          capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)])
+    s.set_normals(tri)
+    s.set_inlet_table([1.0])
+    s.step(5000)
+    rho, u = s.macro()
+    x = fl[:, 2] + org[0] - cx  # surface and profile centre are in physical coordinates
+    y = fl[:, 1] + org[1] - cy
+    r2 = x * x + y * y
+    # velocity profile over the middle third of the tube
+    kmid = (fl[:, 0] > kin + 33) & (fl[:, 0] < kout - 33)
+    ua = umax * np.clip(1.0 - r2[kmid] / R ** 2, 0.0, None)
+    err = np.linalg.norm(u[kmid, 2] - ua) / np.linalg.norm(ua)
+    assert err < 0.05, err
+    assert np.max(np.abs(u[kmid, :2])) < 0.01 * umax
+    # axial density gradient (cross-section means) vs Hagen-Poiseuille,
+    # d rho/dz = -3 * 8 nu Q / (pi R_eff^4), with the measured flux Q and the
+    # staircase section's equivalent radius (pi R_eff^2 = fluid nodes per section)
+    ks = np.unique(fl[kmid, 0])
+    means = np.array([rho[kmid][fl[kmid, 0] == k].mean() for k in ks])
+    slope = np.polyfit(ks, means, 1)[0]
+    kc = ks[len(ks) // 2]
+    sec = fl[:, 0] == kc
+    Reff = np.sqrt(sec.sum() / np.pi)
+    Qf = (rho[sec] * u[sec, 2]).sum()
+    expect = -3.0 * 8.0 * nu * Qf / (np.pi * Reff ** 4)
+    assert abs(slope / expect - 1.0) < 0.05, (slope, expect, Reff)
+    # shear stress on next-to-wall nodes of the middle third vs 2 mu u_max r / R^2
+    w = s.wss()
+    pk = w["pt"] // (mask.shape[1] * mask.shape[2])
+    pj = (w["pt"] // mask.shape[2]) % mask.shape[1]
+    pi = w["pt"] % mask.shape[2]
+    sel = (pk > kin + 33) & (pk < kout - 33)
+    rn = np.hypot(pi[sel] + org[0] - cx, pj[sel] + org[1] - cy)
+    wa = 2.0 * nu * umax * rn / R ** 2
+    rel = np.abs(w["wss"][sel] / (rho.mean() * wa) - 1.0)
+    assert np.median(rel) < 0.15, np.median(rel)
