@@ -498,10 +498,12 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
     // own opposite population (half-way bounce-back); in parity mode any
     // valid address -- the previous value replaces it below.
     const I ai = (I)a, st = (I)P.stride;
+    // the node's own entry of plane 0; plane q is q * stride further
+    const S* __restrict__ fin_a = fin + ai;
     R g[Q];
     if (direct) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin + (q * st + ai), q);
+        for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin_a + q * st, q);
     } else {
         int32_t dl[DR];
         const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
@@ -513,15 +515,15 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const bool src_missing = (miss >> Lat<Q>::opp(q)) & 1u;
-            I idx;
+            I off;  // from the node's own entry of plane 0
             if (q == Lat<Q>::REST) {
-                idx = q * st + ai;
+                off = q * st;
             } else if (MODE == MODE_PHYSICS) {
-                idx = src_missing ? Lat<Q>::opp(q) * st + ai : q * st + ai + dl[q];
+                off = src_missing ? Lat<Q>::opp(q) * st : q * st + dl[q];
             } else {
-                idx = q * st + (src_missing ? ai : ai + dl[q]);
+                off = q * st + (src_missing ? 0 : dl[q]);
             }
-            g[q] = Store<S>::template load<Q>(fin + idx, q);  // w_opp(q) == w_q: same decode
+            g[q] = Store<S>::template load<Q>(fin_a + off, q);  // w_opp(q) == w_q: same decode
         }
     }
 
@@ -652,8 +654,9 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
             relax_all<Q, R, OFF>(g, r, ux, uy, uz, ux * ux + uy * uy + uz * uz, (R)P.inv_tau);
         }
         if (!(fabsf((float)r) < 1e30f)) atomicOr(P.flags, FLAG_NONFINITE);
+        S* __restrict__ fout_a = fout + ai;
 #pragma unroll
-        for (int q = 0; q < Q; ++q) fout[q * st + ai] = Store<S>::template pack<Q>(g[q], q);
+        for (int q = 0; q < Q; ++q) fout_a[q * st] = Store<S>::template pack<Q>(g[q], q);
     }
 }
 
