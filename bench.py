@@ -278,6 +278,73 @@ def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
             "l2": "not flushed (populations exceed L2)", "launches_total": launches}
 
 
+def warmstart_extra(device, n_train=32, n_test=6, tau=0.55):
+    """Learned warm start (scaled-down C5: 64x32x64 grids instead of
+    128x128x256, 32 training vessels): train on the device, then steps and
+    wall time to residual 1e-6 from rest and from the prediction on held-out
+    vessels (FP64 lattices), prediction errors of the network and of the
+    Poiseuille prior it corrects, and the tensor-core convolution throughput
+    of one forward pass at the full C5 grid."""
+    import torch
+    from pv_dec_original_gb300 import warmstart as WS
+    t0 = time.perf_counter()
+    train_m = WS.vessel_members(n_train, seed=1)
+    test_m = WS.vessel_members(n_test, seed=99)
+    sols = WS.steady_ensemble(train_m, tau=tau, steps=60000, device=device)
+    samples = [WS.make_sample(mask, m, rho, u, tau=tau, device=device) for (mask, rho, u), m in zip(sols, train_m)]
+    data_s = time.perf_counter() - t0
+    net = WS.WarmStartNet(sols[0][0].shape, device=device, seed=0)
+    t0 = time.perf_counter()
+    hist = WS.train(net, samples, iters=2000, lr=2e-3, batch=4)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    rows = []
+    for m in test_m:
+        sc, mask = WS.single_lattice(m, tau=tau, device=device)
+        sc.set_graph_steps(100)
+        t0 = time.perf_counter()
+        nc, _ = WS.steps_to_converge(sc, tol=1e-6, max_steps=150000)
+        tc = time.perf_counter() - t0
+        rc, uc = sc.macro()
+        wc = sc.wss()["wss"]
+        t0 = time.perf_counter()
+        x, prior = WS.features(mask, m["inlet_mean"], m["period"], tau=tau, device=device)
+        rho, u = WS.prediction_to_macro(mask, net.forward(x), m["inlet_mean"], prior)
+        sw, _ = WS.single_lattice(m, tau=tau, device=device)
+        sw.set_graph_steps(100)
+        sw.init_from_macro(rho, u, True)
+        nw, _ = WS.steps_to_converge(sw, tol=1e-6, max_steps=150000)
+        tw = time.perf_counter() - t0
+        _, up = WS.prediction_to_macro(mask, torch.zeros(mask.size * WS.C_OUT), m["inlet_mean"], prior)
+        rows.append({"kind": m["kind"], "cold_steps": nc, "cold_s": tc, "warm_steps": nw, "warm_s": tw,
+                     "err_net": float(np.linalg.norm(u - uc) / np.linalg.norm(uc)),
+                     "err_prior": float(np.linalg.norm(up - uc) / np.linalg.norm(uc)),
+                     "wss_diff": float(np.linalg.norm(sw.wss()["wss"] - wc) / np.linalg.norm(wc))})
+    # convolution throughput at the C5 grid (128x128x256), forward pass
+    big = WS.WarmStartNet((256, 128, 128), device=device, seed=0)
+    xb = torch.zeros(256 * 128 * 128 * WS.C_IN, dtype=torch.bfloat16, device=torch.device("cuda", device))
+    big.forward(xb)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record(big.stream)
+    for _ in range(3):
+        big.forward(xb)
+    ev[1].record(big.stream)
+    torch.cuda.synchronize()
+    fwd_ms = ev[0].elapsed_time(ev[1]) / 3
+    flops = sum(2.0 * big.nvox(mm["lvl_out"]) * mm["co"] * mm["taps"] * mm["ci"] for mm in big.meta.values())
+    cold = sum(r["cold_steps"] for r in rows)
+    warm = sum(r["warm_steps"] for r in rows)
+    return {"grid": list(sols[0][0].shape), "train_vessels": n_train, "test_vessels": n_test, "tau": tau,
+            "data_s": data_s, "train_s": train_s, "train_iters": 2000, "loss_first_last": [hist[0], hist[-1]],
+            "cold_steps_total": cold, "warm_steps_total": warm, "warm_over_cold_steps": warm / cold,
+            "warm_over_cold_time": sum(r["warm_s"] for r in rows) / sum(r["cold_s"] for r in rows),
+            "per_vessel": rows,
+            "conv_forward_c5_grid": {"grid": [256, 128, 128], "ms": fwd_ms, "gflop": flops / 1e9,
+                                     "tflops": flops / (fwd_ms * 1e-3) / 1e12,
+                                     "kernel": "mma.sync m16n8k16 BF16 implicit GEMM, FP32 accumulate"}}
+
+
 def read_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -411,6 +478,8 @@ def run_ours(args):
     # lattice, one launch per step, vs the same members as 64 lattices
     if not args.quick and not args.no_ensemble:
         extra["ensemble_c4"] = ensemble_extra(capi, cr, local, args.Q)
+    if not args.quick and not args.no_warmstart:
+        extra["warmstart_c5"] = warmstart_extra(local)
 
     # end to end through the C ABI: per e2e step, H2D of a 100-step inlet
     # table slice from pinned memory, 100 LBM steps (graph replay), D2H of
@@ -550,6 +619,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the secondary FP16 and ensemble measurements")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurement")
+    ap.add_argument("--no-warmstart", action="store_true", help="skip the learned warm-start measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--variant", type=int, default=None, help="force a launch shape (skips the autotuner)")
     args = ap.parse_args()

@@ -1,0 +1,65 @@
+/* Learned warm start: device kernels of the convolutional encoder-decoder
+ * that predicts an initial rho / u field from a signed-distance field and
+ * inlet parameters, and the signed-distance field itself.  No counterpart in
+ * the reference (it always starts from rest, Node.cpp:30-37); the lattice is
+ * then warm-started through lbm_init_from_macro (lbm_gb300.h).
+ *
+ * All pointers are device pointers; calls are asynchronous on `stream`
+ * (a cudaStream_t, NULL = the default stream) and allocate nothing.
+ * Tensors are channels-last ([z][y][x][c]) BF16 with c a multiple of 16
+ * (16, 32 or 64); weights are BF16 [co][tap][ci] (tap = (tz*k + ty)*k + tx),
+ * FP32 biases [co].  Kernel size 3 (padding 1, stride 1 or 2) or 1. */
+#ifndef LBM_NN_H
+#define LBM_NN_H
+
+#include "lbm_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* y = act(conv(x, w) + bias), act = ReLU if relu != 0; dims_in = {D, H, W}
+ * of x; y has ((D - 1)/stride + 1, ...) voxels and co channels.  y_f32
+ * (optional) receives the same values in FP32. */
+lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const void* w, const float* bias, int co,
+                             int ksize, int stride, int relu, void* y, float* y_f32, void* stream);
+
+/* Gradients of the convolution above (before its activation): dx = dL/dx
+ * (BF16, written; needs w_t, scratch of the weight's size), dw += dL/dw and
+ * db += dL/db (FP32, accumulated); any of dx / dw / db may be NULL. */
+lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const void* w, void* w_t, int co,
+                             int ksize, int stride, const void* dy, void* dx, float* dw, float* db, void* stream);
+
+/* dy *= (y > 0) over n elements (ReLU backward from the stored output). */
+lbm_status lbm_nn_relu_bwd(const void* y, void* dy, int64_t n, void* stream);
+
+/* Nearest-neighbour x2 upsampling of x (dims_in, c channels) into y; with
+ * adjoint != 0, x is the gradient of the fine tensor and y receives the
+ * gradient of the coarse one (dims_in). */
+lbm_status lbm_nn_upsample2(const void* x, const int dims_in[3], int c, void* y, int adjoint, void* stream);
+
+/* out = a + b over n BF16 elements. */
+lbm_status lbm_nn_add(const void* a, const void* b, void* out, int64_t n, void* stream);
+
+/* Masked squared error: for voxels with mask != 0 and channels < nc,
+ * *loss += sum (pred - target)^2 * inv_norm; dpred = 2 (pred - target) *
+ * inv_norm (BF16, zero elsewhere).  pred is [nvox][c] FP32, target
+ * [nvox][nc] FP32. */
+lbm_status lbm_nn_mse(const float* pred, const float* target, const uint8_t* mask, int64_t nvox, int c, int nc,
+                      float inv_norm, void* dpred, float* loss, void* stream);
+
+/* One Adam step (bias-corrected, step >= 1) on FP32 master weights w; the
+ * BF16 copy w_bf16 (optional) follows. */
+lbm_status lbm_nn_adam(float* w, void* w_bf16, const float* grad, float* m, float* v, int64_t n, float lr,
+                       float beta1, float beta2, float eps, int64_t step, void* stream);
+
+/* Signed distance (lattice spacings, > 0 in fluid) of every voxel of a
+ * D x H x W mask ([z][y][x], nonzero = fluid) to the fluid boundary, by
+ * jump flooding; scratch holds 2 * D * H * W int32. */
+lbm_status lbm_sdf_from_mask(const uint8_t* mask, const int dims[3], float* sdf, void* scratch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_NN_H */

@@ -35,6 +35,7 @@ UNITS = [
     ("step_fast.cu", True),
     ("capi.cu", False),
     ("noalloc.cu", False),
+    ("nn.cu", True),
 ]
 HOST_UNITS = ["host/LatticeModel.cpp", "host/GeometryReader.cpp", "host/ComplexGeometry.cpp",
               "host/Subdomain.cpp", "host/Simulation.cpp", "host/Boundary.cpp", "host/ConfigReader.cpp",
@@ -55,6 +56,7 @@ def _deps(src: str):
         if h.endswith((".cuh", ".h")):
             d.append(os.path.join(CSRC, h))
     d.append(os.path.join(HERE, "..", "include", "lbm_gb300.h"))
+    d.append(os.path.join(HERE, "..", "include", "lbm_nn.h"))
     hd = os.path.join(CSRC, "host")
     if os.path.isdir(hd):
         d += [os.path.join(hd, h) for h in os.listdir(hd) if h.endswith(".h")]

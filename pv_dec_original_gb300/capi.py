@@ -65,6 +65,8 @@ EXPORTS = [
     "lbm_set_distributions", "lbm_get_macro", "lbm_get_wss", "lbm_get_conservation", "lbm_save", "lbm_load",
     "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_autotune", "lbm_set_variant",
     "lbm_moment_sums_noalloc",
+    "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
+    "lbm_nn_adam", "lbm_sdf_from_mask",
 ]
 NUM_VARIANTS = 5
 
@@ -122,6 +124,15 @@ def load(build_if_missing: bool = True):
     L.lbm_autotune.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     L.lbm_set_variant.argtypes = [P, C.c_int]
     L.lbm_moment_sums_noalloc.argtypes = [P, C.c_int64, C.c_int, P, P]
+    I3 = C.POINTER(C.c_int)
+    L.lbm_nn_conv3d_fwd.argtypes = [P, I3, C.c_int, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P]
+    L.lbm_nn_conv3d_bwd.argtypes = [P, I3, C.c_int, P, P, C.c_int, C.c_int, C.c_int, P, P, P, P, P]
+    L.lbm_nn_relu_bwd.argtypes = [P, P, C.c_int64, P]
+    L.lbm_nn_upsample2.argtypes = [P, I3, C.c_int, P, C.c_int, P]
+    L.lbm_nn_add.argtypes = [P, P, P, C.c_int64, P]
+    L.lbm_nn_mse.argtypes = [P, P, P, C.c_int64, C.c_int, C.c_int, C.c_float, P, P, P]
+    L.lbm_nn_adam.argtypes = [P, P, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int64, P]
+    L.lbm_sdf_from_mask.argtypes = [P, I3, P, P, P]
     _lib = L
     return L
 

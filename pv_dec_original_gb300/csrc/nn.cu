@@ -1,0 +1,533 @@
+// Kernels of the learned warm start: a small 3D convolutional
+// encoder-decoder that maps a signed-distance field plus inlet parameters to
+// an initial rho / u field.  The reference has no counterpart (it always
+// starts from rest, Node.cpp:30-37).
+//
+// Activations are BF16, channels-last (voxel-major, channel counts padded to
+// multiples of 16); weights are BF16 [co][tap][ci] with an FP32 master copy
+// for Adam; every product accumulates in FP32 on the tensor cores
+// (mma.sync m16n8k16 BF16).  A convolution is an implicit GEMM:
+//   forward      rows = output voxels, cols = output channels, K = taps x ci
+//   input grad   rows = input voxels,  cols = input channels,  K = taps x co
+//                (the same kernel with the transposed weights [ci][tap][co])
+//   weight grad  rows = output channels, cols = input channels of one tap,
+//                K = output voxels (split over blocks, FP32 atomics)
+// Kernel size 3 (padding 1, stride 1 or 2) or 1 (stride 1).
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <cstdio>
+
+#include "lbm_internal.cuh"
+#include "lbm_nn.h"
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+struct Conv {
+    int D, H, W;     // input dims
+    int Do, Ho, Wo;  // output dims
+    int ci, co;      // padded channels
+    int ks, stride, pad;
+};
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int kRows = 64;   // GEMM rows per block (4 warps x 16)
+constexpr int kPadK = 24;   // shared row stride in BF16 (16 + 8: no bank conflicts on fragment loads)
+
+// Source voxel of GEMM row r for tap t, or -1.  MODE 0: r is an output
+// voxel, the source an input voxel; MODE 1: r is an input voxel, the source
+// the output voxel whose window covers r at tap t.
+template <int MODE>
+__device__ __forceinline__ int64_t source_voxel(const Conv& g, int64_t r, int t) {
+    const int tz = t / (g.ks * g.ks), ty = (t / g.ks) % g.ks, tx = t % g.ks;
+    if (MODE == 0) {
+        const int ox = (int)(r % g.Wo), oy = (int)((r / g.Wo) % g.Ho), oz = (int)(r / ((int64_t)g.Wo * g.Ho));
+        const int ix = ox * g.stride - g.pad + tx, iy = oy * g.stride - g.pad + ty, iz = oz * g.stride - g.pad + tz;
+        if (ix < 0 || iy < 0 || iz < 0 || ix >= g.W || iy >= g.H || iz >= g.D) return -1;
+        return ((int64_t)iz * g.H + iy) * g.W + ix;
+    } else {
+        const int ix = (int)(r % g.W), iy = (int)((r / g.W) % g.H), iz = (int)(r / ((int64_t)g.W * g.H));
+        const int nx = ix + g.pad - tx, ny = iy + g.pad - ty, nz = iz + g.pad - tz;
+        if (nx < 0 || ny < 0 || nz < 0) return -1;
+        if (nx % g.stride || ny % g.stride || nz % g.stride) return -1;
+        const int ox = nx / g.stride, oy = ny / g.stride, oz = nz / g.stride;
+        if (ox >= g.Wo || oy >= g.Ho || oz >= g.Do) return -1;
+        return ((int64_t)oz * g.Ho + oy) * g.Wo + ox;
+    }
+}
+
+// out[r][n] = act(bias[n] + sum_{t,k} src[source(r,t)][k] * B[n][t][k]).
+// BN = columns (padded channel count of the output, <= 64).
+template <int MODE, int BN>
+__global__ void __launch_bounds__(128) k_conv_gemm(const bf16* __restrict__ src, const bf16* __restrict__ B,
+                                                   const float* __restrict__ bias, bf16* __restrict__ out,
+                                                   float* __restrict__ out_f32, Conv g, int64_t rows, int kc,
+                                                   int relu) {
+    __shared__ __align__(16) bf16 As[kRows][kPadK];
+    __shared__ __align__(16) bf16 Bs[BN][kPadK];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int gq = lane >> 2, tg = lane & 3;
+    const int64_t r0 = (int64_t)blockIdx.x * kRows;
+    const int taps = g.ks * g.ks * g.ks;
+    float acc[BN / 8][4];
+#pragma unroll
+    for (int j = 0; j < BN / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    // this thread's A row and half-row (8 channels)
+    const int arow = tid >> 1, ahalf = tid & 1;
+    const int64_t r = r0 + arow;
+    for (int t = 0; t < taps; ++t) {
+        const int64_t sv = r < rows ? source_voxel<MODE>(g, r, t) : -1;
+        for (int c0 = 0; c0 < kc; c0 += 16) {
+            uint4 av = make_uint4(0, 0, 0, 0);
+            if (sv >= 0) av = *reinterpret_cast<const uint4*>(src + sv * kc + c0 + ahalf * 8);
+            *reinterpret_cast<uint4*>(&As[arow][ahalf * 8]) = av;
+            for (int e = tid; e < BN * 2; e += 128) {
+                const int n = e >> 1, h = e & 1;
+                *reinterpret_cast<uint4*>(&Bs[n][h * 8]) =
+                    *reinterpret_cast<const uint4*>(B + ((int64_t)n * taps + t) * kc + c0 + h * 8);
+            }
+            __syncthreads();
+            uint32_t a[4];
+            const int ar = warp * 16 + gq;
+            a[0] = *reinterpret_cast<const uint32_t*>(&As[ar][tg * 2]);
+            a[1] = *reinterpret_cast<const uint32_t*>(&As[ar + 8][tg * 2]);
+            a[2] = *reinterpret_cast<const uint32_t*>(&As[ar][tg * 2 + 8]);
+            a[3] = *reinterpret_cast<const uint32_t*>(&As[ar + 8][tg * 2 + 8]);
+#pragma unroll
+            for (int j = 0; j < BN / 8; ++j) {
+                const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&Bs[j * 8 + gq][tg * 2]);
+                const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&Bs[j * 8 + gq][tg * 2 + 8]);
+                mma_bf16(acc[j], a, b0, b1);
+            }
+            __syncthreads();
+        }
+    }
+    // epilogue: bias, ReLU, BF16 (and optionally FP32) store
+#pragma unroll
+    for (int j = 0; j < BN / 8; ++j) {
+        const int n = j * 8 + tg * 2;
+        const float b0 = bias ? bias[n] : 0.f, b1 = bias ? bias[n + 1] : 0.f;
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+            const int64_t rr = r0 + warp * 16 + gq + hh * 8;
+            if (rr >= rows) continue;
+            float v0 = acc[j][2 * hh] + b0, v1 = acc[j][2 * hh + 1] + b1;
+            if (relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+            *reinterpret_cast<__nv_bfloat162*>(out + rr * BN + n) = __floats2bfloat162_rn(v0, v1);
+            if (out_f32) { out_f32[rr * BN + n] = v0; out_f32[rr * BN + n + 1] = v1; }
+        }
+    }
+}
+
+// dW[co][t][ci] += sum over output voxels m of dY[m][co] * X[src(m,t)][ci]
+// (FP32 atomics; one block per (tap, chunk of output voxels)).  CO, CI:
+// padded channel counts (CO <= 64 rows in 16-row warp slices).
+template <int CO, int CI>
+__global__ void __launch_bounds__(128) k_conv_wgrad(const bf16* __restrict__ x, const bf16* __restrict__ dy,
+                                                    float* __restrict__ dw, Conv g, int64_t rows, int chunk) {
+    __shared__ __align__(16) bf16 As[CO][kPadK];  // [co][16 voxels]
+    __shared__ __align__(16) bf16 Bs[CI][kPadK];  // [ci][16 voxels]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int gq = lane >> 2, tg = lane & 3;
+    const int t = blockIdx.y;
+    const int taps = g.ks * g.ks * g.ks;
+    const int64_t m_begin = (int64_t)blockIdx.x * chunk;
+    const int64_t m_end = m_begin + chunk < rows ? m_begin + chunk : rows;
+    float acc[CI / 8][4];
+#pragma unroll
+    for (int j = 0; j < CI / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    for (int64_t m0 = m_begin; m0 < m_end; m0 += 16) {
+        // A: 16 voxels x CO channels, transposed into As[co][v]
+        for (int e = tid; e < 16 * (CO / 8); e += 128) {
+            const int v = e / (CO / 8), c8 = e % (CO / 8);
+            const int64_t m = m0 + v;
+            uint4 val = make_uint4(0, 0, 0, 0);
+            if (m < m_end) val = *reinterpret_cast<const uint4*>(dy + m * CO + c8 * 8);
+            const bf16* pv = reinterpret_cast<const bf16*>(&val);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) As[c8 * 8 + q][v] = pv[q];
+        }
+        // B: 16 voxels x CI channels of tap t, transposed into Bs[ci][v]
+        for (int e = tid; e < 16 * (CI / 8); e += 128) {
+            const int v = e / (CI / 8), c8 = e % (CI / 8);
+            const int64_t m = m0 + v;
+            uint4 val = make_uint4(0, 0, 0, 0);
+            if (m < m_end) {
+                const int64_t sv = source_voxel<0>(g, m, t);
+                if (sv >= 0) val = *reinterpret_cast<const uint4*>(x + sv * CI + c8 * 8);
+            }
+            const bf16* pv = reinterpret_cast<const bf16*>(&val);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) Bs[c8 * 8 + q][v] = pv[q];
+        }
+        __syncthreads();
+        if (warp * 16 < CO) {
+            uint32_t a[4];
+            const int ar = warp * 16 + gq;
+            a[0] = *reinterpret_cast<const uint32_t*>(&As[ar][tg * 2]);
+            a[1] = *reinterpret_cast<const uint32_t*>(&As[ar + 8][tg * 2]);
+            a[2] = *reinterpret_cast<const uint32_t*>(&As[ar][tg * 2 + 8]);
+            a[3] = *reinterpret_cast<const uint32_t*>(&As[ar + 8][tg * 2 + 8]);
+#pragma unroll
+            for (int j = 0; j < CI / 8; ++j) {
+                const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&Bs[j * 8 + gq][tg * 2]);
+                const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&Bs[j * 8 + gq][tg * 2 + 8]);
+                mma_bf16(acc[j], a, b0, b1);
+            }
+        }
+        __syncthreads();
+    }
+    if (warp * 16 < CO) {
+#pragma unroll
+        for (int j = 0; j < CI / 8; ++j) {
+            const int n = j * 8 + tg * 2;
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const int co = warp * 16 + gq + hh * 8;
+                float* p = dw + ((int64_t)co * taps + t) * CI + n;
+                atomicAdd(p, acc[j][2 * hh]);
+                atomicAdd(p + 1, acc[j][2 * hh + 1]);
+            }
+        }
+    }
+}
+
+// db[c] += sum_m dy[m][c]
+__global__ void k_bias_grad(const bf16* __restrict__ dy, float* __restrict__ db, int64_t rows, int c) {
+    const int ch = threadIdx.x % c;
+    const int lanes = blockDim.x / c;
+    float s = 0.f;
+    for (int64_t m = (int64_t)blockIdx.x * lanes + threadIdx.x / c; m < rows; m += (int64_t)gridDim.x * lanes)
+        s += __bfloat162float(dy[m * c + ch]);
+    if (threadIdx.x / c < lanes) atomicAdd(db + ch, s);
+}
+
+// W [co][t][ci] -> Wt [ci][t][co]
+__global__ void k_transpose_w(const bf16* __restrict__ w, bf16* __restrict__ wt, int co, int taps, int ci) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)co * taps * ci) return;
+    const int c = (int)(e % ci), t = (int)((e / ci) % taps), o = (int)(e / ((int64_t)ci * taps));
+    wt[((int64_t)c * taps + t) * co + o] = w[e];
+}
+
+// dy *= (y > 0): ReLU backward through the stored activation
+__global__ void k_relu_bwd(const bf16* __restrict__ y, bf16* __restrict__ dy, int64_t n) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n && !(__bfloat162float(y[e]) > 0.f)) dy[e] = __float2bfloat16(0.f);
+}
+
+// nearest-neighbour x2 upsampling of [D][H][W][c] and its adjoint
+__global__ void k_up2(const bf16* __restrict__ in, bf16* __restrict__ out, int D, int H, int W, int c) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)8 * D * H * W * c;
+    if (e >= n) return;
+    const int ch = (int)(e % c);
+    const int64_t v = e / c;
+    const int x = (int)(v % (2 * W)), y = (int)((v / (2 * W)) % (2 * H)), z = (int)(v / ((int64_t)4 * W * H));
+    out[e] = in[(((int64_t)(z / 2) * H + y / 2) * W + x / 2) * c + ch];
+}
+
+__global__ void k_up2_bwd(const bf16* __restrict__ dout, bf16* __restrict__ din, int D, int H, int W, int c) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)D * H * W * c;
+    if (e >= n) return;
+    const int ch = (int)(e % c);
+    const int64_t v = e / c;
+    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((int64_t)W * H));
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int zz = 2 * z + (k >> 2), yy = 2 * y + ((k >> 1) & 1), xx = 2 * x + (k & 1);
+        s += __bfloat162float(dout[(((int64_t)zz * 2 * H + yy) * 2 * W + xx) * c + ch]);
+    }
+    din[e] = __float2bfloat16(s);
+}
+
+// out = a + b (BF16, FP32 add)
+__global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf16* __restrict__ out, int64_t n) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) out[e] = __float2bfloat16(__bfloat162float(a[e]) + __bfloat162float(b[e]));
+}
+
+// Masked mean squared error over the first nc channels of pred/target
+// ([voxel][c], FP32): loss += sum / norm; dpred (BF16) = 2 (pred - target) / norm.
+__global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target,
+                      const uint8_t* __restrict__ mask, int64_t nvox, int c, int nc, float inv_norm,
+                      bf16* __restrict__ dpred, float* __restrict__ loss) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (e < nvox * c) {
+        const int ch = (int)(e % c);
+        const int64_t v = e / c;
+        float d = 0.f;
+        if (ch < nc && mask[v]) d = pred[e] - target[v * nc + ch];
+        l = d * d * inv_norm;
+        dpred[e] = __float2bfloat16(2.f * d * inv_norm);
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+
+// Adam on an FP32 master copy; the BF16 weights follow.
+__global__ void k_adam(float* __restrict__ w, bf16* __restrict__ wb, const float* __restrict__ grad,
+                       float* __restrict__ m, float* __restrict__ v, int64_t n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const float gval = grad[e];
+    const float mm = b1 * m[e] + (1.f - b1) * gval;
+    const float vv = b2 * v[e] + (1.f - b2) * gval * gval;
+    m[e] = mm;
+    v[e] = vv;
+    const float wn = w[e] - lr * (mm * c1) / (sqrtf(vv * c2) + eps);
+    w[e] = wn;
+    if (wb) wb[e] = __float2bfloat16(wn);
+}
+
+// --------------------------------------------------------------------------
+// Signed distance field of a mask by jump flooding: seeds are the fluid
+// voxels with a non-fluid 6-neighbour (or on the box face); every voxel
+// keeps the nearest seed found at offsets k = N/2, N/4, ..., 1, then a final
+// pass at offset 1.  sdf > 0 in fluid, < 0 outside, in lattice spacings.
+__global__ void k_jfa_seed(const uint8_t* __restrict__ mask, int D, int H, int W, int32_t* __restrict__ seed) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)D * H * W;
+    if (v >= n) return;
+    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((int64_t)W * H));
+    bool s = false;
+    if (mask[v]) {
+        const int d[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+        for (int k = 0; k < 6 && !s; ++k) {
+            const int xx = x + d[k][0], yy = y + d[k][1], zz = z + d[k][2];
+            s = xx < 0 || yy < 0 || zz < 0 || xx >= W || yy >= H || zz >= D ||
+                !mask[((int64_t)zz * H + yy) * W + xx];
+        }
+    }
+    seed[v] = s ? (int32_t)v : -1;
+}
+
+__global__ void k_jfa_step(const int32_t* __restrict__ in, int32_t* __restrict__ out, int D, int H, int W, int k) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)D * H * W;
+    if (v >= n) return;
+    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((int64_t)W * H));
+    int32_t best = in[v];
+    float bd = 3.4e38f;
+    if (best >= 0) {
+        const float dx = (float)(x - (int)(best % W)), dy = (float)(y - (int)((best / W) % H)),
+                    dz = (float)(z - (int)(best / ((int64_t)W * H)));
+        bd = dx * dx + dy * dy + dz * dz;
+    }
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = x + dx * k, yy = y + dy * k, zz = z + dz * k;
+                if (xx < 0 || yy < 0 || zz < 0 || xx >= W || yy >= H || zz >= D) continue;
+                const int32_t s = in[((int64_t)zz * H + yy) * W + xx];
+                if (s < 0) continue;
+                const float ex = (float)(x - (int)(s % W)), ey = (float)(y - (int)((s / W) % H)),
+                            ez = (float)(z - (int)(s / ((int64_t)W * H)));
+                const float d = ex * ex + ey * ey + ez * ez;
+                if (d < bd) { bd = d; best = s; }
+            }
+    out[v] = best;
+}
+
+__global__ void k_jfa_finish(const int32_t* __restrict__ seed, const uint8_t* __restrict__ mask, int D, int H,
+                             int W, float* __restrict__ sdf) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)D * H * W;
+    if (v >= n) return;
+    const int32_t s = seed[v];
+    float d = 0.f;
+    if (s >= 0) {
+        const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((int64_t)W * H));
+        const float ex = (float)(x - (int)(s % W)), ey = (float)(y - (int)((s / W) % H)),
+                    ez = (float)(z - (int)(s / ((int64_t)W * H)));
+        d = sqrtf(ex * ex + ey * ey + ez * ez);
+    }
+    // a seed voxel is half a spacing inside the wall
+    sdf[v] = mask[v] ? d + 0.5f : -(d + 0.5f);
+}
+
+int report(const char* what, cudaError_t e) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg), "%s: %s", what, e == cudaSuccess ? "invalid argument" : cudaGetErrorString(e));
+    lbm::set_last_global_error(msg);
+    return e == cudaSuccess ? LBM_ERR_ARG : LBM_ERR_CUDA;
+}
+
+bool padded16(int c) { return c > 0 && c % 16 == 0 && c <= 64; }
+
+Conv make_conv(const int dims_in[3], int ci, int co, int ks, int stride) {
+    Conv g{};
+    g.D = dims_in[0]; g.H = dims_in[1]; g.W = dims_in[2];
+    g.ci = ci; g.co = co; g.ks = ks; g.stride = stride; g.pad = ks / 2;
+    g.Do = (g.D + 2 * g.pad - ks) / stride + 1;
+    g.Ho = (g.H + 2 * g.pad - ks) / stride + 1;
+    g.Wo = (g.W + 2 * g.pad - ks) / stride + 1;
+    return g;
+}
+
+template <int MODE>
+cudaError_t launch_gemm(int bn, const bf16* src, const bf16* B, const float* bias, bf16* out, float* out_f32,
+                        const Conv& g, int64_t rows, int kc, int relu, cudaStream_t st) {
+    const unsigned blocks = (unsigned)lbm::ceil_div(rows, kRows);
+    switch (bn) {
+        case 16: k_conv_gemm<MODE, 16><<<blocks, 128, 0, st>>>(src, B, bias, out, out_f32, g, rows, kc, relu); break;
+        case 32: k_conv_gemm<MODE, 32><<<blocks, 128, 0, st>>>(src, B, bias, out, out_f32, g, rows, kc, relu); break;
+        default: k_conv_gemm<MODE, 64><<<blocks, 128, 0, st>>>(src, B, bias, out, out_f32, g, rows, kc, relu); break;
+    }
+    return cudaGetLastError();
+}
+
+template <int CO>
+cudaError_t launch_wgrad_ci(int ci, const bf16* x, const bf16* dy, float* dw, const Conv& g, int64_t rows,
+                            cudaStream_t st) {
+    const int chunk = 2048;
+    const dim3 grid((unsigned)lbm::ceil_div(rows, chunk), (unsigned)(g.ks * g.ks * g.ks));
+    switch (ci) {
+        case 16: k_conv_wgrad<CO, 16><<<grid, 128, 0, st>>>(x, dy, dw, g, rows, chunk); break;
+        case 32: k_conv_wgrad<CO, 32><<<grid, 128, 0, st>>>(x, dy, dw, g, rows, chunk); break;
+        default: k_conv_wgrad<CO, 64><<<grid, 128, 0, st>>>(x, dy, dw, g, rows, chunk); break;
+    }
+    return cudaGetLastError();
+}
+
+unsigned grid1(int64_t n) { return (unsigned)lbm::ceil_div(n > 0 ? n : 1, 256); }
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const void* w, const float* bias, int co,
+                             int ksize, int stride, int relu, void* y, float* y_f32, void* stream) {
+    if (!x || !dims_in || !w || !y || !padded16(ci) || !padded16(co) || (ksize != 1 && ksize != 3) ||
+        (stride != 1 && stride != 2) || (ksize == 1 && stride != 1))
+        return report("lbm_nn_conv3d_fwd", cudaSuccess);
+    const Conv g = make_conv(dims_in, ci, co, ksize, stride);
+    const int64_t rows = (int64_t)g.Do * g.Ho * g.Wo;
+    cudaError_t e = launch_gemm<0>(co, static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias,
+                                   static_cast<bf16*>(y), y_f32, g, rows, ci, relu, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? LBM_OK : report("lbm_nn_conv3d_fwd", e);
+}
+
+lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const void* w, void* w_t, int co,
+                             int ksize, int stride, const void* dy, void* dx, float* dw, float* db, void* stream) {
+    if (!x || !dims_in || !w || !dy || !padded16(ci) || !padded16(co) || (ksize != 1 && ksize != 3) ||
+        (stride != 1 && stride != 2) || (ksize == 1 && stride != 1) || (dx && !w_t))
+        return report("lbm_nn_conv3d_bwd", cudaSuccess);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const Conv g = make_conv(dims_in, ci, co, ksize, stride);
+    const int taps = ksize * ksize * ksize;
+    const int64_t rows_out = (int64_t)g.Do * g.Ho * g.Wo, rows_in = (int64_t)g.D * g.H * g.W;
+    cudaError_t e = cudaSuccess;
+    if (dx) {
+        const int64_t nw = (int64_t)co * taps * ci;
+        k_transpose_w<<<grid1(nw), 256, 0, st>>>(static_cast<const bf16*>(w), static_cast<bf16*>(w_t), co, taps, ci);
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = launch_gemm<1>(ci, static_cast<const bf16*>(dy), static_cast<const bf16*>(w_t), nullptr,
+                               static_cast<bf16*>(dx), nullptr, g, rows_in, co, 0, st);
+    }
+    if (e == cudaSuccess && dw) {
+        const bf16* xb = static_cast<const bf16*>(x);
+        const bf16* dyb = static_cast<const bf16*>(dy);
+        switch (co) {
+            case 16: e = launch_wgrad_ci<16>(ci, xb, dyb, dw, g, rows_out, st); break;
+            case 32: e = launch_wgrad_ci<32>(ci, xb, dyb, dw, g, rows_out, st); break;
+            default: e = launch_wgrad_ci<64>(ci, xb, dyb, dw, g, rows_out, st); break;
+        }
+    }
+    if (e == cudaSuccess && db) {
+        k_bias_grad<<<(unsigned)lbm::ceil_div(rows_out, 256), 256, 0, st>>>(static_cast<const bf16*>(dy), db,
+                                                                            rows_out, co);
+        e = cudaGetLastError();
+    }
+    return e == cudaSuccess ? LBM_OK : report("lbm_nn_conv3d_bwd", e);
+}
+
+lbm_status lbm_nn_relu_bwd(const void* y, void* dy, int64_t n, void* stream) {
+    if (!y || !dy || n < 0) return report("lbm_nn_relu_bwd", cudaSuccess);
+    if (n == 0) return LBM_OK;
+    k_relu_bwd<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(y),
+                                                                        static_cast<bf16*>(dy), n);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_nn_relu_bwd", e);
+}
+
+lbm_status lbm_nn_upsample2(const void* x, const int dims_in[3], int c, void* y, int adjoint, void* stream) {
+    if (!x || !dims_in || !y || c <= 0) return report("lbm_nn_upsample2", cudaSuccess);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t n = (int64_t)dims_in[0] * dims_in[1] * dims_in[2] * c;
+    if (!adjoint)
+        k_up2<<<grid1(8 * n), 256, 0, st>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), dims_in[0],
+                                            dims_in[1], dims_in[2], c);
+    else  // x = gradient of the upsampled tensor, y = gradient of the coarse one (dims_in)
+        k_up2_bwd<<<grid1(n), 256, 0, st>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), dims_in[0],
+                                            dims_in[1], dims_in[2], c);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_nn_upsample2", e);
+}
+
+lbm_status lbm_nn_add(const void* a, const void* b, void* out, int64_t n, void* stream) {
+    if (!a || !b || !out || n < 0) return report("lbm_nn_add", cudaSuccess);
+    if (n == 0) return LBM_OK;
+    k_add<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(a),
+                                                                   static_cast<const bf16*>(b),
+                                                                   static_cast<bf16*>(out), n);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_nn_add", e);
+}
+
+lbm_status lbm_nn_mse(const float* pred, const float* target, const uint8_t* mask, int64_t nvox, int c, int nc,
+                      float inv_norm, void* dpred, float* loss, void* stream) {
+    if (!pred || !target || !mask || !dpred || !loss || nvox < 0 || nc > c) return report("lbm_nn_mse", cudaSuccess);
+    k_mse<<<grid1(nvox * c), 256, 0, static_cast<cudaStream_t>(stream)>>>(pred, target, mask, nvox, c, nc, inv_norm,
+                                                                           static_cast<bf16*>(dpred), loss);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_nn_mse", e);
+}
+
+lbm_status lbm_nn_adam(float* w, void* w_bf16, const float* grad, float* m, float* v, int64_t n, float lr,
+                       float beta1, float beta2, float eps, int64_t step, void* stream) {
+    if (!w || !grad || !m || !v || n < 0 || step < 1) return report("lbm_nn_adam", cudaSuccess);
+    if (n == 0) return LBM_OK;
+    const float c1 = 1.f / (1.f - powf(beta1, (float)step)), c2 = 1.f / (1.f - powf(beta2, (float)step));
+    k_adam<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(w, static_cast<bf16*>(w_bf16), grad, m, v, n,
+                                                                    lr, beta1, beta2, eps, c1, c2);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_nn_adam", e);
+}
+
+lbm_status lbm_sdf_from_mask(const uint8_t* mask, const int dims[3], float* sdf, void* scratch, void* stream) {
+    if (!mask || !dims || !sdf || !scratch || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0)
+        return report("lbm_sdf_from_mask", cudaSuccess);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int D = dims[0], H = dims[1], W = dims[2];
+    const int64_t n = (int64_t)D * H * W;
+    int32_t* a = static_cast<int32_t*>(scratch);
+    int32_t* b = a + n;
+    k_jfa_seed<<<grid1(n), 256, 0, st>>>(mask, D, H, W, a);
+    int k = 1;
+    while (k * 2 < (D > H ? (D > W ? D : W) : (H > W ? H : W))) k *= 2;
+    for (; k >= 1; k /= 2) {
+        k_jfa_step<<<grid1(n), 256, 0, st>>>(a, b, D, H, W, k);
+        int32_t* t = a; a = b; b = t;
+    }
+    k_jfa_step<<<grid1(n), 256, 0, st>>>(a, b, D, H, W, 1);
+    k_jfa_finish<<<grid1(n), 256, 0, st>>>(b, mask, D, H, W, sdf);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_sdf_from_mask", e);
+}
+
+}  // extern "C"

@@ -29,9 +29,11 @@ from . import waveform
 
 
 class Ensemble:
-    def __init__(self, members, Q=19, precision="f16", tau=0.55, gap=1, tawss_div=1.0, device=0, periods=None):
+    def __init__(self, members, Q=19, precision="f16", tau=0.55, gap=1, tawss_div=1.0, device=0, periods=None,
+                 steady=False):
         """members: dicts with "surface" (geometry.Surface), "center" (tube axis
-        x, y in surface coordinates), "radius", "inlet_mean", "period"."""
+        x, y in surface coordinates), "radius", "inlet_mean", "period".
+        steady: a constant inlet at each member's mean instead of its waveform."""
         self.members = members
         parts = []
         for m in members:
@@ -68,14 +70,18 @@ class Ensemble:
             self.tri.append(t)
             ox += nx + gap
         self.mask = packed
+        self.member_masks = [p[1] for p in parts]
         self.solver = capi.Solver(Q, precision, capi.LBM_PHYSICS, tau, 1.0, (0.0, 0.0, 0.0), 1.0, tawss_div, device)
         self.solver.set_geometry(packed, bcs)
         for idx, (t, m) in enumerate(zip(self.tri, members)):
             lo = (self.x0[idx] - 0.5, -1e30, -1e30)
             hi = (self.x1[idx] - 0.5, 1e30, 1e30)
             self.solver.set_normals_box(t, lo, hi)
-            n = None if periods is None else int(round(periods * m["period"]))
-            self.solver.set_waveform(idx, waveform.sinusoid_table(m["inlet_mean"], m["period"], n))
+            if steady:
+                self.solver.set_waveform(idx, [m["inlet_mean"]])
+            else:
+                n = None if periods is None else int(round(periods * m["period"]))
+                self.solver.set_waveform(idx, waveform.sinusoid_table(m["inlet_mean"], m["period"], n))
         self.counts = self.solver.counts()
 
     @property
@@ -87,6 +93,10 @@ class Ensemble:
 
     def step_async(self, n=1):
         self.solver.step_async(n)
+
+    def member_mask(self, k):
+        """Member k's own mask ([z][y][x], as voxelized alone)."""
+        return self.member_masks[k]
 
     def member_of_x(self, i):
         """Member index of lattice column x = i (-1 in a gap)."""

@@ -1,0 +1,476 @@
+"""Learned warm start: predict a steady rho / u field from the geometry and
+the inlet, start the lattice there, and let the plain LBM finish the job.
+
+The network is a 4-level 3D convolutional encoder-decoder (16, 32, 64, 64
+channels, skip connections by addition, nearest-neighbour upsampling) on a
+D x H x W grid (multiples of 8).  Input channels: signed distance to the
+wall (``lbm_sdf_from_mask``), the fluid mask, the inlet mean velocity and
+period; output channels: rho - 1 and u (scaled).  Every convolution,
+its gradients, the loss and Adam run in this library's kernels
+(``include/lbm_nn.h``: BF16 implicit GEMM on the tensor cores, FP32
+accumulation); PyTorch only allocates device memory and builds input
+tensors.  Training data are steady solutions of the plain LBM on seeded
+stenosed tubes and bifurcations, computed as one packed ensemble.
+
+The LBM stays the judge: a warm-started lattice is run to the same
+convergence criterion as a cold one (``steps_to_converge``, on FP64 lattices
+so that the criterion sits far above the storage's rounding noise), so a
+poor prediction costs steps, never accuracy.  The reference always starts from
+rest (Node.cpp:30-37); it has no counterpart to this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import capi
+
+C_IN = 16   # padded input channels (sdf, mask, inlet mean, inlet period, axial position, Poiseuille prior u_z, rho)
+C_OUT = 16  # padded output channels (rho - 1, ux, uy, uz)
+# network targets, normalised by the inlet amplitude U (the flows are slow:
+# u and rho - 1 scale with U): (rho - 1) / U * RHO_SCALE and u / U * U_SCALE
+RHO_SCALE = 0.5
+U_SCALE = 1.0
+SDF_SCALE = 0.2
+MEAN_SCALE = 30.0
+PERIOD_SCALE = 1.0 / 4000.0
+
+# (name, input, ci, co, kernel, stride, relu); "up:" inputs are upsampled x2,
+# "+" names the tensor added to the layer's output (skip connection)
+LAYERS = [
+    ("c0a", "x", 16, 16, 3, 1, 1, None),
+    ("c0b", "c0a", 16, 16, 3, 1, 1, None),
+    ("d1", "c0b", 16, 32, 3, 2, 1, None),
+    ("c1", "d1", 32, 32, 3, 1, 1, None),
+    ("d2", "c1", 32, 64, 3, 2, 1, None),
+    ("c2", "d2", 64, 64, 3, 1, 1, None),
+    ("d3", "c2", 64, 64, 3, 2, 1, None),
+    ("c3", "d3", 64, 64, 3, 1, 1, None),
+    ("u2", "up:c3", 64, 64, 3, 1, 1, "c2"),
+    ("c2u", "u2", 64, 64, 3, 1, 1, None),
+    ("u1", "up:c2u", 64, 32, 3, 1, 1, "c1"),
+    ("c1u", "u1", 32, 32, 3, 1, 1, None),
+    ("u0", "up:c1u", 32, 16, 3, 1, 1, "c0b"),
+    ("c0u", "u0", 16, 16, 3, 1, 1, None),
+    ("out", "c0u", 16, 16, 1, 1, 0, None),
+]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _dims(d):
+    return (C.c_int * 3)(*[int(v) for v in d])
+
+
+class WarmStartNet:
+    """Parameters, activations and gradients on one device; forward,
+    backward and Adam through the C ABI."""
+
+    def __init__(self, dims, device=0, seed=0):
+        torch = _torch()
+        self.torch = torch
+        self.L = capi.load()
+        self.dims = tuple(int(v) for v in dims)  # (D, H, W)
+        assert all(v % 8 == 0 for v in self.dims), "grid dims must be multiples of 8"
+        self.dev = torch.device("cuda", device)
+        self.stream = torch.cuda.current_stream(self.dev)
+        self.st = C.c_void_p(self.stream.cuda_stream)
+        rng = np.random.default_rng(seed)
+        # level of every tensor (0 = full grid) and its channels
+        self.level = {"x": 0}
+        self.chan = {"x": C_IN}
+        w_off, b_off = 0, 0
+        self.meta = {}
+        for name, src, ci, co, ks, stride, relu, skip in LAYERS:
+            lvl_in = self.level[src[3:]] - 1 if src.startswith("up:") else self.level[src]
+            lvl_out = lvl_in + (1 if stride == 2 else 0)
+            self.level[name] = lvl_out
+            self.chan[name] = co
+            taps = ks ** 3
+            self.meta[name] = dict(src=src, ci=ci, co=co, ks=ks, stride=stride, relu=relu, skip=skip,
+                                   lvl_in=lvl_in, lvl_out=lvl_out, w_off=w_off, w_n=co * taps * ci,
+                                   b_off=b_off, taps=taps)
+            w_off += co * taps * ci
+            b_off += co
+        self.nw, self.nb = w_off, b_off
+        w = np.zeros(self.nw, np.float32)
+        for name, m in self.meta.items():
+            ci_real = 7 if m["src"] == "x" else m["ci"]
+            co_real = 4 if name == "out" else m["co"]
+            std = math.sqrt(2.0 / (m["taps"] * ci_real)) * (0.3 if name == "out" else 1.0)
+            blk = np.zeros((m["co"], m["taps"], m["ci"]), np.float32)
+            blk[:co_real, :, :ci_real] = rng.normal(0.0, std, (co_real, m["taps"], ci_real))
+            w[m["w_off"]:m["w_off"] + m["w_n"]] = blk.reshape(-1)
+        f32 = dict(dtype=torch.float32, device=self.dev)
+        self.w = torch.from_numpy(w).to(self.dev)
+        self.wb = self.w.to(torch.bfloat16)
+        self.b = torch.zeros(self.nb, **f32)
+        self.gw = torch.zeros(self.nw, **f32)
+        self.gb = torch.zeros(self.nb, **f32)
+        self.mw, self.vw = torch.zeros(self.nw, **f32), torch.zeros(self.nw, **f32)
+        self.mb, self.vb = torch.zeros(self.nb, **f32), torch.zeros(self.nb, **f32)
+        self.wt = torch.empty(max(m["w_n"] for m in self.meta.values()), dtype=torch.bfloat16, device=self.dev)
+        self.step_count = 0
+        self._alloc()
+
+    # ------------------------------------------------------------------ buffers
+    def grid(self, lvl):
+        return tuple(v >> lvl for v in self.dims)
+
+    def nvox(self, lvl):
+        g = self.grid(lvl)
+        return g[0] * g[1] * g[2]
+
+    def _alloc(self):
+        torch = self.torch
+        bf = dict(dtype=torch.bfloat16, device=self.dev)
+        self.act, self.grad, self.up, self.pre = {}, {}, {}, {}
+        for name, m in self.meta.items():
+            n = self.nvox(m["lvl_out"]) * m["co"]
+            self.act[name] = torch.empty(n, **bf)
+            self.grad[name] = torch.empty(n, **bf)
+            if m["src"].startswith("up:"):
+                self.up[name] = torch.empty(self.nvox(m["lvl_in"]) * m["ci"], **bf)
+            if m["skip"]:
+                self.pre[name] = torch.empty(n, **bf)  # the layer's own (ReLU) output before the skip sum
+        self.grad_up = {k: torch.empty_like(v) for k, v in self.up.items()}
+        self.skip_grad = {m["skip"]: torch.empty_like(self.act[m["skip"]]) for m in self.meta.values() if m["skip"]}
+        self.y32 = torch.empty(self.nvox(0) * C_OUT, dtype=torch.float32, device=self.dev)
+        self.dpred = torch.empty(self.nvox(0) * C_OUT, **bf)
+        self.loss = torch.zeros(1, dtype=torch.float32, device=self.dev)
+
+    def _check(self, rc):
+        capi._check(rc)
+
+    # ------------------------------------------------------------------ forward
+    def forward(self, x):
+        """x: BF16 [D*H*W*C_IN] channels-last input; returns FP32 [voxels][C_OUT]."""
+        L = self.L
+        self.x = x
+        for name, m in self.meta.items():
+            src = m["src"]
+            if src.startswith("up:"):
+                s = src[3:]
+                self._check(L.lbm_nn_upsample2(_ptr(self.act[s]), _dims(self.grid(self.level[s])), m["ci"],
+                                               _ptr(self.up[name]), 0, self.st))
+                xin = self.up[name]
+            else:
+                xin = x if src == "x" else self.act[src]
+            w = self.wb[m["w_off"]:m["w_off"] + m["w_n"]]
+            b = self.b[m["b_off"]:m["b_off"] + m["co"]]
+            y32 = self.y32 if name == "out" else None
+            y = self.pre[name] if m["skip"] else self.act[name]
+            self._check(L.lbm_nn_conv3d_fwd(_ptr(xin), _dims(self.grid(m["lvl_in"])), m["ci"], _ptr(w), _ptr(b),
+                                            m["co"], m["ks"], m["stride"], m["relu"], _ptr(y), _ptr(y32), self.st))
+            if m["skip"]:
+                self._check(L.lbm_nn_add(_ptr(y), _ptr(self.act[m["skip"]]), _ptr(self.act[name]), y.numel(),
+                                         self.st))
+        return self.y32
+
+    # ------------------------------------------------------------------ backward
+    def backward(self, dy_out):
+        """dy_out: BF16 gradient of the output layer's result; accumulates
+        the parameter gradients into gw / gb."""
+        L = self.L
+        self.grad["out"].copy_(dy_out)
+        for name in reversed(list(self.meta.keys())):
+            m = self.meta[name]
+            g = self.grad[name]
+            if m["skip"]:
+                # the sum's gradient also reaches the skip source
+                self.skip_grad[m["skip"]].copy_(g)
+            if m["relu"]:
+                y = self.pre[name] if m["skip"] else self.act[name]
+                self._check(L.lbm_nn_relu_bwd(_ptr(y), _ptr(g), g.numel(), self.st))
+            src = m["src"]
+            if src.startswith("up:"):
+                xin, dx = self.up[name], self.grad_up[name]
+            elif src == "x":
+                xin, dx = self.x, None
+            else:
+                xin, dx = self.act[src], self.grad[src]
+            w = self.wb[m["w_off"]:m["w_off"] + m["w_n"]]
+            self._check(L.lbm_nn_conv3d_bwd(_ptr(xin), _dims(self.grid(m["lvl_in"])), m["ci"], _ptr(w),
+                                            _ptr(self.wt), m["co"], m["ks"], m["stride"], _ptr(g), _ptr(dx),
+                                            _ptr(self.gw[m["w_off"]:m["w_off"] + m["w_n"]]),
+                                            _ptr(self.gb[m["b_off"]:m["b_off"] + m["co"]]), self.st))
+            if src.startswith("up:"):
+                s = src[3:]
+                self._check(L.lbm_nn_upsample2(_ptr(dx), _dims(self.grid(self.level[s])), m["ci"],
+                                               _ptr(self.grad[s]), 1, self.st))
+            elif src in self.skip_grad:
+                self._check(L.lbm_nn_add(_ptr(dx), _ptr(self.skip_grad[src]), _ptr(dx), dx.numel(), self.st))
+
+    def zero_grad(self):
+        self.gw.zero_()
+        self.gb.zero_()
+
+    def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.step_count += 1
+        L = self.L
+        self._check(L.lbm_nn_adam(_ptr(self.w), _ptr(self.wb), _ptr(self.gw), _ptr(self.mw), _ptr(self.vw), self.nw,
+                                  lr, b1, b2, eps, self.step_count, self.st))
+        self._check(L.lbm_nn_adam(_ptr(self.b), None, _ptr(self.gb), _ptr(self.mb), _ptr(self.vb), self.nb, lr, b1,
+                                  b2, eps, self.step_count, self.st))
+
+    def loss_and_grad(self, pred, target, mask, inv_norm):
+        """Masked MSE over the 4 physical output channels (added to
+        self.loss on the device); returns the BF16 output gradient."""
+        self._check(self.L.lbm_nn_mse(_ptr(pred), _ptr(target), _ptr(mask), self.nvox(0), C_OUT, 4, inv_norm,
+                                      _ptr(self.dpred), _ptr(self.loss), self.st))
+        return self.dpred
+
+
+# ---------------------------------------------------------------------- data
+def sdf_of_mask(mask, device=0):
+    """Signed distance (device FP32 [D*H*W]) of a [D][H][W] mask."""
+    torch = _torch()
+    dev = torch.device("cuda", device)
+    m = torch.from_numpy(np.ascontiguousarray(mask, np.uint8)).to(dev)
+    out = torch.empty(mask.size, dtype=torch.float32, device=dev)
+    scratch = torch.empty(2 * mask.size, dtype=torch.int32, device=dev)
+    st = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    capi._check(capi.load().lbm_sdf_from_mask(_ptr(m), _dims(mask.shape), _ptr(out), _ptr(scratch), st))
+    return out
+
+
+def poiseuille_prior(mask, inlet, tau):
+    """Slice-wise Hagen-Poiseuille estimate of the steady flow (flow along
+    +z, parabolic inlet of peak `inlet` on the first fluid slice, density 1
+    on the last): with s the in-slice distance to the half-way wall and R(z)
+    its largest value in slice z, u_z = 2 Q / (pi R^2) (1 - (R - s)^2 / R^2)
+    and rho from d rho/dz = -3 * 8 nu Q / (pi R^4).  Returns voxel arrays."""
+    from scipy.ndimage import distance_transform_edt
+    D = mask.shape[0]
+    fl = mask > 0
+    s = np.zeros(mask.shape, np.float64)
+    for z in range(D):
+        if fl[z].any():
+            s[z] = np.where(fl[z], distance_transform_edt(fl[z]) - 0.5, 0.0)
+    R = s.reshape(D, -1).max(1)
+    zs = np.nonzero(R > 0)[0]
+    uz = np.zeros(mask.shape, np.float64)
+    rho = np.ones(mask.shape, np.float64)
+    if zs.size == 0:
+        return rho, uz
+    Q = math.pi * R[zs[0]] ** 2 * inlet / 2.0
+    nu = (tau - 0.5) / 3.0
+    Rs = np.maximum(R, 1.0)
+    peak = 2.0 * Q / (math.pi * Rs ** 2)
+    prof = np.clip(1.0 - (Rs[:, None, None] - s) ** 2 / Rs[:, None, None] ** 2, 0.0, 1.0)
+    uz = np.where(fl, peak[:, None, None] * prof, 0.0)
+    drho = np.where(R > 0, 3.0 * 8.0 * nu * Q / (math.pi * Rs ** 4), 0.0)
+    tail = np.concatenate([np.cumsum(drho[::-1])[::-1][1:], [0.0]])  # sum over the slices downstream
+    rho = np.where(fl, 1.0 + tail[:, None, None], 1.0)
+    return rho, uz
+
+
+def features(mask, inlet_mean, period, tau=0.8, device=0):
+    """BF16 channels-last network input [D*H*W*C_IN] and the prior (rho,
+    u_z) voxel arrays the network's output corrects."""
+    torch = _torch()
+    dev = torch.device("cuda", device)
+    n = mask.size
+    sdf = sdf_of_mask(mask, device)
+    rho_p, uz_p = poiseuille_prior(mask, inlet_mean, tau)
+    x = torch.zeros((n, C_IN), dtype=torch.float32, device=dev)
+    x[:, 0] = torch.clamp(sdf * SDF_SCALE, -3.0, 3.0)
+    x[:, 1] = torch.from_numpy(mask.reshape(-1).astype(np.float32)).to(dev)
+    x[:, 2] = inlet_mean * MEAN_SCALE
+    x[:, 3] = period * PERIOD_SCALE
+    # axial position (flow along z): the pressure level depends on the
+    # distance to the outlet, beyond the convolutions' receptive field
+    D, H, W = mask.shape
+    x[:, 4] = (torch.arange(D, device=dev, dtype=torch.float32) / D).repeat_interleave(H * W)
+    x[:, 5] = torch.from_numpy((uz_p / inlet_mean).reshape(-1).astype(np.float32)).to(dev)
+    x[:, 6] = torch.from_numpy(((rho_p - 1.0) / inlet_mean * RHO_SCALE).reshape(-1).astype(np.float32)).to(dev)
+    return x.to(torch.bfloat16).reshape(-1).contiguous(), (rho_p, uz_p)
+
+
+def make_target(mask, rho, u, inlet, prior, device=0):
+    """FP32 [D*H*W][4] target: the scaled correction of the prior."""
+    torch = _torch()
+    rho_p, uz_p = prior
+    t = np.zeros((mask.size, 4), np.float32)
+    fl = mask.reshape(-1) > 0
+    t[fl, 0] = (rho - rho_p.reshape(-1)[fl]) / inlet * RHO_SCALE
+    t[fl, 1:] = u / inlet * U_SCALE
+    t[fl, 3] -= uz_p.reshape(-1)[fl] / inlet * U_SCALE
+    return torch.from_numpy(t.reshape(-1)).to(torch.device("cuda", device))
+
+
+def smooth_masked(mask, v, rounds=2):
+    """[1, 2, 1] / 4 filter along each axis, restricted to fluid voxels
+    (weights renormalised where a neighbour is solid): removes the
+    voxel-scale (checkerboard) content of a prediction, which the lattice
+    would otherwise carry as undamped modes."""
+    fl = mask > 0
+    v = np.where(fl, v, 0.0)
+    w = fl.astype(np.float64)
+    for _ in range(rounds):
+        for a in range(3):
+            num = 2.0 * v
+            den = 2.0 * w
+            for sh in (1, -1):
+                num = num + np.roll(v * w, sh, axis=a) * _edge(mask.shape, a, sh)
+                den = den + np.roll(w, sh, axis=a) * _edge(mask.shape, a, sh)
+            v = np.where(fl, num / np.maximum(den, 1e-30), 0.0)
+    return v
+
+
+def _edge(shape, a, sh):
+    """1 where np.roll along axis a by sh brings a real neighbour (not a wrap)."""
+    e = np.ones(shape[a])
+    e[0 if sh == 1 else -1] = 0.0
+    return e.reshape([-1 if k == a else 1 for k in range(3)])
+
+
+def prediction_to_macro(mask, y32, inlet, prior, smooth=2):
+    """Per-active-node rho (FP32) and u (FP32, 3 per node) from the output
+    (prior + correction, smoothed over the fluid)."""
+    rho_p, uz_p = prior
+    y = y32.reshape(-1, C_OUT)[:, :4].cpu().numpy().astype(np.float64)
+    shape = mask.shape
+    rho = rho_p + (y[:, 0] * inlet / RHO_SCALE).reshape(shape)
+    u = [(y[:, 1 + c] * inlet / U_SCALE).reshape(shape) for c in range(3)]
+    u[2] = u[2] + uz_p
+    if smooth:
+        rho = 1.0 + smooth_masked(mask, rho - 1.0, smooth)
+        u = [smooth_masked(mask, c, smooth) for c in u]
+    fl = mask.reshape(-1) > 0
+    r = rho.reshape(-1)[fl].astype(np.float32)
+    uu = np.stack([c.reshape(-1)[fl] for c in u], 1).astype(np.float32)
+    return r, uu
+
+
+def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4):
+    """Seeded stenosed tubes (and every k-th a small Y-bifurcation) filling
+    a fixed box (x, y, z) between an inlet at z = 0 and an outlet at z = top."""
+    from . import geometry as G
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = box
+    out = []
+    for m in range(n):
+        mean = float(rng.uniform(0.01, 0.04))
+        period = float(rng.uniform(2000.0, 6000.0))
+        cx, cy = 0.5 * (nx - 1) + 0.173, 0.5 * (ny - 1) + 0.061
+        if bifurcation_every and m % bifurcation_every == bifurcation_every - 1:
+            r = float(rng.uniform(4.0, 5.5))
+            s = G.y_bifurcation(r, 0.72 * r, float(rng.uniform(8.0, 14.0)), z_in=1.3, z_out=nz - 1.4,
+                                z_split=0.5 * nz, center=(cx, cy), seed=seed * 1000 + m, h=1.0)
+            kind = "bifurcation"
+        else:
+            r = float(rng.uniform(4.0, 9.0))
+            s = G.stenosed_tube(r, nz - 2.7, float(rng.uniform(0.2, 0.7)), float(rng.uniform(0.0, 0.3)),
+                                center=(cx, cy), z0=1.3, seed=seed * 1000 + m, h=max(1.0, r / 8.0))
+            kind = "stenosed_tube"
+        lo, hi = s.v.reshape(-1, 3).min(0), s.v.reshape(-1, 3).max(0)
+        if lo.min() < 0.0 or hi[0] > nx - 1.0 or hi[1] > ny - 1.0 or hi[2] > nz:
+            raise ValueError(f"member {m} leaves the {box} box")
+        meta = dict(s.meta)
+        s = G.add_bbox_anchors(s, (0.0, 0.0, 0.0), (nx - 1.0, ny - 1.0, float(nz)))
+        s.meta = meta
+        out.append({"surface": s, "radius": r, "center": (cx, cy), "inlet_mean": mean, "period": period,
+                    "kind": kind})
+    return out
+
+
+def steady_ensemble(members, tau=0.8, steps=40000, precision="f32", device=0):
+    """Steady solutions (constant inlet at each member's mean) of all members
+    advanced as one packed lattice; returns per member (mask, rho, u)."""
+    from .ensemble import Ensemble
+    ens = Ensemble(members, 19, precision, tau, device=device, steady=True)
+    ens.solver.set_graph_steps(32)
+    ens.step(steps)
+    rho, u, mem = ens.macro()
+    out = []
+    for k, m in enumerate(members):
+        mask = ens.member_mask(k)
+        out.append((mask, rho[mem == k], u[mem == k]))
+    ens.solver.close()
+    return out
+
+
+def residual_runner(solver, check=100):
+    """Relative change of u over `check` steps, for a convergence loop."""
+    prev = solver.macro()[1]
+
+    def step():
+        nonlocal prev
+        solver.step(check)
+        u = solver.macro()[1]
+        r = float(np.max(np.abs(u - prev)) / max(np.max(np.abs(u)), 1e-30))
+        prev = u
+        return r
+
+    return step
+
+
+def steps_to_converge(solver, tol=1e-6, check=100, max_steps=60000):
+    """Steps until max|u(t) - u(t - check)| / max|u| < tol (or max_steps);
+    returns (steps, last residual)."""
+    step = residual_runner(solver, check)
+    n, r = 0, float("inf")
+    while n < max_steps:
+        r = step()
+        n += check
+        if r < tol:
+            break
+    return n, r
+
+
+def single_lattice(member, tau=0.8, precision="f64", device=0):
+    """One member as its own lattice with a constant inlet (steady problem)."""
+    tri = member["surface"].tri12()
+    mask, vd = capi.voxelize(tri, 1.0)
+    bb = np.array(vd.bbox[:])
+    fl = np.argwhere(mask > 0)
+    kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
+    s = capi.Solver(19, precision, capi.LBM_PHYSICS, tau, 1.0, (bb[0], bb[2], bb[4]), 1.0, 1.0, device)
+    s.set_geometry(mask, [capi.bc_spec(capi.LBM_BC_VELOCITY, "z-", kin, 1.0, 1, member["center"][0],
+                                       member["center"][1], member["radius"]),
+                          capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)])
+    s.set_normals(tri)
+    s.set_inlet_table([member["inlet_mean"]])
+    return s, mask
+
+
+def make_sample(mask, member, rho, u, tau=0.8, device=0):
+    """(input, target, device mask, 1 / (4 * fluid voxels)) for training."""
+    torch = _torch()
+    x, prior = features(mask, member["inlet_mean"], member["period"], tau, device)
+    t = make_target(mask, rho, u, member["inlet_mean"], prior, device)
+    m = torch.from_numpy(np.ascontiguousarray(mask.reshape(-1), np.uint8)).to(torch.device("cuda", device))
+    return x, t, m, 1.0 / (4.0 * max(1, int(mask.sum())))
+
+
+def train(net, samples, iters=400, lr=2e-3, batch=4, log=None):
+    """samples: list of make_sample tuples; Adam with a cosine-decayed
+    learning rate.  Returns the loss history (mean over each batch)."""
+    hist = []
+    rng = np.random.default_rng(0)
+    base = lr
+    for it in range(iters):
+        lr = base * 0.5 * (1.0 + math.cos(math.pi * it / iters)) + 0.02 * base
+        net.zero_grad()
+        net.loss.zero_()
+        for k in rng.choice(len(samples), size=min(batch, len(samples)), replace=False):
+            x, t, m, inv = samples[k]
+            y = net.forward(x)
+            d = net.loss_and_grad(y, t, m, inv)
+            net.backward(d)
+        net.adam(lr)
+        if it % 20 == 0 or it == iters - 1:
+            hist.append(float(net.loss.item()) / batch)
+            if log:
+                log(it, hist[-1])
+    return hist
