@@ -552,7 +552,7 @@ def run_ours(args):
                     "step": f"{B} LBM steps per call batch + WSS/OSI/TAWSS and rho/u read-back (pinned host buffers)"},
             "gpu_launches": launches,
             "autotune": {"variant": tuned[0], "ms_per_step_by_variant": tuned[1],
-                         "variants": "(block, min blocks/SM): (128,12) (128,10) (128,8) (256,3) (256,1)"},
+                         "variants": "(block, min blocks/SM): (128,12) (128,10) (128,8) (256,3) (256,1); 5: tiled bulk-copy kernel"},
             "clocks": clk.summary(),
             "extra": extra,
         }

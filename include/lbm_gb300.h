@@ -244,14 +244,17 @@ lbm_status lbm_get_launch_count(lbm_handle* h, int64_t* launches);
 /* Steps per captured CUDA graph (0 = launch kernels directly). */
 lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph);
 
-/* Launch-shape variants of the step kernel (block size x minimum resident
- * blocks per SM): (128,12) (128,10) (128,8) (256,3) (256,1); a new handle
- * starts on variant 0, FP64 on variant 4.  lbm_autotune times each variant for trial_steps steps on a
+/* Launch-shape variants of the step kernel: one node per thread with
+ * (block size, minimum resident blocks per SM) = (128,12) (128,10) (128,8)
+ * (256,3) (256,1), and variant 5, the tiled kernel (bulk copies stage each
+ * 256-node tile's sources in shared memory; physics mode, FP32 / FP16 /
+ * BF16; elsewhere it runs variant 0, or 4 for FP64).  A new handle starts on
+ * variant 0, FP64 on variant 4.  lbm_autotune times each variant for trial_steps steps on a
  * snapshot of the current state, restores the state, keeps the fastest and
  * reports it (and, if ms_per_step is not NULL, the time of every variant:
  * LBM_NUM_VARIANTS floats).  No reference counterpart (the reference has a
  * single serial loop). */
-#define LBM_NUM_VARIANTS 5
+#define LBM_NUM_VARIANTS 6
 lbm_status lbm_autotune(lbm_handle* h, int trial_steps, int* best, float* ms_per_step);
 lbm_status lbm_set_variant(lbm_handle* h, int variant);
 

@@ -68,7 +68,7 @@ EXPORTS = [
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
     "lbm_nn_adam", "lbm_sdf_from_mask",
 ]
-NUM_VARIANTS = 5
+NUM_VARIANTS = 6
 
 
 def lib_path() -> str:

@@ -13,6 +13,8 @@
 // buf[cur] and writes buf[1-cur].  A read-out pulls from buf[1-cur] -- the
 // previous step's populations -- and applies the boundary rules again, or
 // reads buf[0] directly if no step ran since the start.
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -43,6 +45,9 @@ struct lbm_handle {
     void* nw_prev = nullptr;
     double *nw_n = nullptr, *nw_wss = nullptr, *nw_acc = nullptr, *nw_accm = nullptr;
     float *nw_nf = nullptr, *nw_wssf = nullptr;  // FP32-arithmetic formats
+    int64_t nw_stride = 0;                         // plane stride of nw_nf
+    int32_t* tile_plan = nullptr;                  // tiled step kernel (physics, FP32-arithmetic formats)
+    TileGeom tile{};
     float* nw_ring = nullptr;                      // [kRingSlots][4][nnw]
     double* nw_out = nullptr;                      // read-out staging, [5][nnw]
     float2* nw_accf = nullptr;
@@ -175,7 +180,7 @@ void free_geometry(lbm_handle* h) {
                     g.sp_of_act, h->bct, h->sp_flux,
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
-                    h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf,
+                    h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf, h->tile_plan,
                     h->nw_ring, h->nw_out};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -187,6 +192,8 @@ void free_geometry(lbm_handle* h) {
     h->bct = nullptr;
     h->sp_flux = nullptr;
     h->nw_nf = h->nw_wssf = nullptr;
+    h->tile_plan = nullptr;
+    h->tile = TileGeom{};
     h->nw_accf = nullptr;
     h->nw_ring = nullptr;
     h->nw_out = nullptr;
@@ -225,6 +232,9 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.nw_acc = h->nw_acc;
     p.nw_accm = h->nw_accm;
     p.nw_nf = h->nw_nf;
+    p.nw_stride = h->nw_stride;
+    p.tile_plan = h->tile_plan;
+    p.tile = h->tile;
     p.nw_ring = h->nw_ring;
     p.nw_accf = h->nw_accf;
     p.nw_prev = h->nw_prev;
@@ -290,6 +300,8 @@ int check_flags(lbm_handle* h) {
     unsigned f = 0;
     CK(h, cudaMemcpyAsync(&f, h->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
+    if (f & FLAG_TIMEOUT)
+        return fail(h, LBM_ERR_CUDA, "tiled step: a bulk copy did not complete within the wait limit");
     if (f & FLAG_NONFINITE)
         return fail(h, LBM_ERR_NONFINITE, "a density became NaN/Inf: the run diverged (check tau and the inlet)");
     return LBM_OK;
@@ -488,6 +500,112 @@ void build_segments(int Q, const uint8_t* mask, int nx, int ny, int nz, int64_t&
                     std::vector<int32_t>& delta) {
     if (Q == 19) build_segments_q<19>(mask, nx, ny, nz, nact, seg_of, delta);
     else build_segments_q<27>(mask, nx, ny, nz, nact, seg_of, delta);
+}
+
+// FP32 copy of the normals [3][nn] with plane stride `stride`.
+std::vector<float> float_normals(const std::vector<double>& nd, int64_t nn, int64_t stride) {
+    std::vector<float> nf(3 * stride, 0.f);
+    for (int a = 0; a < 3; ++a)
+        for (int64_t k = 0; k < nn; ++k) nf[a * stride + k] = (float)nd[a * nn + k];
+    return nf;
+}
+
+// Plan of the tiled step kernel: per tile of kTileNodes active nodes and
+// population plane q, the window of plane q holding every valid pull source
+// of the tile's nodes (widened to 16-byte boundaries); the tile's pull
+// segments and next-to-wall entries; the shared-memory layout of a pipeline
+// stage.  Returns false (no plan) when a stage does not fit.
+template <int Q>
+bool build_tile_plan_q(const uint8_t* mask, int nx, int ny, int nz, int64_t nact, int64_t stride, int es,
+                       const std::vector<int32_t>& seg_of, const std::vector<int32_t>& delta,
+                       const std::vector<int32_t>& sp_of_act, int64_t nnw, std::vector<int32_t>& plan, TileGeom& G) {
+    constexpr int T = kTileNodes, DR = kDeltaRow<Q>, PI = 2 * Q + kTilePlanExtra;
+    const int A = 16 / es;  // elements per 16 bytes
+    const int64_t ntiles = ceil_div(nact, T);
+    const int64_t nxy = (int64_t)nx * ny;
+    std::vector<int64_t> lo((size_t)ntiles * Q, INT64_MAX), hi((size_t)ntiles * Q, -1);
+    int64_t an = 0;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                if (!mask[(int64_t)k * nxy + (int64_t)j * nx + i]) continue;
+                const int32_t* d = delta.data() + (int64_t)seg_of[an] * DR;
+                const int64_t t = an / T;
+                for (int q = 0; q < Q; ++q) {
+                    const int x = i - Lat<Q>::cx(q), y = j - Lat<Q>::cy(q), z = k - Lat<Q>::cz(q);
+                    if (x < 0 || x >= nx || y < 0 || y >= ny || z < 0 || z >= nz ||
+                        !mask[(int64_t)z * nxy + (int64_t)y * nx + x])
+                        continue;
+                    const int64_t src = an + d[q];
+                    int64_t& l = lo[t * Q + q];
+                    int64_t& h = hi[t * Q + q];
+                    if (src < l) l = src;
+                    if (src > h) h = src;
+                }
+                ++an;
+            }
+    plan.assign((size_t)ntiles * PI, 0);
+    int64_t wcap = A, segmax = 1, nwcap = 4;
+    for (int64_t t = 0; t < ntiles; ++t) {
+        int32_t* pl = plan.data() + t * PI;
+        for (int q = 0; q < Q; ++q) {
+            const int64_t h = hi[t * Q + q];
+            if (h < 0) continue;
+            const int64_t l0 = lo[t * Q + q] / A * A, h1 = ceil_div(h + 1, A) * A;
+            if (h1 > stride) return false;
+            pl[q] = (int32_t)l0;
+            pl[Q + q] = (int32_t)(h1 - l0);
+            wcap = std::max(wcap, h1 - l0);
+        }
+        const int64_t a0 = t * T, a1 = std::min(nact, a0 + T) - 1;
+        pl[2 * Q] = seg_of[a0];
+        pl[2 * Q + 1] = seg_of[a1] - seg_of[a0] + 1;
+        segmax = std::max<int64_t>(segmax, pl[2 * Q + 1]);
+        int64_t smin = INT64_MAX, smax = -1;
+        for (int64_t a = a0; a <= a1; ++a)
+            if (sp_of_act[a] >= 0 && sp_of_act[a] < nnw) {
+                smin = std::min<int64_t>(smin, sp_of_act[a]);
+                smax = std::max<int64_t>(smax, sp_of_act[a]);
+            }
+        if (smax >= 0) {
+            pl[2 * Q + 2] = (int32_t)(smin / 4 * 4);
+            pl[2 * Q + 3] = (int32_t)(ceil_div(smax + 1, 4) * 4 - smin / 4 * 4);
+            nwcap = std::max<int64_t>(nwcap, pl[2 * Q + 3]);
+        }
+    }
+    const int segcap = (int)std::min<int64_t>(segmax, 64);
+    for (int64_t t = 0; t < ntiles; ++t) {
+        int32_t* pl = plan.data() + t * PI;
+        pl[2 * Q + 1] = std::min(pl[2 * Q + 1], segcap);  // the rest read their rows from global memory
+    }
+    wcap = ceil_div(wcap, 8) * 8;
+    auto al = [](int64_t v) { return (int)ceil_div(v, 128) * 128; };
+    TileGeom g{};
+    g.ntiles = ntiles;
+    g.wcap = (int)wcap;
+    g.segcap = segcap;
+    g.nwcap = (int)nwcap;
+    g.off_pull = 0;
+    g.off_own = al(g.off_pull + (int64_t)Q * wcap * es);
+    g.off_word = al(g.off_own + (int64_t)Q * T * es);
+    g.off_sp = al(g.off_word + (int64_t)T * 8);
+    g.off_delta = al(g.off_sp + (int64_t)T * 4);
+    g.off_nrm = al(g.off_delta + (int64_t)segcap * DR * 4);
+    g.off_hdr = al(g.off_nrm + 3 * nwcap * 4);
+    g.stage_bytes = al(g.off_hdr + (Q + 3) * 4);
+    // deepest pipeline and most CTAs per SM that fit 227 KB per CTA / 228 KB per SM
+    const int choices[4][2] = {{3, 2}, {2, 2}, {3, 1}, {2, 1}};
+    for (const auto& c : choices) {
+        const int smem = c[0] * g.stage_bytes + c[0] * 8;
+        if (smem <= 232448 && c[1] * (smem + 1024) <= 233472) {
+            g.nstage = c[0];
+            g.ctas_per_sm = c[1];
+            g.smem_bytes = smem;
+            G = g;
+            return true;
+        }
+    }
+    return false;
 }
 
 const uint32_t kCkptMagic = 0x4c424d43;  // "CMBL"
@@ -690,8 +808,9 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     CK(h, dalloc(h, &h->nw_wss, sizeof(double) * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_acc, sizeof(double) * 3 * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_accm, sizeof(double) * (h->g.nnw + 1)));
-    CK(h, dalloc(h, &h->nw_nf, sizeof(float) * 3 * (h->g.nnw + 1)));
-    CK(h, cudaMemsetAsync(h->nw_nf, 0, sizeof(float) * 3 * (h->g.nnw + 1), h->st));
+    h->nw_stride = ceil_div(h->g.nnw + 1, 4) * 4;  // 16-byte planes: the tiled kernel copies them in bulk
+    CK(h, dalloc(h, &h->nw_nf, sizeof(float) * 3 * h->nw_stride));
+    CK(h, cudaMemsetAsync(h->nw_nf, 0, sizeof(float) * 3 * h->nw_stride, h->st));
     CK(h, dalloc(h, &h->nw_wssf, sizeof(float) * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_accf, sizeof(float2) * 4 * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_ring, sizeof(float) * kRingSlots * 4 * (h->g.nnw + 1)));
@@ -724,6 +843,26 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     }
     c.fluid = h->g.nact - bnd;
     h->counts = c;
+    // plan of the tiled step kernel (physics mode, FP32-arithmetic formats)
+    if (h->d.mode == LBM_PHYSICS && h->d.precision != LBM_F64 && h->g.nact > 0) {
+        std::vector<int32_t> spa(h->g.nact);
+        CK(h, cudaMemcpyAsync(spa.data(), h->g.sp_of_act, sizeof(int32_t) * h->g.nact, cudaMemcpyDeviceToHost, h->st));
+        CK(h, cudaStreamSynchronize(h->st));
+        std::vector<int32_t> plan;
+        TileGeom G{};
+        const int es = (int)elem_size(h->d.precision);
+        const bool ok = Q == 19 ? build_tile_plan_q<19>(mask, h->nx, h->ny, h->nz, h->g.nact, h->stride, es, seg_of,
+                                                         delta, spa, h->g.nnw, plan, G)
+                                : build_tile_plan_q<27>(mask, h->nx, h->ny, h->nz, h->g.nact, h->stride, es, seg_of,
+                                                         delta, spa, h->g.nnw, plan, G);
+        if (ok) {
+            CK(h, dalloc(h, &h->tile_plan, sizeof(int32_t) * plan.size()));
+            CK(h, cudaMemcpyAsync(h->tile_plan, plan.data(), sizeof(int32_t) * plan.size(), cudaMemcpyHostToDevice,
+                                  h->st));
+            CK(h, cudaStreamSynchronize(h->st));
+            h->tile = G;
+        }
+    }
     return lbm_init_equilibrium(h);
 }
 
@@ -741,10 +880,9 @@ lbm_status lbm_set_normals_from_surface(lbm_handle* h, const double* tri12, int6
     if (e == cudaSuccess && h->g.nnw > 0) {
         // FP32 copy for the FP32-arithmetic formats
         std::vector<double> nd(3 * h->g.nnw);
-        std::vector<float> nf(3 * h->g.nnw);
         e = cudaMemcpyAsync(nd.data(), h->nw_n, sizeof(double) * nd.size(), cudaMemcpyDeviceToHost, h->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-        for (size_t k = 0; k < nd.size(); ++k) nf[k] = (float)nd[k];
+        const std::vector<float> nf = float_normals(nd, h->g.nnw, h->nw_stride);
         if (e == cudaSuccess) e = cudaMemcpyAsync(h->nw_nf, nf.data(), sizeof(float) * nf.size(), cudaMemcpyHostToDevice, h->st);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
@@ -795,14 +933,14 @@ lbm_status lbm_set_normals_from_surface_box(lbm_handle* h, const double* tri12, 
     if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), d_out, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(nd.data(), h->nw_n, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-    std::vector<float> nf(3 * nn);
+    std::vector<float> nf;
     if (e == cudaSuccess) {
         for (int64_t k = 0; k < m; ++k)
             for (int a = 0; a < 3; ++a) nd[a * nn + sel_idx[k]] = part[a * m + k];
-        for (int64_t k = 0; k < 3 * nn; ++k) nf[k] = (float)nd[k];
+        nf = float_normals(nd, nn, h->nw_stride);
         e = cudaMemcpyAsync(h->nw_n, nd.data(), sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, h->st);
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h->nw_nf, nf.data(), sizeof(float) * 3 * nn, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->nw_nf, nf.data(), sizeof(float) * nf.size(), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     cudaFree(d_tri);
     cudaFree(d_pt);

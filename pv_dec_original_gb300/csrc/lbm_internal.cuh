@@ -13,7 +13,30 @@ namespace lbm {
 enum : uint8_t { CLS_SOLID = 0, CLS_FLUID = 1, CLS_WALL = 2, CLS_BC0 = 3, CLS_NW_BIT = 0x80, CLS_MASK = 0x7f };
 
 // Error flags raised by kernels (polled by the host after each batch).
-enum : unsigned { FLAG_NONFINITE = 1u, FLAG_EXACT_ZERO = 2u, FLAG_BOUNDS = 4u };
+enum : unsigned { FLAG_NONFINITE = 1u, FLAG_EXACT_ZERO = 2u, FLAG_BOUNDS = 4u, FLAG_TIMEOUT = 8u };
+
+// Tiled step: tiles of kTileNodes consecutive active nodes whose sources
+// are staged in shared memory by bulk copies.  Per-tile plan (int32):
+// [0, Q) source-window start per population plane (element index, 16-byte
+// aligned), [Q, 2Q) window length (elements, a multiple of 16 bytes), then
+// the tile's first pull segment, its segment count (capped at segcap), the
+// start of its next-to-wall entries (a multiple of 4) and their count (a
+// multiple of 4).
+constexpr int kTileNodes = 256;
+constexpr int kTilePlanExtra = 4;
+
+// Shared-memory layout of one pipeline stage (byte offsets) and the caps
+// the plan guarantees.
+struct TileGeom {
+    int64_t ntiles;      // 0: no plan (the tiled variant falls back)
+    int wcap;            // elements per plane of a source window
+    int segcap;          // delta rows per tile
+    int nwcap;           // next-to-wall entries per tile (per normal plane)
+    int nstage;          // pipeline depth (2 or 3)
+    int ctas_per_sm;
+    int stage_bytes, smem_bytes;
+    int off_pull, off_own, off_word, off_sp, off_delta, off_nrm, off_hdr;
+};
 
 struct BCDev {
     int kind;
@@ -54,7 +77,8 @@ struct StepParams {
     // kRingSlots steps' stresses (write-only in a step), and compensated
     // two-float accumulators (hi, lo) of tau_x, tau_y, tau_z, |tau| that the
     // step whose slot is the ring's last folds the whole ring into
-    const float* nw_nf;       // [3][nnw]
+    const float* nw_nf;       // [3][nw_stride]
+    int64_t nw_stride;        // plane stride of nw_nf (nnw + 1 rounded up to 4)
     float* nw_ring;           // [kRingSlots][4][nnw]: step s in slot s % kRingSlots
     float2* nw_accf;          // [4][nnw]
     void* nw_prev;            // parity: rho, ux, uy, uz of the previous collision, [4][nnw]
@@ -76,6 +100,8 @@ struct StepParams {
     int64_t* step_next;        // the other slot: written with *step_base + 1
     int step_off;
     int direct;                // read-out of the initial state: no pull, no boundary rules
+    const int32_t* tile_plan;  // per tile: 2 Q + kTilePlanExtra int32
+    TileGeom tile;
     const BCDev* bct;  // boundary-condition rules (device table)
     int nbc;
     unsigned* flags;
@@ -91,7 +117,7 @@ constexpr int kStepThreads = 256;
 // Launchers (one per translation unit family).  kind: 0 step, 1 prologue
 // (collide the initial state), 2 materialize (post-boundary f + sums).
 constexpr int kRingSlots = 16;  // steps between folds of the FP32 stress ring
-constexpr int kNumVariants = 5;  // launch-shape variants of the step kernel (step_kernels.cuh)
+constexpr int kNumVariants = 6;  // launch-shape variants of the step kernel (step_kernels.cuh)
 cudaError_t launch_step_f64(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 cudaError_t launch_step_f32(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 cudaError_t launch_step_f16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);

@@ -94,6 +94,8 @@ template <> struct Store<double> {
     template <int Q>
     __device__ static __forceinline__ real load(const double* p, int q) { return *p; }
     template <int Q>
+    __device__ static __forceinline__ real decode(double v, int q) { return v; }
+    template <int Q>
     __device__ static __forceinline__ double pack(real f, int q) { return f; }
 };
 
@@ -102,6 +104,8 @@ template <> struct Store<float> {
     static constexpr bool offset = true;
     template <int Q>
     __device__ static __forceinline__ real load(const float* p, int q) { return __ldg(p); }
+    template <int Q>
+    __device__ static __forceinline__ real decode(float v, int q) { return v; }
     template <int Q>
     __device__ static __forceinline__ float pack(real d, int q) { return d; }
 };
@@ -115,6 +119,10 @@ template <> struct Store<__half> {
         return __half2float(__ldg(p)) * ((float)Lat<Q>::w(q) * (1.0f / S));
     }
     template <int Q>
+    __device__ static __forceinline__ real decode(__half v, int q) {
+        return __half2float(v) * ((float)Lat<Q>::w(q) * (1.0f / S));
+    }
+    template <int Q>
     __device__ static __forceinline__ __half pack(real d, int q) {
         return __float2half_rn(d * (S / (float)Lat<Q>::w(q)));
     }
@@ -126,6 +134,10 @@ template <> struct Store<__nv_bfloat16> {
     template <int Q>
     __device__ static __forceinline__ real load(const __nv_bfloat16* p, int q) {
         return __bfloat162float(__ldg(p)) * (float)Lat<Q>::w(q);
+    }
+    template <int Q>
+    __device__ static __forceinline__ real decode(__nv_bfloat16 v, int q) {
+        return __bfloat162float(v) * (float)Lat<Q>::w(q);
     }
     template <int Q>
     __device__ static __forceinline__ __nv_bfloat16 pack(real d, int q) {

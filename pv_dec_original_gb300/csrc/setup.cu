@@ -396,7 +396,8 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     SETUP_CHECK(cudaMallocAsync(&out.act_idx, sizeof(int32_t) * npts, st));
     SETUP_CHECK(cudaMallocAsync(&out.act_pt, sizeof(int64_t) * (out.nact + 1), st));
     SETUP_CHECK(cudaMallocAsync(&out.act_word, sizeof(uint64_t) * (out.nact + 1), st));
-    SETUP_CHECK(cudaMallocAsync(&out.sp_of_act, sizeof(int32_t) * (out.nact + 1), st));
+    // padded: the tiled step kernel copies whole 16-byte groups
+    SETUP_CHECK(cudaMallocAsync(&out.sp_of_act, sizeof(int32_t) * (out.nact + 4), st));
     if (Q == 19)
         k_active_index<19><<<blocks(npts), 256, 0, st>>>(aflag, apos, flag, pos, out.cls, nx, ny, nz, d_seg_of_act,
                                                          out.act_idx, out.act_pt, out.act_word, out.sp_of_act);

@@ -459,74 +459,21 @@ __device__ __forceinline__ uint32_t word_miss(uint64_t w) { return (uint32_t)((w
 __device__ __forceinline__ int word_class(uint64_t w) { return (int)((w >> 59) & 0xfull); }
 __device__ __forceinline__ bool word_nw(uint64_t w) { return (w >> 63) & 1ull; }
 
-// One node's update: pull, boundary rules, wall shear stress, collision and
-// store (or the read-out sums).
+// After the pull: boundary rules, wall shear stress, collision and store
+// (or the read-out sums) of node a with post-stream populations g.  nr and
+// slot: the next-to-wall normal and stress-ring slot (FP32 formats).
 template <int Q, typename S, int MODE, int KIND, bool WIDE>
-__device__ __forceinline__ void node_update(const StepParams& P, const int64_t a, const uint64_t word,
-                                            const int32_t sp_entry, double (&part)[kPartialStride]) {
+__device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a, const uint64_t word,
+                                            const int64_t s, const bool lng, const int c, const uint32_t miss,
+                                            typename Store<S>::real (&g)[Q], const float (&nr)[3], const int slot,
+                                            double (&part)[kPartialStride]) {
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
     using R = typename Store<S>::real;
     constexpr bool OFF = Store<S>::offset;
-    constexpr int DR = kDeltaRow<Q>;
-    const S* __restrict__ fin = static_cast<const S*>(P.fin);
     S* __restrict__ fout = static_cast<S*>(P.fout);
     const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
     constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
-    const uint32_t miss = word_miss(word);  // zero on interior nodes
-    const int c = word_class(word);
-    // Boundary-list work: in parity mode every boundary-list node (history
-    // of missing links, the wall rule); in physics mode only
-    // boundary-condition and next-to-wall nodes (bounce-back is folded
-    // into the loads).  The list entry is fetched before the loads.
-    const bool lng = MODE == MODE_PARITY ? word_special(word) : (c >= CLS_BC0 || word_nw(word));
-    const int64_t s = lng ? (int64_t)sp_entry : 0;
-    // FP32 formats: a next-to-wall node loads its normal now, beside the
-    // populations, so the stress below waits on nothing
-    float nr[3] = {0.f, 0.f, 0.f};
-    int slot = 0;
-    if constexpr (OFF && KIND == KIND_STEP) {
-        if (lng && s < P.nnw) {
-            nr[0] = __ldg(P.nw_nf + s);
-            nr[1] = __ldg(P.nw_nf + P.nnw + s);
-            nr[2] = __ldg(P.nw_nf + 2 * P.nnw + s);
-            slot = (int)(*P.step_base % kRingSlots);
-        }
-    }
-
-    // ---- stream: one load per population, issued by every lane together.
-    // A link whose source is missing reads, in physics mode, the node's
-    // own opposite population (half-way bounce-back); in parity mode any
-    // valid address -- the previous value replaces it below.
     const I ai = (I)a, st = (I)P.stride;
-    // the node's own entry of plane 0; plane q is q * stride further
-    const S* __restrict__ fin_a = fin + ai;
-    R g[Q];
-    if (direct) {
-#pragma unroll
-        for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin_a + q * st, q);
-    } else {
-        int32_t dl[DR];
-        const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
-#pragma unroll
-        for (int k = 0; k < DR / 4; ++k) {
-            const int4 v = __ldg(drow + k);
-            dl[4 * k] = v.x; dl[4 * k + 1] = v.y; dl[4 * k + 2] = v.z; dl[4 * k + 3] = v.w;
-        }
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const bool src_missing = (miss >> Lat<Q>::opp(q)) & 1u;
-            I off;  // from the node's own entry of plane 0
-            if (q == Lat<Q>::REST) {
-                off = q * st;
-            } else if (MODE == MODE_PHYSICS) {
-                off = src_missing ? Lat<Q>::opp(q) * st : q * st + dl[q];
-            } else {
-                off = q * st + (src_missing ? 0 : dl[q]);
-            }
-            g[q] = Store<S>::template load<Q>(fin_a + off, q);  // w_opp(q) == w_q: same decode
-        }
-    }
-
     int nw = -1;  // next-to-wall index: boundary-list entries below nnw
     if (lng) {
         // ---- boundary-list node: history, boundary rules
@@ -660,6 +607,77 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
     }
 }
 
+// One node's update: pull, boundary rules, wall shear stress, collision and
+// store (or the read-out sums).
+template <int Q, typename S, int MODE, int KIND, bool WIDE>
+__device__ __forceinline__ void node_update(const StepParams& P, const int64_t a, const uint64_t word,
+                                            const int32_t sp_entry, double (&part)[kPartialStride]) {
+    using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
+    using R = typename Store<S>::real;
+    constexpr bool OFF = Store<S>::offset;
+    constexpr int DR = kDeltaRow<Q>;
+    const S* __restrict__ fin = static_cast<const S*>(P.fin);
+    S* __restrict__ fout = static_cast<S*>(P.fout);
+    const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
+    constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
+    const uint32_t miss = word_miss(word);  // zero on interior nodes
+    const int c = word_class(word);
+    // Boundary-list work: in parity mode every boundary-list node (history
+    // of missing links, the wall rule); in physics mode only
+    // boundary-condition and next-to-wall nodes (bounce-back is folded
+    // into the loads).  The list entry is fetched before the loads.
+    const bool lng = MODE == MODE_PARITY ? word_special(word) : (c >= CLS_BC0 || word_nw(word));
+    const int64_t s = lng ? (int64_t)sp_entry : 0;
+    // FP32 formats: a next-to-wall node loads its normal now, beside the
+    // populations, so the stress below waits on nothing
+    float nr[3] = {0.f, 0.f, 0.f};
+    int slot = 0;
+    if constexpr (OFF && KIND == KIND_STEP) {
+        if (lng && s < P.nnw) {
+            nr[0] = __ldg(P.nw_nf + s);
+            nr[1] = __ldg(P.nw_nf + P.nw_stride + s);
+            nr[2] = __ldg(P.nw_nf + 2 * P.nw_stride + s);
+            slot = (int)(*P.step_base % kRingSlots);
+        }
+    }
+
+    // ---- stream: one load per population, issued by every lane together.
+    // A link whose source is missing reads, in physics mode, the node's
+    // own opposite population (half-way bounce-back); in parity mode any
+    // valid address -- the previous value replaces it below.
+    const I ai = (I)a, st = (I)P.stride;
+    // the node's own entry of plane 0; plane q is q * stride further
+    const S* __restrict__ fin_a = fin + ai;
+    R g[Q];
+    if (direct) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin_a + q * st, q);
+    } else {
+        int32_t dl[DR];
+        const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
+#pragma unroll
+        for (int k = 0; k < DR / 4; ++k) {
+            const int4 v = __ldg(drow + k);
+            dl[4 * k] = v.x; dl[4 * k + 1] = v.y; dl[4 * k + 2] = v.z; dl[4 * k + 3] = v.w;
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const bool src_missing = (miss >> Lat<Q>::opp(q)) & 1u;
+            I off;  // from the node's own entry of plane 0
+            if (q == Lat<Q>::REST) {
+                off = q * st;
+            } else if (MODE == MODE_PHYSICS) {
+                off = src_missing ? Lat<Q>::opp(q) * st : q * st + dl[q];
+            } else {
+                off = q * st + (src_missing ? 0 : dl[q]);
+            }
+            g[q] = Store<S>::template load<Q>(fin_a + off, q);  // w_opp(q) == w_q: same decode
+        }
+    }
+
+    node_finish<Q, S, MODE, KIND, WIDE>(P, a, word, s, lng, c, miss, g, nr, slot, part);
+}
+
 // WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
 // lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
 // One thread per active node.
@@ -708,6 +726,227 @@ cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Tiled step.  A tile is kTileNodes consecutive active nodes; in active-index
+// order the pull sources of a tile's nodes for population q lie in one
+// contiguous window of plane q (measured on the bifurcation: about the tile's
+// own size), so one bulk copy per plane (cp.async.bulk, the TMA engine)
+// stages all of them in shared memory, with the tile's own entries of every
+// plane (bounce-back reads them), its node words, boundary-list entries,
+// delta rows and next-to-wall normals.  Persistent CTAs of kTileNodes
+// threads loop over tiles; an mbarrier per stage tracks the copies, NS
+// stages deep, so a tile's loads fly while earlier tiles compute.  Every
+// wait is bounded: a copy that does not land raises FLAG_TIMEOUT, the CTA
+// waits (bounded) for what it issued and returns.
+
+constexpr int64_t kWaitLimit = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// false when the phase did not complete within the limit
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int64_t k = 0; k < kWaitLimit; ++k)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Issue every copy of tile t into one stage (one thread).  Sizes and
+// alignments come from the plan: windows start and end on 16-byte
+// boundaries inside their planes.
+template <int Q, typename S>
+__device__ __forceinline__ void tile_issue(const StepParams& P, int64_t t, unsigned char* sb, uint64_t* bar) {
+    constexpr int T = kTileNodes, DR = kDeltaRow<Q>;
+    const TileGeom& G = P.tile;
+    const int32_t* pl = P.tile_plan + t * (2 * Q + kTilePlanExtra);
+    const S* fin = static_cast<const S*>(P.fin);
+    int32_t* hdr = reinterpret_cast<int32_t*>(sb + G.off_hdr);
+    const int64_t t0 = t * T;
+    const int nt = (int)(P.nact - t0 < T ? P.nact - t0 : T);
+    const int nown = (int)(P.stride - t0 < T ? P.stride - t0 : T);
+    const int seg0 = pl[2 * Q], nseg = pl[2 * Q + 1], nw0 = pl[2 * Q + 2], nwl = pl[2 * Q + 3];
+    const int nword = (nt + 1) & ~1, nsp = (nt + 3) & ~3;
+    uint32_t bytes = (uint32_t)(Q * nown * (int)sizeof(S) + nword * 8 + nsp * 4 + nseg * DR * 4 + 3 * nwl * 4);
+    for (int q = 0; q < Q; ++q) {
+        hdr[q] = pl[q];
+        bytes += (uint32_t)(pl[Q + q] * (int)sizeof(S));
+    }
+    hdr[Q] = seg0;
+    hdr[Q + 1] = nseg;
+    hdr[Q + 2] = nw0;
+    // the previous tile's reads of this stage (generic proxy) before the
+    // copies (async proxy) overwrite it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_tx(bar, bytes);
+    S* pull = reinterpret_cast<S*>(sb + G.off_pull);
+    S* own = reinterpret_cast<S*>(sb + G.off_own);
+    for (int q = 0; q < Q; ++q) {
+        if (pl[Q + q] > 0)
+            bulk_load(pull + (int64_t)q * G.wcap, fin + (int64_t)q * P.stride + pl[q], (uint32_t)(pl[Q + q] * sizeof(S)),
+                      bar);
+        bulk_load(own + q * T, fin + (int64_t)q * P.stride + t0, (uint32_t)(nown * sizeof(S)), bar);
+    }
+    bulk_load(sb + G.off_word, P.act_word + t0, (uint32_t)(nword * 8), bar);
+    bulk_load(sb + G.off_sp, P.sp_of_act + t0, (uint32_t)(nsp * 4), bar);
+    if (nseg > 0) bulk_load(sb + G.off_delta, P.seg_delta + (int64_t)seg0 * DR, (uint32_t)(nseg * DR * 4), bar);
+    if (nwl > 0)
+        for (int k = 0; k < 3; ++k)
+            bulk_load(sb + G.off_nrm + k * G.nwcap * 4, P.nw_nf + k * P.nw_stride + nw0, (uint32_t)(nwl * 4), bar);
+}
+
+// Physics mode, FP32-arithmetic formats, 32-bit offsets.
+template <int Q, typename S, int NS>
+__global__ void __launch_bounds__(kTileNodes, 1) tile_step_kernel(const StepParams P) {
+    using R = typename Store<S>::real;
+    constexpr int T = kTileNodes, DR = kDeltaRow<Q>;
+    const TileGeom& G = P.tile;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NS * G.stage_bytes);
+    const int tid = threadIdx.x;
+    const int64_t grid = gridDim.x;
+    int issued[NS], used[NS];  // phases issued / consumed per stage (thread 0 issues)
+#pragma unroll
+    for (int k = 0; k < NS; ++k) issued[k] = used[k] = 0;
+    if (tid == 0) {
+        for (int k = 0; k < NS; ++k) mbar_init(&bar[k], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int k = 0; k < NS - 1; ++k) {
+            const int64_t t = blockIdx.x + k * grid;
+            if (t < G.ntiles) {
+                tile_issue<Q, S>(P, t, smem + k * G.stage_bytes, &bar[k]);
+                ++issued[k];
+            }
+        }
+    double part[kPartialStride];
+    bool failed = false;
+    int it = 0;
+    for (int64_t t = blockIdx.x; t < G.ntiles; t += grid, ++it) {
+        const int stg = it % NS;
+        if (tid == 0) {
+            const int64_t tn = t + (int64_t)(NS - 1) * grid;
+            const int sn = (it + NS - 1) % NS;
+            if (tn < G.ntiles) {
+                tile_issue<Q, S>(P, tn, smem + sn * G.stage_bytes, &bar[sn]);
+                ++issued[sn];
+            }
+        }
+        const bool ok = mbar_wait(&bar[stg], (uint32_t)(used[stg] & 1));
+        ++used[stg];
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        const unsigned char* sb = smem + stg * G.stage_bytes;
+        const int32_t* hdr = reinterpret_cast<const int32_t*>(sb + G.off_hdr);
+        const int64_t a = t * T + tid;
+        if (a < P.nact) {
+            const uint64_t word = reinterpret_cast<const uint64_t*>(sb + G.off_word)[tid];
+            const int32_t sp_entry = reinterpret_cast<const int32_t*>(sb + G.off_sp)[tid];
+            const uint32_t miss = word_miss(word);
+            const int c = word_class(word);
+            const bool lng = c >= CLS_BC0 || word_nw(word);
+            const int64_t s = lng ? (int64_t)sp_entry : 0;
+            float nr[3] = {0.f, 0.f, 0.f};
+            int slot = 0;
+            if (lng && s < P.nnw) {
+                const float* nrm = reinterpret_cast<const float*>(sb + G.off_nrm);
+                const int k = (int)(s - hdr[Q + 2]);
+                nr[0] = nrm[k];
+                nr[1] = nrm[G.nwcap + k];
+                nr[2] = nrm[2 * G.nwcap + k];
+                slot = (int)(*P.step_base % kRingSlots);
+            }
+            int32_t dl[DR];
+            const int64_t rs = word_segment(word) - hdr[Q];
+            const int4* drow = (rs >= 0 && rs < hdr[Q + 1])
+                                   ? reinterpret_cast<const int4*>(sb + G.off_delta) + rs * (DR / 4)
+                                   : reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
+#pragma unroll
+            for (int k = 0; k < DR / 4; ++k) {
+                const int4 v = drow[k];
+                dl[4 * k] = v.x; dl[4 * k + 1] = v.y; dl[4 * k + 2] = v.z; dl[4 * k + 3] = v.w;
+            }
+            const S* pull = reinterpret_cast<const S*>(sb + G.off_pull);
+            const S* own = reinterpret_cast<const S*>(sb + G.off_own);
+            R g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                S v;
+                if (q == Lat<Q>::REST) v = own[q * T + tid];
+                else if ((miss >> Lat<Q>::opp(q)) & 1u) v = own[Lat<Q>::opp(q) * T + tid];
+                else v = pull[q * G.wcap + (int)(a + dl[q] - hdr[q])];
+                g[q] = Store<S>::template decode<Q>(v, q);
+            }
+            node_finish<Q, S, MODE_PHYSICS, KIND_STEP, false>(P, a, word, s, lng, c, miss, g, nr, slot, part);
+        }
+        __syncthreads();
+    }
+    if (failed) {
+        if (tid == 0) {
+            atomicOr(P.flags, FLAG_TIMEOUT);
+            // wait, bounded, for the copies this CTA still has in flight
+            for (int k = 0; k < NS; ++k)
+                for (; used[k] < issued[k]; ++used[k])
+                    if (!mbar_wait(&bar[k], (uint32_t)(used[k] & 1))) break;
+        }
+        __syncthreads();
+        return;
+    }
+    if (blockIdx.x == 0 && tid == 0) *P.step_next = *P.step_base + 1;
+}
+
+template <int Q, typename S, int NS>
+cudaError_t launch_tile_ns(const StepParams& p, cudaStream_t st) {
+    static int attr_bytes = 0;  // per instantiation: opt-in shared memory set so far
+    if (p.tile.smem_bytes > attr_bytes) {
+        cudaError_t e = cudaFuncSetAttribute(tile_step_kernel<Q, S, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             p.tile.smem_bytes);
+        if (e != cudaSuccess) return e;
+        attr_bytes = p.tile.smem_bytes;
+    }
+    int dev = 0, nsm = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
+                                                   cudaSuccess || nsm <= 0)
+        nsm = 1;
+    int64_t grid = (int64_t)nsm * p.tile.ctas_per_sm;
+    if (grid > p.tile.ntiles) grid = p.tile.ntiles;
+    tile_step_kernel<Q, S, NS><<<(unsigned)grid, kTileNodes, p.tile.smem_bytes, st>>>(p);
+    return cudaGetLastError();
+}
+
+template <int Q, typename S>
+cudaError_t launch_tile(const StepParams& p, cudaStream_t st) {
+    return p.tile.nstage == 3 ? launch_tile_ns<Q, S, 3>(p, st) : launch_tile_ns<Q, S, 2>(p, st);
+}
+
 template <int Q, typename S, int MODE>
 cudaError_t launch_family(int kind, int variant, const StepParams& p, cudaStream_t st) {
     if (kind == KIND_STEP) {
@@ -716,6 +955,14 @@ cudaError_t launch_family(int kind, int variant, const StepParams& p, cudaStream
             case 2: return launch_step_variant<Q, S, MODE, 2>(p, st);
             case 3: return launch_step_variant<Q, S, MODE, 3>(p, st);
             case 4: return launch_step_variant<Q, S, MODE, 4>(p, st);
+            case 5:
+                // the tiled kernel where a plan exists (physics, FP32-arithmetic
+                // formats, 32-bit offsets); the default shape elsewhere
+                if constexpr (Store<S>::offset && MODE == MODE_PHYSICS) {
+                    if (p.tile.ntiles > 0 && p.tile_plan && (int64_t)Q * p.stride < ((int64_t)1 << 31))
+                        return launch_tile<Q, S>(p, st);
+                }
+                return launch_step_variant<Q, S, MODE, Store<S>::offset ? 0 : 4>(p, st);
             default: return launch_step_variant<Q, S, MODE, 0>(p, st);
         }
     }
