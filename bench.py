@@ -215,6 +215,75 @@ def time_steps(cr, s, steps, flush, stream):
     return ms
 
 
+def d3q27_extra(capi, cr, mask, surf, tri, origin, device, flush, steps):
+    """D3Q27 on the same bifurcation: FP32 and FP16 storage, per-step CUDA
+    events with the L2 flushed between steps (as the headline)."""
+    out = {}
+    for prec in ("f32", "f16"):
+        s, _ = make_solver(capi, mask, surf, tri, 27, prec, origin, device)
+        s.step(5)
+        best, _ = s.autotune(5)
+        ms = time_steps(cr, s, steps, flush, s.stream())
+        m = sum(ms) / len(ms)
+        act = s.counts()["active"]
+        out[prec] = {"mlups": act / (m * 1e-3) / 1e6, "ms_per_step": m, "variant": best,
+                     "hbm_gbs": act * BYTES_PER_LU[(27, prec)] / (m * 1e-3) / 1e9}
+        s.close()
+    return out
+
+
+def precision_extra(capi, cr, device, steps=1200, timed=200):
+    """The precision configuration: the bifurcation (parent r=24, daughters
+    r=17) in a 384x288x768 lattice, D3Q19 BGK physics, pulsatile inlet;
+    FP32, FP16-scaled and BF16 offset storage against an FP64 run of the same
+    case on the GPU after `steps` steps (BGK at tau=0.55 stays stable for
+    about 2000 steps on this lattice, FP64 included): velocity L2 relative
+    error, relative error of the pressure drop (mean density on the inlet
+    plane minus the outlet plane, over 3), TAWSS L2 relative error; MLUPS of
+    each format (events around `timed` graph-replayed steps; the populations
+    exceed L2)."""
+    from pv_dec_original_gb300 import geometry as G
+    surf = G.config_c2_bifurcation(lattice=(384, 288, 768))
+    tri = surf.tri12()
+    mask, desc = capi.voxelize(tri, 1.0)
+    bb = np.array(desc.bbox[:])
+    origin = (bb[0], bb[2], bb[4])
+    fl = np.argwhere(mask > 0)
+    res = {}
+    ref = None
+    for prec in ("f64", "f32", "f16", "bf16"):
+        s, (kin, kout) = make_solver(capi, mask, surf, tri, 19, prec, origin, device)
+        if prec != "f64":
+            s.autotune(3)
+        s.set_graph_steps(100)
+        s.step(steps)
+        rho, u = s.macro()
+        tawss = s.wss()["tawss"]
+        drop = (rho[fl[:, 0] == kin].mean() - rho[fl[:, 0] == kout].mean()) / 3.0
+        st = s.stream()
+        a, b = cr.event(), cr.event()
+        cr.record(a, st)
+        s.step_async(timed)
+        cr.record(b, st)
+        ms = cr.elapsed_ms(a, b) / timed
+        s.check_status()
+        act = s.counts()["active"]
+        row = {"mlups": act / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+               "hbm_gbs": act * BYTES_PER_LU[(19, prec)] / (ms * 1e-3) / 1e9}
+        if ref is None:
+            ref = (u, drop, tawss)
+        else:
+            row["u_l2_rel"] = float(np.linalg.norm(u - ref[0]) / np.linalg.norm(ref[0]))
+            row["pressure_drop_rel"] = float(abs(drop - ref[1]) / abs(ref[1]))
+            row["tawss_l2_rel"] = float(np.linalg.norm(tawss - ref[2]) / np.linalg.norm(ref[2]))
+        res[prec] = row
+        s.close()
+    for prec in ("f16", "bf16"):
+        res[prec]["speedup_vs_f32"] = res[prec]["mlups"] / res["f32"]["mlups"]
+    return {"lattice": [384, 288, 768], "active_nodes": int(len(fl)), "steps": steps, "tau": TAU,
+            "reference": "FP64 run of the same case on the GPU (physics mode)", "formats": res}
+
+
 def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
     """Aggregate MLUPS of the C4 ensemble packed into one lattice (captured
     graph, one step-kernel launch per step) against the same members as
@@ -476,6 +545,10 @@ def run_ours(args):
 
     # batched ensemble (64 seeded stenosed tubes, FP16 storage): one packed
     # lattice, one launch per step, vs the same members as 64 lattices
+    if not args.quick and args.Q == 19:
+        extra["d3q27"] = d3q27_extra(capi, cr, mask, surf, tri, origin, local, flush, args.steps)
+    if not args.quick and not args.no_precision:
+        extra["precision_c3"] = precision_extra(capi, cr, local)
     if not args.quick and not args.no_ensemble:
         extra["ensemble_c4"] = ensemble_extra(capi, cr, local, args.Q)
     if not args.quick and not args.no_warmstart:
@@ -619,6 +692,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the secondary FP16 and ensemble measurements")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurement")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 384x288x768 precision measurement")
     ap.add_argument("--no-warmstart", action="store_true", help="skip the learned warm-start measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--variant", type=int, default=None, help="force a launch shape (skips the autotuner)")
