@@ -81,6 +81,9 @@ typedef int lbm_status;
 /* Boundary-condition rules per handle (an ensemble packs one inlet and one
  * outlet rule per member into one lattice). */
 #define LBM_MAX_BC 256
+
+#define LBM_COLLISION_BGK 0
+#define LBM_COLLISION_REGULARIZED 1
 /* Inlet waveforms per handle (lbm_set_waveform). */
 #define LBM_MAX_WAVES 256
 
@@ -126,6 +129,12 @@ typedef struct {
     double wss_scale;  /* C of the wall shear stress (reference: 1060*dt^2/(s^2*1e-6)) */
     double tawss_div;  /* TAWSS = accumulated |tau| / tawss_div (reference: 0.9) */
     int device;        /* CUDA device ordinal */
+    /* Physics mode: LBM_COLLISION_BGK (the reference's, Simulation.cpp:96-261)
+     * or LBM_COLLISION_REGULARIZED (no reference counterpart: the
+     * non-equilibrium part is projected on its second moment before
+     * relaxing, which keeps flows stable at tau near 1/2 where BGK diverges).
+     * Parity mode is always BGK. */
+    int collision;
 } lbm_desc;
 
 lbm_status lbm_create(const lbm_desc* desc, lbm_handle** out);

@@ -337,6 +337,7 @@ struct oracle_sim {
     double *nw_n, *wall_n, *wss, *acc, *accm, *osi, *tawss;
     oracle_bc bc[16];
     int nbc;
+    int regularized;   /* physics mode: regularized collision instead of BGK */
     double* amp;
     int64_t namp, step;
     double C, tawss_div;
@@ -652,6 +653,31 @@ static void wss_ref(int Q, const double* f, const double* feq, const double* n, 
     }
 }
 
+/* Regularized collision (physics mode, no reference counterpart: the
+ * reference is BGK): f* = feq + (1 - 1/tau) f1, with the non-equilibrium part
+ * projected on its second moment, f1_q = w_q / (2 cs^4) (c_q c_q - cs^2 I) : Pi,
+ * Pi = sum_q (f_q - feq_q) c_q c_q, cs^2 = 1/3.  Written from the definition
+ * (a direct sum over directions), so it checks the device kernel's analytic
+ * form of Pi. */
+static void regularize_node(int Q, double tau, const double* f, double* fnew, const double* feq) {
+    double P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int q = 0; q < Q; ++q) {
+        const int* c = cvec(Q, q);
+        double fne = f[q] - feq[q];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) P[a][b] += fne * c[a] * c[b];
+    }
+    for (int q = 0; q < Q; ++q) {
+        const int* c = cvec(Q, q);
+        double qp = 0.0;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) qp += (c[a] * c[b] - (a == b ? 1.0 / 3.0 : 0.0)) * P[a][b];
+        fnew[q] = feq[q] + (1.0 - 1.0 / tau) * weight(Q, q) * 4.5 * qp;
+    }
+}
+
+void oracle_sim_set_collision(oracle_sim* s, int regularized) { s->regularized = regularized; }
+
 /* Library physics semantics: traction of the viscous stress
  * -(1 - 1/(2 tau)) sum_a f_neq c c, projected on the wall plane; f_neq from
  * the same post-boundary f (no time lag). */
@@ -683,8 +709,11 @@ void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads) {
         double amp = s->amp[s->step % s->namp];
         /* collide */
 #pragma omp parallel for schedule(static)
-        for (int64_t a = 0; a < na; ++a)
+        for (int64_t a = 0; a < na; ++a) {
             collide_node(Q, s->tau, s->f + a * Q, s->fnew + a * Q, s->feq + a * Q, s->rho + a, s->u + 3 * a);
+            if (s->mode == ORC_PHYSICS && s->regularized)
+                regularize_node(Q, s->tau, s->f + a * Q, s->fnew + a * Q, s->feq + a * Q);
+        }
         /* stream */
         if (s->mode == ORC_PARITY) {
             /* push; a destination keeps its value when the link is missing or

@@ -70,6 +70,8 @@ void oracle_sim_set_wss(oracle_sim* s, double C, double tawss_div);
 /* Wall and next-to-wall normals from the surface (Subdomain.cpp:224-370). */
 void oracle_sim_compute_normals(oracle_sim* s, const double* tri12, int64_t ntri, int nthreads);
 void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads);
+/* Physics mode: regularized collision (1) instead of BGK (0, default). */
+void oracle_sim_set_collision(oracle_sim* s, int regularized);
 
 int64_t oracle_sim_nactive(const oracle_sim* s);
 int64_t oracle_sim_nnw(const oracle_sim* s);

@@ -60,6 +60,7 @@ def lib():
         L.oracle_sim_set_wss.argtypes = [C.c_void_p, C.c_double, C.c_double]
         L.oracle_sim_compute_normals.argtypes = [C.c_void_p, P(d), C.c_int64, C.c_int]
         L.oracle_sim_step.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.oracle_sim_set_collision.argtypes = [C.c_void_p, C.c_int]
         L.oracle_sim_nactive.argtypes = [C.c_void_p]
         L.oracle_sim_nactive.restype = C.c_int64
         L.oracle_sim_nnw.argtypes = [C.c_void_p]
@@ -153,6 +154,10 @@ class Sim:
 
     def step(self, n=1, nthreads=0):
         lib().oracle_sim_step(self.h, n, nthreads)
+
+    def set_collision(self, regularized):
+        """Physics mode: regularized collision (True) or BGK (False)."""
+        lib().oracle_sim_set_collision(self.h, int(bool(regularized)))
 
     @property
     def nactive(self):

@@ -19,6 +19,8 @@ LBM_BC_REF_INLET, LBM_BC_REF_OUTLET_YMAX, LBM_BC_REF_OUTLET_ZMIN, LBM_BC_VELOCIT
 FACES = {"x-": 0, "x+": 1, "y-": 2, "y+": 3, "z-": 4, "z+": 5}
 PRECISIONS = {"f64": LBM_F64, "f32": LBM_F32, "f16": LBM_F16, "bf16": LBM_BF16}
 MAX_BC = 256
+LBM_COLLISION_BGK = 0
+LBM_COLLISION_REGULARIZED = 1
 MAX_WAVES = 256
 
 ERRORS = {-1: "LBM_ERR_ARG", -2: "LBM_ERR_CUDA", -3: "LBM_ERR_STATE", -4: "LBM_ERR_NONFINITE",
@@ -40,7 +42,7 @@ class VoxDesc(C.Structure):
 class Desc(C.Structure):
     _fields_ = [("Q", C.c_int), ("precision", C.c_int), ("mode", C.c_int), ("tau", C.c_double),
                 ("spacing", C.c_double), ("origin", C.c_double * 3), ("wss_scale", C.c_double),
-                ("tawss_div", C.c_double), ("device", C.c_int)]
+                ("tawss_div", C.c_double), ("device", C.c_int), ("collision", C.c_int)]
 
 
 class BCSpec(C.Structure):
@@ -198,11 +200,12 @@ class Solver:
     """One device-resident lattice behind the C ABI."""
 
     def __init__(self, Q=19, precision=LBM_F32, mode=LBM_PHYSICS, tau=0.8, spacing=1.0, origin=(0.0, 0.0, 0.0),
-                 wss_scale=1.0, tawss_div=0.9, device=0):
+                 wss_scale=1.0, tawss_div=0.9, device=0, collision=0):
         L = load()
         if isinstance(precision, str):
             precision = PRECISIONS[precision]
-        d = Desc(Q, precision, mode, tau, spacing, (C.c_double * 3)(*origin), wss_scale, tawss_div, device)
+        d = Desc(Q, precision, mode, tau, spacing, (C.c_double * 3)(*origin), wss_scale, tawss_div, device,
+                 collision)
         h = C.c_void_p()
         _check(L.lbm_create(C.byref(d), C.byref(h)))
         self.h = h

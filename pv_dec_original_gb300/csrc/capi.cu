@@ -239,6 +239,7 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.nw_accf = h->nw_accf;
     p.nw_prev = h->nw_prev;
     p.tau = h->d.tau;
+    p.collision = h->d.mode == LBM_PHYSICS ? h->d.collision : LBM_COLLISION_BGK;
     p.wss_C = h->d.wss_scale;
     p.inv_tau = 1.0 / h->d.tau;
     p.inv_tau_f = (float)p.inv_tau;
@@ -688,6 +689,8 @@ lbm_status lbm_create(const lbm_desc* desc, lbm_handle** out) {
     if (elem_size(desc->precision) == 0) return fail(nullptr, LBM_ERR_ARG, "unknown precision");
     if (desc->mode != LBM_PARITY && desc->mode != LBM_PHYSICS) return fail(nullptr, LBM_ERR_ARG, "unknown mode");
     if (!(desc->tau > 0.5)) return fail(nullptr, LBM_ERR_ARG, "tau must be > 0.5 (BGK stability)");
+    if (desc->collision != LBM_COLLISION_BGK && desc->collision != LBM_COLLISION_REGULARIZED)
+        return fail(nullptr, LBM_ERR_ARG, "collision must be LBM_COLLISION_BGK or LBM_COLLISION_REGULARIZED");
     if (!(desc->spacing > 0)) return fail(nullptr, LBM_ERR_ARG, "spacing must be > 0");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);

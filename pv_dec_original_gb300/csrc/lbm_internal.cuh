@@ -83,6 +83,7 @@ struct StepParams {
     float2* nw_accf;          // [4][nnw]
     void* nw_prev;            // parity: rho, ux, uy, uz of the previous collision, [4][nnw]
     double tau;
+    int collision;             // LBM_COLLISION_* (physics mode)
     double wss_C;
     // scalars derived on the host: FP64 arithmetic is slow on GB300, so no
     // thread recomputes them

@@ -167,13 +167,13 @@ __device__ __forceinline__ void relax_pairs(float (&f)[Q], float A, float B, flo
 
 // Second moments sum_q d_q c_qa c_qb (xx, yy, zz, xy, xz, yz) from the
 // pair sums d_q + d_opp(q): c c^T is even in c.
-template <int Q, int q = 0>
-__device__ __forceinline__ void second_moments(const float (&d)[Q], float (&m)[6]) {
+template <int Q, int q = 0, typename R>
+__device__ __forceinline__ void second_moments(const R (&d)[Q], R (&m)[6]) {
     if constexpr (q < Q) {
         constexpr int o = Lat<Q>::opp(q);
         if constexpr (q < o) {
             constexpr int cx = Lat<Q>::cx(q), cy = Lat<Q>::cy(q), cz = Lat<Q>::cz(q);
-            const float p = d[q] + d[o];
+            const R p = d[q] + d[o];
             m[0] = cadd<cx * cx>(m[0], p);
             m[1] = cadd<cy * cy>(m[1], p);
             m[2] = cadd<cz * cz>(m[2], p);
@@ -181,8 +181,58 @@ __device__ __forceinline__ void second_moments(const float (&d)[Q], float (&m)[6
             m[4] = cadd<cx * cz>(m[4], p);
             m[5] = cadd<cy * cz>(m[5], p);
         }
-        second_moments<Q, q + 1>(d, m);
+        second_moments<Q, q + 1, R>(d, m);
     }
+}
+
+// Regularized collision (physics mode): the non-equilibrium part is replaced
+// by its projection on the second moment,
+//   f*_q = feq_q + (1 - omega) w_q 4.5 (c_q.Pi.c_q - tr Pi / 3),
+//   Pi = sum_q (f_q - feq_q) c_q c_q = M - r/3 I - A u u,
+// with M the second moment of the stored values (offsets d = f - w, or full
+// f) and, as in relax_pairs, A = 1 + r and B = r - 1.5 A u^2 for offsets
+// (A = rho for full f: both give feq - base = w (B + 4.5 A du^2 +|- 3 A du)).
+// Filtering the higher moments keeps flows stable at relaxation times near
+// 1/2 where BGK diverges.  kreg = 4.5 (1 - omega).
+template <int Q, typename R, int q = 0>
+__device__ __forceinline__ void relax_reg_pairs(R (&f)[Q], const R (&P)[6], R T3, R A, R B, R ux, R uy, R uz,
+                                                R kreg) {
+    if constexpr (q < Q) {
+        constexpr int o = Lat<Q>::opp(q);
+        constexpr int cx = Lat<Q>::cx(q), cy = Lat<Q>::cy(q), cz = Lat<Q>::cz(q);
+        if constexpr (q == Lat<Q>::REST) {
+            f[q] = (R)Lat<Q>::w(q) * (B - kreg * T3);
+        } else if constexpr (q < o) {
+            // c.Pi.c with c components in {0, +-1}
+            R cpc = R(0);
+            cpc = cx != 0 ? cpc + P[0] : cpc;
+            cpc = cy != 0 ? cpc + P[1] : cpc;
+            cpc = cz != 0 ? cpc + P[2] : cpc;
+            if constexpr (cx * cy != 0) cpc = cadd<cx * cy>(cadd<cx * cy>(cpc, P[3]), P[3]);
+            if constexpr (cx * cz != 0) cpc = cadd<cx * cz>(cadd<cx * cz>(cpc, P[4]), P[4]);
+            if constexpr (cy * cz != 0) cpc = cadd<cy * cz>(cadd<cy * cz>(cpc, P[5]), P[5]);
+            const R du = cdot<Q, q, R>(ux, uy, uz);
+            const R w = (R)Lat<Q>::w(q);
+            const R t = A * du;
+            const R e = w * ((R(4.5) * t) * du + B + kreg * (cpc - T3));
+            const R anti = (R(3.0) * w) * t;
+            f[q] = e + anti;
+            f[o] = e - anti;
+        }
+        relax_reg_pairs<Q, R, q + 1>(f, P, T3, A, B, ux, uy, uz, kreg);
+    }
+}
+
+template <int Q, typename R>
+__device__ __forceinline__ void relax_regularized(R (&f)[Q], R r, R A, R ux, R uy, R uz, R om) {
+    R m[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
+    second_moments<Q, 0, R>(f, m);
+    const R r3 = r * (R(1) / R(3));
+    const R P[6] = {m[0] - (r3 + A * ux * ux), m[1] - (r3 + A * uy * uy), m[2] - (r3 + A * uz * uz),
+                    m[3] - A * ux * uy,        m[4] - A * ux * uz,        m[5] - A * uy * uz};
+    const R T3 = (P[0] + P[1] + P[2]) * (R(1) / R(3));
+    const R B = r - R(1.5) * A * (ux * ux + uy * uy + uz * uz);
+    relax_reg_pairs<Q, R>(f, P, T3, A, B, ux, uy, uz, R(4.5) * (R(1) - om));
 }
 
 // Wall shear stress from the non-equilibrium stress tensor
@@ -592,7 +642,10 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
             }
         }
         // ---- collide and store (every lane)
-        if constexpr (OFF) {
+        if (MODE == MODE_PHYSICS && P.collision == LBM_COLLISION_REGULARIZED) {
+            if constexpr (OFF) relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f);
+            else relax_regularized<Q, R>(g, r, r, ux, uy, uz, (R)P.inv_tau);
+        } else if constexpr (OFF) {
             const float om = P.inv_tau_f;
             const float A = 1.0f + r;
             const float B = r - 1.5f * A * (ux * ux + uy * uy + uz * uz);
