@@ -348,12 +348,18 @@ def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
 
 
 def warmstart_extra(device, n_train=32, n_test=6, tau=0.55):
-    """Learned warm start (scaled-down C5: 64x32x64 grids instead of
-    128x128x256, 32 training vessels): train on the device, then steps and
-    wall time to residual 1e-6 from rest and from the prediction on held-out
-    vessels (FP64 lattices), prediction errors of the network and of the
-    Poiseuille prior it corrects, and the tensor-core convolution throughput
-    of one forward pass at the full C5 grid."""
+    """Learned warm start (scaled-down C5: 64x32x32 grids instead of
+    128x128x256, 32 training vessels): train on the device, then on held-out
+    vessels the steps and wall time until the wall shear stress of an FP32
+    lattice stays within 1% of the converged WSS (an FP64 lattice from rest
+    run to the residual 1e-6), for a start from rest, from the Poiseuille
+    prior alone and from the network's prediction (prior + learned
+    correction); wall time = prediction time (all on the device) + steps x
+    the lattice's measured time per step.  Beside it: the FP64 steps to the
+    residual 1e-6 from the network's start (capped at 4x the cold count),
+    the prediction errors of the network and of the prior, and the
+    tensor-core convolution throughput of one forward pass at the full C5
+    grid."""
     import torch
     from pv_dec_original_gb300 import warmstart as WS
     t0 = time.perf_counter()
@@ -368,27 +374,54 @@ def warmstart_extra(device, n_train=32, n_test=6, tau=0.55):
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     rows = []
+    dev = torch.device("cuda", device)
     for m in test_m:
-        sc, mask = WS.single_lattice(m, tau=tau, device=device)
+        # the judge's answer: an FP64 lattice from rest to the residual 1e-6
+        sr, mask = WS.single_lattice(m, tau=tau, precision="f64", device=device)
+        sr.set_graph_steps(100)
+        n64, r64 = WS.steps_to_converge(sr, tol=1e-6, max_steps=150000)
+        _, uc = sr.macro()
+        wc = sr.wss()["wss"]
+        sr.close()
+        # timed arms on FP32 lattices (the production storage)
+        sc, _ = WS.single_lattice(m, tau=tau, precision="f32", device=device)
         sc.set_graph_steps(100)
+        c1 = WS.steps_to_wss(sc, wc, 0.01, max_steps=150000)
         t0 = time.perf_counter()
-        nc, _ = WS.steps_to_converge(sc, tol=1e-6, max_steps=150000)
-        tc = time.perf_counter() - t0
-        rc, uc = sc.macro()
-        wc = sc.wss()["wss"]
-        t0 = time.perf_counter()
+        sc.step(2000)
+        t_step = (time.perf_counter() - t0) / 2000
+        sc.close()
+        arms = {}
+        for arm in ("prior", "net"):
+            sw, _ = WS.single_lattice(m, tau=tau, precision="f32", device=device)
+            sw.set_graph_steps(100)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            x, prior = WS.features(mask, m["inlet_mean"], m["period"], tau=tau, device=device)
+            y = net.forward(x) if arm == "net" else WS.zero_output(prior)
+            rho, u = WS.prediction_to_device(y, prior)
+            sw.init_from_macro_device(rho.data_ptr(), u.data_ptr(), True, torch.cuda.current_stream(dev).cuda_stream)
+            t_pred = time.perf_counter() - t0
+            w1 = WS.steps_to_wss(sw, wc, 0.01, max_steps=max(4 * (c1 or 0), 20000))
+            sw.close()
+            ua = u.cpu().numpy().reshape(-1, 3)
+            arms[arm] = {"steps_1pct_wss": w1, "s_1pct_wss": None if w1 is None else t_pred + w1 * t_step,
+                         "predict_s": t_pred, "err_u": float(np.linalg.norm(ua - uc) / np.linalg.norm(uc))}
+        # the residual criterion from the network's start, FP64 (capped at 4x the cold count)
+        s64, _ = WS.single_lattice(m, tau=tau, precision="f64", device=device)
+        s64.set_graph_steps(100)
         x, prior = WS.features(mask, m["inlet_mean"], m["period"], tau=tau, device=device)
-        rho, u = WS.prediction_to_macro(mask, net.forward(x), m["inlet_mean"], prior)
-        sw, _ = WS.single_lattice(m, tau=tau, device=device)
-        sw.set_graph_steps(100)
-        sw.init_from_macro(rho, u, True)
-        nw, _ = WS.steps_to_converge(sw, tol=1e-6, max_steps=150000)
-        tw = time.perf_counter() - t0
-        _, up = WS.prediction_to_macro(mask, torch.zeros(mask.size * WS.C_OUT), m["inlet_mean"], prior)
-        rows.append({"kind": m["kind"], "cold_steps": nc, "cold_s": tc, "warm_steps": nw, "warm_s": tw,
-                     "err_net": float(np.linalg.norm(u - uc) / np.linalg.norm(uc)),
-                     "err_prior": float(np.linalg.norm(up - uc) / np.linalg.norm(uc)),
-                     "wss_diff": float(np.linalg.norm(sw.wss()["wss"] - wc) / np.linalg.norm(wc))})
+        rho, u = WS.prediction_to_device(net.forward(x), prior)
+        s64.init_from_macro_device(rho.data_ptr(), u.data_ptr(), True, torch.cuda.current_stream(dev).cuda_stream)
+        nres, rres = WS.steps_to_converge(s64, tol=1e-6, max_steps=4 * n64)
+        arms["net"]["f64_steps_residual_1e-6"] = nres if rres < 1e-6 else None
+        arms["net"]["f64_final_residual"] = rres
+        arms["net"]["f64_wss_diff_at_end"] = WS.wss_error(s64.wss()["wss"], wc)
+        s64.close()
+        rows.append({"kind": m["kind"], "active": int(mask.sum()), "f32_us_per_step": t_step * 1e6,
+                     "cold": {"steps_1pct_wss": c1, "s_1pct_wss": None if c1 is None else c1 * t_step,
+                              "f64_steps_residual_1e-6": n64, "f64_final_residual": r64},
+                     **arms})
     # convolution throughput at the C5 grid (128x128x256), forward pass
     big = WS.WarmStartNet((256, 128, 128), device=device, seed=0)
     xb = torch.zeros(256 * 128 * 128 * WS.C_IN, dtype=torch.bfloat16, device=torch.device("cuda", device))
@@ -402,12 +435,19 @@ def warmstart_extra(device, n_train=32, n_test=6, tau=0.55):
     torch.cuda.synchronize()
     fwd_ms = ev[0].elapsed_time(ev[1]) / 3
     flops = sum(2.0 * big.nvox(mm["lvl_out"]) * mm["co"] * mm["taps"] * mm["ci"] for mm in big.meta.values())
-    cold = sum(r["cold_steps"] for r in rows)
-    warm = sum(r["warm_steps"] for r in rows)
+    ok = [r for r in rows if all(r[k]["steps_1pct_wss"] is not None for k in ("cold", "prior", "net"))]
+    tot = lambda arm, k: sum(r[arm][k] for r in ok)
     return {"grid": list(sols[0][0].shape), "train_vessels": n_train, "test_vessels": n_test, "tau": tau,
             "data_s": data_s, "train_s": train_s, "train_iters": 2000, "loss_first_last": [hist[0], hist[-1]],
-            "cold_steps_total": cold, "warm_steps_total": warm, "warm_over_cold_steps": warm / cold,
-            "warm_over_cold_time": sum(r["warm_s"] for r in rows) / sum(r["cold_s"] for r in rows),
+            "criterion": "FP32 lattice WSS within 1% of the converged (residual 1e-6, FP64, from rest) WSS at 3 "
+                         "checks 100 steps apart; time = prediction (features, network, prior, smoothing, state "
+                         "build) + steps x measured FP32 time per step",
+            "vessels_reaching_1pct": {k: sum(r[k]["steps_1pct_wss"] is not None for r in rows)
+                                      for k in ("cold", "prior", "net")},
+            "net_over_cold_time": tot("net", "s_1pct_wss") / tot("cold", "s_1pct_wss"),
+            "prior_over_cold_time": tot("prior", "s_1pct_wss") / tot("cold", "s_1pct_wss"),
+            "net_over_cold_steps": tot("net", "steps_1pct_wss") / tot("cold", "steps_1pct_wss"),
+            "prior_over_cold_steps": tot("prior", "steps_1pct_wss") / tot("cold", "steps_1pct_wss"),
             "per_vessel": rows,
             "conv_forward_c5_grid": {"grid": [256, 128, 128], "ms": fwd_ms, "gflop": flops / 1e9,
                                      "tflops": flops / (fwd_ms * 1e-3) / 1e12,

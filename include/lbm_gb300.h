@@ -197,6 +197,11 @@ lbm_status lbm_init_equilibrium(lbm_handle* h);
 /* f = f_eq(rho, u) + regularised non-equilibrium part (regularized != 0) or
  * f_eq only; rho and u (3 per node) per active node, FP32. */
 lbm_status lbm_init_from_macro(lbm_handle* h, const float* rho, const float* u, int regularized);
+/* The same from DEVICE arrays (nact and 3 * nact floats) written on
+ * `stream` (a cudaStream_t, NULL = the default stream): the handle's stream
+ * waits for `stream`, then builds the state; returns when it is built. */
+lbm_status lbm_init_from_macro_device(lbm_handle* h, const float* rho, const float* u, int regularized,
+                                      void* stream);
 
 /* Advance nsteps full reference steps: collide, stream, inlet, outlets,
  * wall rule, wall shear stress, OSI/TAWSS (Simulation.cpp:577-586). */
@@ -255,10 +260,10 @@ lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph);
 
 /* Launch-shape variants of the step kernel: one node per thread with
  * (block size, minimum resident blocks per SM) = (128,12) (128,10) (128,8)
- * (256,3) (256,1), and variant 5, the tiled kernel (bulk copies stage each
+ * (256,3) (256,1); variant 5, the tiled kernel (bulk copies stage each
  * 256-node tile's sources in shared memory; physics mode, FP32 / FP16 /
- * BF16; elsewhere it runs variant 0, or 4 for FP64).  A new handle starts on
- * variant 0, FP64 on variant 4.  lbm_autotune times each variant for trial_steps steps on a
+ * BF16; elsewhere it runs variant 0, or 4 for FP64).  A new handle starts
+ * on variant 0, FP64 on variant 4.  lbm_autotune times each variant for trial_steps steps on a
  * snapshot of the current state, restores the state, keeps the fastest and
  * reports it (and, if ms_per_step is not NULL, the time of every variant:
  * LBM_NUM_VARIANTS floats).  No reference counterpart (the reference has a

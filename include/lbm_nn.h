@@ -58,6 +58,32 @@ lbm_status lbm_nn_adam(float* w, void* w_bf16, const float* grad, float* m, floa
  * jump flooding; scratch holds 2 * D * H * W int32. */
 lbm_status lbm_sdf_from_mask(const uint8_t* mask, const int dims[3], float* sdf, void* scratch, void* stream);
 
+/* Slice-wise Hagen-Poiseuille prior of a vessel along +z (inlet on the
+ * first fluid slice with peak velocity `inlet`, density 1 after the last):
+ * dist = in-slice distance to the wall (jump flooding per z slice, 0 on
+ * solid), R(z) = its slice maximum, u_z = 2 Q / (pi R^2) (1 - (R - dist)^2 /
+ * R^2) with Q = pi R0^2 inlet / 2, and drho = rho - 1 from d rho / dz =
+ * -3 * 8 nu Q / (pi R^4).  scratch: 2 * D * H * W int32 + 3 * D floats. */
+lbm_status lbm_ws_prior(const uint8_t* mask, const int dims[3], double inlet, double nu, float* dist, float* drho,
+                        float* uz, void* scratch, void* stream);
+
+/* `rounds` passes of a masked [1, 2, 1] / 4 filter along z, y and x over an
+ * FP32 field v (weights renormalised next to solid voxels or the box face,
+ * zero on solid); tmp: scratch of v's size. */
+lbm_status lbm_ws_smooth(const uint8_t* mask, const int dims[3], float* v, float* tmp, int rounds, void* stream);
+
+/* Network output y ([nvox][c] FP32, c >= 4) to fields [4][nvox]: rho - 1 =
+ * drho_p + y0 inlet / rho_scale, u = y1..3 inlet / u_scale, u_z += uz_p;
+ * zero on solid voxels. */
+lbm_status lbm_ws_output(const float* y, int c, const uint8_t* mask, const float* drho_p, const float* uz_p,
+                         int64_t nvox, float inlet, float rho_scale, float u_scale, float* fields, void* stream);
+
+/* rho[a] = 1 + fields[0][idx[a]], u[3a + k] = fields[1 + k][idx[a]]: the
+ * per-node input of lbm_init_from_macro_device (idx = the fluid voxels in
+ * raster order, which is the lattice's active-node order). */
+lbm_status lbm_ws_gather(const float* fields, int64_t nvox, const int64_t* idx, int64_t nact, float* rho, float* u,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,7 +68,8 @@ EXPORTS = [
     "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_autotune", "lbm_set_variant",
     "lbm_moment_sums_noalloc",
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
-    "lbm_nn_adam", "lbm_sdf_from_mask",
+    "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
+    "lbm_init_from_macro_device",
 ]
 NUM_VARIANTS = 6
 
@@ -135,6 +136,11 @@ def load(build_if_missing: bool = True):
     L.lbm_nn_mse.argtypes = [P, P, P, C.c_int64, C.c_int, C.c_int, C.c_float, P, P, P]
     L.lbm_nn_adam.argtypes = [P, P, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int64, P]
     L.lbm_sdf_from_mask.argtypes = [P, I3, P, P, P]
+    L.lbm_ws_prior.argtypes = [P, I3, C.c_double, C.c_double, P, P, P, P, P]
+    L.lbm_ws_smooth.argtypes = [P, I3, P, P, C.c_int, P]
+    L.lbm_ws_output.argtypes = [P, C.c_int, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, P, P]
+    L.lbm_ws_gather.argtypes = [P, C.c_int64, P, C.c_int64, P, P, P]
+    L.lbm_init_from_macro_device.argtypes = [P, P, P, C.c_int, P]
     _lib = L
     return L
 
@@ -258,6 +264,11 @@ class Solver:
 
     def init_equilibrium(self):
         self._c(load().lbm_init_equilibrium(self.h))
+
+    def init_from_macro_device(self, rho_ptr, u_ptr, regularized=True, stream=0):
+        """Warm start from device arrays (nact and 3 * nact FP32) written on `stream`."""
+        self._c(load().lbm_init_from_macro_device(self.h, C.c_void_p(rho_ptr), C.c_void_p(u_ptr), int(regularized),
+                                                  C.c_void_p(stream)))
 
     def init_from_macro(self, rho, u, regularized=True):
         self._c(load().lbm_init_from_macro(self.h, np.ascontiguousarray(rho, np.float32),

@@ -702,7 +702,7 @@ lbm_status lbm_create(const lbm_desc* desc, lbm_handle** out) {
     if (h->d.tawss_div == 0.0) h->d.tawss_div = 0.9;
     // FP64 keeps every population in two registers: start it on the
     // unconstrained shape, the FP32-arithmetic formats on the 40-register one
-    h->variant = h->d.precision == LBM_F64 ? kNumVariants - 1 : 0;
+    h->variant = h->d.precision == LBM_F64 ? 4 : 0;
     e = cudaSetDevice(desc->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->slots, 2 * sizeof(int64_t));
@@ -984,6 +984,27 @@ lbm_status lbm_set_distributions(lbm_handle* h, const double* f) {
     CK(h, cudaMemcpyAsync(h->out_f, f, bytes, cudaMemcpyHostToDevice, h->st));
     CK(h, init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->out_f, h->g.nact, h->st));
     return start_state(h, false);
+}
+
+lbm_status lbm_init_from_macro_device(lbm_handle* h, const float* rho, const float* u, int regularized,
+                                      void* stream) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, rho && u, LBM_ERR_ARG, "null rho or u");
+    CK(h, cudaSetDevice(h->d.device));
+    const int64_t na = h->g.nact;
+    if (!h->out_f) CK(h, dalloc(h, &h->out_f, sizeof(double) * na * h->d.Q));
+    cudaEvent_t ev = nullptr;
+    CK(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, static_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->st, ev, 0);
+    if (e == cudaSuccess)
+        e = warm_start_f(h->d.Q, rho, u, h->g.act_idx, h->g.act_pt, na, h->nx, h->ny, h->nz, h->d.tau, regularized,
+                         h->out_f, h->st);
+    if (e == cudaSuccess) e = init_state(h->d.precision, h->d.Q, 1, h->buf[0], h->stride, h->out_f, na, h->st);
+    cudaEventDestroy(ev);
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("init_from_macro_device: ") + cudaGetErrorString(e));
+    return start_state(h, true);
 }
 
 lbm_status lbm_init_from_macro(lbm_handle* h, const float* rho, const float* u, int regularized) {

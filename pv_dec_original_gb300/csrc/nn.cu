@@ -298,6 +298,9 @@ __global__ void k_adam(float* __restrict__ w, bf16* __restrict__ wb, const float
 // voxels with a non-fluid 6-neighbour (or on the box face); every voxel
 // keeps the nearest seed found at offsets k = N/2, N/4, ..., 1, then a final
 // pass at offset 1.  sdf > 0 in fluid, < 0 outside, in lattice spacings.
+// PLANAR: every z slice on its own (seeds from in-plane neighbours, search
+// in the slice), for the in-slice distance to the wall.
+template <bool PLANAR>
 __global__ void k_jfa_seed(const uint8_t* __restrict__ mask, int D, int H, int W, int32_t* __restrict__ seed) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = (int64_t)D * H * W;
@@ -306,7 +309,7 @@ __global__ void k_jfa_seed(const uint8_t* __restrict__ mask, int D, int H, int W
     bool s = false;
     if (mask[v]) {
         const int d[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
-        for (int k = 0; k < 6 && !s; ++k) {
+        for (int k = 0; k < (PLANAR ? 4 : 6) && !s; ++k) {
             const int xx = x + d[k][0], yy = y + d[k][1], zz = z + d[k][2];
             s = xx < 0 || yy < 0 || zz < 0 || xx >= W || yy >= H || zz >= D ||
                 !mask[((int64_t)zz * H + yy) * W + xx];
@@ -315,6 +318,7 @@ __global__ void k_jfa_seed(const uint8_t* __restrict__ mask, int D, int H, int W
     seed[v] = s ? (int32_t)v : -1;
 }
 
+template <bool PLANAR>
 __global__ void k_jfa_step(const int32_t* __restrict__ in, int32_t* __restrict__ out, int D, int H, int W, int k) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = (int64_t)D * H * W;
@@ -327,7 +331,7 @@ __global__ void k_jfa_step(const int32_t* __restrict__ in, int32_t* __restrict__
                     dz = (float)(z - (int)(best / ((int64_t)W * H)));
         bd = dx * dx + dy * dy + dz * dz;
     }
-    for (int dz = -1; dz <= 1; ++dz)
+    for (int dz = (PLANAR ? 0 : -1); dz <= (PLANAR ? 0 : 1); ++dz)
         for (int dy = -1; dy <= 1; ++dy)
             for (int dx = -1; dx <= 1; ++dx) {
                 const int xx = x + dx * k, yy = y + dy * k, zz = z + dz * k;
@@ -342,6 +346,7 @@ __global__ void k_jfa_step(const int32_t* __restrict__ in, int32_t* __restrict__
     out[v] = best;
 }
 
+template <bool PLANAR>
 __global__ void k_jfa_finish(const int32_t* __restrict__ seed, const uint8_t* __restrict__ mask, int D, int H,
                              int W, float* __restrict__ sdf) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -356,7 +361,108 @@ __global__ void k_jfa_finish(const int32_t* __restrict__ seed, const uint8_t* __
         d = sqrtf(ex * ex + ey * ey + ez * ez);
     }
     // a seed voxel is half a spacing inside the wall
-    sdf[v] = mask[v] ? d + 0.5f : -(d + 0.5f);
+    sdf[v] = mask[v] ? d + 0.5f : (PLANAR ? 0.f : -(d + 0.5f));
+}
+
+// --------------------------------------------------------------------------
+// Slice-wise Hagen-Poiseuille prior (flow along +z): with s the in-slice
+// distance to the wall and R(z) its largest value in slice z,
+// u_z = 2 Q / (pi R^2) (1 - (R - s)^2 / R^2) and rho - 1 from
+// d rho / dz = -3 * 8 nu Q / (pi R^4), zero at the last slice;
+// Q = pi R0^2 u_in / 2 on the first fluid slice.
+__global__ void k_slice_max(const float* __restrict__ dist, int HW, float* __restrict__ R) {
+    __shared__ float red[256];
+    const int z = blockIdx.x;
+    float m = 0.f;
+    for (int i = threadIdx.x; i < HW; i += blockDim.x) m = fmaxf(m, dist[(int64_t)z * HW + i]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w /= 2) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) R[z] = red[0];
+}
+
+// one thread: per-slice peak velocity and density offset (suffix sums)
+__global__ void k_prior_axis(const float* __restrict__ R, int D, double inlet, double nu, float* __restrict__ peak,
+                             float* __restrict__ tail) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int z0 = -1;
+    for (int z = 0; z < D && z0 < 0; ++z)
+        if (R[z] > 0.f) z0 = z;
+    const double pi = 3.14159265358979323846;
+    const double Q = z0 < 0 ? 0.0 : pi * (double)R[z0] * (double)R[z0] * inlet / 2.0;
+    double acc = 0.0;  // sum of drho over the slices downstream of z
+    for (int z = D - 1; z >= 0; --z) {
+        const double Rs = fmax((double)R[z], 1.0);
+        peak[z] = (float)(2.0 * Q / (pi * Rs * Rs));
+        tail[z] = (float)acc;
+        if (R[z] > 0.f) acc += 3.0 * 8.0 * nu * Q / (pi * Rs * Rs * Rs * Rs);
+    }
+}
+
+__global__ void k_prior_fill(const uint8_t* __restrict__ mask, const float* __restrict__ dist,
+                             const float* __restrict__ R, const float* __restrict__ peak,
+                             const float* __restrict__ tail, int64_t n, int HW, float* __restrict__ drho,
+                             float* __restrict__ uz) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int z = (int)(v / HW);
+    float u = 0.f, r = 0.f;
+    if (mask[v]) {
+        const float Rs = fmaxf(R[z], 1.f), e = Rs - dist[v];
+        u = peak[z] * fminf(fmaxf(1.f - e * e / (Rs * Rs), 0.f), 1.f);
+        r = tail[z];
+    }
+    uz[v] = u;
+    drho[v] = r;
+}
+
+// Masked [1, 2, 1] / 4 filter along one axis (weights renormalised where a
+// neighbour is solid or outside the box); zero on solid voxels.
+__global__ void k_smooth_axis(const uint8_t* __restrict__ mask, const float* __restrict__ in,
+                              float* __restrict__ out, int D, int H, int W, int axis) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)D * H * W;
+    if (v >= n) return;
+    if (!mask[v]) { out[v] = 0.f; return; }
+    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((int64_t)W * H));
+    const int c = axis == 0 ? z : (axis == 1 ? y : x);
+    const int len = axis == 0 ? D : (axis == 1 ? H : W);
+    const int64_t st = axis == 0 ? (int64_t)W * H : (axis == 1 ? (int64_t)W : 1);
+    float num = 2.f * in[v], den = 2.f;
+    if (c + 1 < len && mask[v + st]) { num += in[v + st]; den += 1.f; }
+    if (c - 1 >= 0 && mask[v - st]) { num += in[v - st]; den += 1.f; }
+    out[v] = num / den;
+}
+
+// Network output [n][c] (FP32) to fields [4][n]: rho - 1 = prior + y0 U /
+// rho_scale, u = y1..3 U / u_scale (+ prior u_z); zero on solid voxels.
+__global__ void k_ws_output(const float* __restrict__ y, int c, const uint8_t* __restrict__ mask,
+                            const float* __restrict__ drho_p, const float* __restrict__ uz_p, int64_t n, float inlet,
+                            float rho_scale, float u_scale, float* __restrict__ f) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const bool fl = mask[v] != 0;
+    const float* yv = y + v * c;
+    f[v] = fl ? drho_p[v] + yv[0] * inlet / rho_scale : 0.f;
+    f[n + v] = fl ? yv[1] * inlet / u_scale : 0.f;
+    f[2 * n + v] = fl ? yv[2] * inlet / u_scale : 0.f;
+    f[3 * n + v] = fl ? yv[3] * inlet / u_scale + uz_p[v] : 0.f;
+}
+
+// Gather fluid voxels (index list) into per-node rho (1 + field 0) and
+// interleaved u (3 per node).
+__global__ void k_ws_gather(const float* __restrict__ f, int64_t n, const int64_t* __restrict__ idx, int64_t m,
+                            float* __restrict__ rho, float* __restrict__ u) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= m) return;
+    const int64_t v = idx[a];
+    rho[a] = 1.f + f[v];
+    u[3 * a] = f[n + v];
+    u[3 * a + 1] = f[2 * n + v];
+    u[3 * a + 2] = f[3 * n + v];
 }
 
 int report(const char* what, cudaError_t e) {
@@ -404,6 +510,24 @@ cudaError_t launch_wgrad_ci(int ci, const bf16* x, const bf16* dy, float* dw, co
 }
 
 unsigned grid1(int64_t n) { return (unsigned)lbm::ceil_div(n > 0 ? n : 1, 256); }
+
+// jump flooding into scratch (2 n int32), distances into out
+template <bool PLANAR>
+void jfa(const uint8_t* mask, int D, int H, int W, int32_t* scratch, float* out, cudaStream_t st) {
+    const int64_t n = (int64_t)D * H * W;
+    int32_t* a = scratch;
+    int32_t* b = a + n;
+    k_jfa_seed<PLANAR><<<grid1(n), 256, 0, st>>>(mask, D, H, W, a);
+    const int big = PLANAR ? (H > W ? H : W) : (D > H ? (D > W ? D : W) : (H > W ? H : W));
+    int k = 1;
+    while (k * 2 < big) k *= 2;
+    for (; k >= 1; k /= 2) {
+        k_jfa_step<PLANAR><<<grid1(n), 256, 0, st>>>(a, b, D, H, W, k);
+        int32_t* t = a; a = b; b = t;
+    }
+    k_jfa_step<PLANAR><<<grid1(n), 256, 0, st>>>(a, b, D, H, W, 1);
+    k_jfa_finish<PLANAR><<<grid1(n), 256, 0, st>>>(b, mask, D, H, W, out);
+}
 
 }  // namespace
 
@@ -514,20 +638,65 @@ lbm_status lbm_sdf_from_mask(const uint8_t* mask, const int dims[3], float* sdf,
         return report("lbm_sdf_from_mask", cudaSuccess);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int D = dims[0], H = dims[1], W = dims[2];
-    const int64_t n = (int64_t)D * H * W;
-    int32_t* a = static_cast<int32_t*>(scratch);
-    int32_t* b = a + n;
-    k_jfa_seed<<<grid1(n), 256, 0, st>>>(mask, D, H, W, a);
-    int k = 1;
-    while (k * 2 < (D > H ? (D > W ? D : W) : (H > W ? H : W))) k *= 2;
-    for (; k >= 1; k /= 2) {
-        k_jfa_step<<<grid1(n), 256, 0, st>>>(a, b, D, H, W, k);
-        int32_t* t = a; a = b; b = t;
-    }
-    k_jfa_step<<<grid1(n), 256, 0, st>>>(a, b, D, H, W, 1);
-    k_jfa_finish<<<grid1(n), 256, 0, st>>>(b, mask, D, H, W, sdf);
+    jfa<false>(mask, D, H, W, static_cast<int32_t*>(scratch), sdf, st);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? LBM_OK : report("lbm_sdf_from_mask", e);
+}
+
+lbm_status lbm_ws_prior(const uint8_t* mask, const int dims[3], double inlet, double nu, float* dist, float* drho,
+                        float* uz, void* scratch, void* stream) {
+    if (!mask || !dims || !dist || !drho || !uz || !scratch || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0)
+        return report("lbm_ws_prior", cudaSuccess);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int D = dims[0], H = dims[1], W = dims[2];
+    const int64_t n = (int64_t)D * H * W;
+    int32_t* jf = static_cast<int32_t*>(scratch);
+    float* R = reinterpret_cast<float*>(jf + 2 * n);
+    float* peak = R + D;
+    float* tail = peak + D;
+    jfa<true>(mask, D, H, W, jf, dist, st);
+    k_slice_max<<<D, 256, 0, st>>>(dist, H * W, R);
+    k_prior_axis<<<1, 1, 0, st>>>(R, D, inlet, nu, peak, tail);
+    k_prior_fill<<<grid1(n), 256, 0, st>>>(mask, dist, R, peak, tail, n, H * W, drho, uz);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_ws_prior", e);
+}
+
+lbm_status lbm_ws_smooth(const uint8_t* mask, const int dims[3], float* v, float* tmp, int rounds, void* stream) {
+    if (!mask || !dims || !v || !tmp || rounds < 0 || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0)
+        return report("lbm_ws_smooth", cudaSuccess);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int D = dims[0], H = dims[1], W = dims[2];
+    const int64_t n = (int64_t)D * H * W;
+    float* src = v;
+    float* dst = tmp;
+    for (int r = 0; r < rounds; ++r)
+        for (int a = 0; a < 3; ++a) {  // z, y, x in turn
+            k_smooth_axis<<<grid1(n), 256, 0, st>>>(mask, src, dst, D, H, W, a);
+            float* t = src; src = dst; dst = t;
+        }
+    if (src != v) cudaMemcpyAsync(v, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_ws_smooth", e);
+}
+
+lbm_status lbm_ws_output(const float* y, int c, const uint8_t* mask, const float* drho_p, const float* uz_p,
+                         int64_t nvox, float inlet, float rho_scale, float u_scale, float* fields, void* stream) {
+    if (!y || c < 4 || !mask || !drho_p || !uz_p || nvox < 0 || !fields) return report("lbm_ws_output", cudaSuccess);
+    if (nvox == 0) return LBM_OK;
+    k_ws_output<<<grid1(nvox), 256, 0, static_cast<cudaStream_t>(stream)>>>(y, c, mask, drho_p, uz_p, nvox, inlet,
+                                                                            rho_scale, u_scale, fields);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_ws_output", e);
+}
+
+lbm_status lbm_ws_gather(const float* fields, int64_t nvox, const int64_t* idx, int64_t nact, float* rho, float* u,
+                         void* stream) {
+    if (!fields || nvox < 0 || (nact > 0 && (!idx || !rho || !u)) || nact < 0) return report("lbm_ws_gather", cudaSuccess);
+    if (nact == 0) return LBM_OK;
+    k_ws_gather<<<grid1(nact), 256, 0, static_cast<cudaStream_t>(stream)>>>(fields, nvox, idx, nact, rho, u);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_ws_gather", e);
 }
 
 }  // extern "C"

@@ -763,7 +763,8 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
 struct Variant {
     int bt, minb;
 };
-constexpr Variant kVariants[kNumVariants] = {{128, 12}, {128, 10}, {128, 8}, {256, 3}, {256, 1}};
+constexpr int kFlatVariants = 5;  // 0..4; 5 = tiled
+constexpr Variant kVariants[kFlatVariants] = {{128, 12}, {128, 10}, {128, 8}, {256, 3}, {256, 1}};
 
 template <int Q, typename S, int MODE, int V>
 cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {

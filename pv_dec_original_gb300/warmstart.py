@@ -15,7 +15,11 @@ stenosed tubes and bifurcations, computed as one packed ensemble.
 The LBM stays the judge: a warm-started lattice is run to the same
 convergence criterion as a cold one (``steps_to_converge``, on FP64 lattices
 so that the criterion sits far above the storage's rounding noise), so a
-poor prediction costs steps, never accuracy.  The reference always starts from
+poor prediction costs steps, never accuracy.  The figure of merit is the
+number of steps (and the wall time, prediction included) after which the
+wall shear stress stays within 1% of the converged cold-start WSS
+(``converge_with_history`` / ``first_within`` for the cold run,
+``steps_to_wss`` for a warm one).  The reference always starts from
 rest (Node.cpp:30-37); it has no counterpart to this module.
 """
 from __future__ import annotations
@@ -243,113 +247,107 @@ def sdf_of_mask(mask, device=0):
     return out
 
 
-def poiseuille_prior(mask, inlet, tau):
-    """Slice-wise Hagen-Poiseuille estimate of the steady flow (flow along
-    +z, parabolic inlet of peak `inlet` on the first fluid slice, density 1
-    on the last): with s the in-slice distance to the half-way wall and R(z)
-    its largest value in slice z, u_z = 2 Q / (pi R^2) (1 - (R - s)^2 / R^2)
-    and rho from d rho/dz = -3 * 8 nu Q / (pi R^4).  Returns voxel arrays."""
-    from scipy.ndimage import distance_transform_edt
-    D = mask.shape[0]
-    fl = mask > 0
-    s = np.zeros(mask.shape, np.float64)
-    for z in range(D):
-        if fl[z].any():
-            s[z] = np.where(fl[z], distance_transform_edt(fl[z]) - 0.5, 0.0)
-    R = s.reshape(D, -1).max(1)
-    zs = np.nonzero(R > 0)[0]
-    uz = np.zeros(mask.shape, np.float64)
-    rho = np.ones(mask.shape, np.float64)
-    if zs.size == 0:
-        return rho, uz
-    Q = math.pi * R[zs[0]] ** 2 * inlet / 2.0
-    nu = (tau - 0.5) / 3.0
-    Rs = np.maximum(R, 1.0)
-    peak = 2.0 * Q / (math.pi * Rs ** 2)
-    prof = np.clip(1.0 - (Rs[:, None, None] - s) ** 2 / Rs[:, None, None] ** 2, 0.0, 1.0)
-    uz = np.where(fl, peak[:, None, None] * prof, 0.0)
-    drho = np.where(R > 0, 3.0 * 8.0 * nu * Q / (math.pi * Rs ** 4), 0.0)
-    tail = np.concatenate([np.cumsum(drho[::-1])[::-1][1:], [0.0]])  # sum over the slices downstream
-    rho = np.where(fl, 1.0 + tail[:, None, None], 1.0)
-    return rho, uz
+class Prior:
+    """Device data of one vessel grid: the mask, its fluid voxels (raster
+    order = the lattice's active-node order) and the slice-wise
+    Hagen-Poiseuille prior (rho - 1, u_z) from ``lbm_ws_prior``."""
+
+    def __init__(self, mask, inlet, tau, device=0):
+        torch = _torch()
+        self.dev = torch.device("cuda", device)
+        self.shape = tuple(int(v) for v in mask.shape)
+        self.n = int(mask.size)
+        self.mask = torch.from_numpy(np.ascontiguousarray(mask.reshape(-1), np.uint8)).to(self.dev)
+        self.idx = torch.from_numpy(np.flatnonzero(mask.reshape(-1) > 0).astype(np.int64)).to(self.dev)
+        self.inlet = float(inlet)
+        D = self.shape[0]
+        f32 = dict(dtype=torch.float32, device=self.dev)
+        self.dist = torch.empty(self.n, **f32)
+        self.drho = torch.empty(self.n, **f32)
+        self.uz = torch.empty(self.n, **f32)
+        scratch = torch.empty(2 * self.n + 3 * D, dtype=torch.int32, device=self.dev)
+        self.stream = torch.cuda.current_stream(self.dev)
+        capi._check(capi.load().lbm_ws_prior(_ptr(self.mask), _dims(self.shape), self.inlet, (tau - 0.5) / 3.0,
+                                             _ptr(self.dist), _ptr(self.drho), _ptr(self.uz), _ptr(scratch),
+                                             C.c_void_p(self.stream.cuda_stream)))
+        self._keep = scratch
+
+    @property
+    def nact(self):
+        return int(self.idx.numel())
 
 
 def features(mask, inlet_mean, period, tau=0.8, device=0):
-    """BF16 channels-last network input [D*H*W*C_IN] and the prior (rho,
-    u_z) voxel arrays the network's output corrects."""
+    """BF16 channels-last network input [D*H*W*C_IN] and the Prior the
+    network's output corrects (every array built on the device)."""
     torch = _torch()
     dev = torch.device("cuda", device)
     n = mask.size
     sdf = sdf_of_mask(mask, device)
-    rho_p, uz_p = poiseuille_prior(mask, inlet_mean, tau)
+    prior = Prior(mask, inlet_mean, tau, device)
     x = torch.zeros((n, C_IN), dtype=torch.float32, device=dev)
     x[:, 0] = torch.clamp(sdf * SDF_SCALE, -3.0, 3.0)
-    x[:, 1] = torch.from_numpy(mask.reshape(-1).astype(np.float32)).to(dev)
+    x[:, 1] = prior.mask.to(torch.float32)
     x[:, 2] = inlet_mean * MEAN_SCALE
     x[:, 3] = period * PERIOD_SCALE
     # axial position (flow along z): the pressure level depends on the
     # distance to the outlet, beyond the convolutions' receptive field
     D, H, W = mask.shape
     x[:, 4] = (torch.arange(D, device=dev, dtype=torch.float32) / D).repeat_interleave(H * W)
-    x[:, 5] = torch.from_numpy((uz_p / inlet_mean).reshape(-1).astype(np.float32)).to(dev)
-    x[:, 6] = torch.from_numpy(((rho_p - 1.0) / inlet_mean * RHO_SCALE).reshape(-1).astype(np.float32)).to(dev)
-    return x.to(torch.bfloat16).reshape(-1).contiguous(), (rho_p, uz_p)
+    x[:, 5] = prior.uz / inlet_mean
+    x[:, 6] = prior.drho / inlet_mean * RHO_SCALE
+    return x.to(torch.bfloat16).reshape(-1).contiguous(), prior
 
 
 def make_target(mask, rho, u, inlet, prior, device=0):
-    """FP32 [D*H*W][4] target: the scaled correction of the prior."""
+    """FP32 [D*H*W][4] target: the scaled correction of the prior (rho, u
+    per active node, host arrays)."""
     torch = _torch()
-    rho_p, uz_p = prior
-    t = np.zeros((mask.size, 4), np.float32)
-    fl = mask.reshape(-1) > 0
-    t[fl, 0] = (rho - rho_p.reshape(-1)[fl]) / inlet * RHO_SCALE
-    t[fl, 1:] = u / inlet * U_SCALE
-    t[fl, 3] -= uz_p.reshape(-1)[fl] / inlet * U_SCALE
-    return torch.from_numpy(t.reshape(-1)).to(torch.device("cuda", device))
+    t = torch.zeros((mask.size, 4), dtype=torch.float32, device=prior.dev)
+    r = torch.from_numpy(np.ascontiguousarray(rho, np.float64) - 1.0).to(prior.dev, torch.float32)
+    uu = torch.from_numpy(np.ascontiguousarray(u, np.float32).reshape(-1, 3)).to(prior.dev)
+    i = prior.idx
+    t[i, 0] = (r - prior.drho[i]) / inlet * RHO_SCALE
+    t[i, 1:] = uu / inlet * U_SCALE
+    t[i, 3] -= prior.uz[i] / inlet * U_SCALE
+    return t.reshape(-1)
 
 
-def smooth_masked(mask, v, rounds=2):
-    """[1, 2, 1] / 4 filter along each axis, restricted to fluid voxels
-    (weights renormalised where a neighbour is solid): removes the
-    voxel-scale (checkerboard) content of a prediction, which the lattice
-    would otherwise carry as undamped modes."""
-    fl = mask > 0
-    v = np.where(fl, v, 0.0)
-    w = fl.astype(np.float64)
-    for _ in range(rounds):
-        for a in range(3):
-            num = 2.0 * v
-            den = 2.0 * w
-            for sh in (1, -1):
-                num = num + np.roll(v * w, sh, axis=a) * _edge(mask.shape, a, sh)
-                den = den + np.roll(w, sh, axis=a) * _edge(mask.shape, a, sh)
-            v = np.where(fl, num / np.maximum(den, 1e-30), 0.0)
-    return v
-
-
-def _edge(shape, a, sh):
-    """1 where np.roll along axis a by sh brings a real neighbour (not a wrap)."""
-    e = np.ones(shape[a])
-    e[0 if sh == 1 else -1] = 0.0
-    return e.reshape([-1 if k == a else 1 for k in range(3)])
+def prediction_to_device(y32, prior, smooth=2):
+    """Per-active-node rho (nact) and u (3 * nact, interleaved) as device
+    FP32 tensors from the network output y32 ([voxels][C_OUT] FP32 on the
+    device): prior + correction, smoothed over the fluid, gathered
+    (``lbm_ws_output``, ``lbm_ws_smooth``, ``lbm_ws_gather``)."""
+    torch = _torch()
+    L = capi.load()
+    st = C.c_void_p(prior.stream.cuda_stream)
+    n, m = prior.n, prior.nact
+    f32 = dict(dtype=torch.float32, device=prior.dev)
+    fields = torch.empty(4 * n, **f32)
+    capi._check(L.lbm_ws_output(_ptr(y32), C_OUT, _ptr(prior.mask), _ptr(prior.drho), _ptr(prior.uz), n,
+                                prior.inlet, RHO_SCALE, U_SCALE, _ptr(fields), st))
+    if smooth:
+        tmp = torch.empty(n, **f32)
+        for k in range(4):
+            capi._check(L.lbm_ws_smooth(_ptr(prior.mask), _dims(prior.shape), C.c_void_p(fields.data_ptr() + 4 * k * n),
+                                        _ptr(tmp), int(smooth), st))
+    rho = torch.empty(m, **f32)
+    u = torch.empty(3 * m, **f32)
+    capi._check(L.lbm_ws_gather(_ptr(fields), n, _ptr(prior.idx), m, _ptr(rho), _ptr(u), st))
+    return rho, u
 
 
 def prediction_to_macro(mask, y32, inlet, prior, smooth=2):
-    """Per-active-node rho (FP32) and u (FP32, 3 per node) from the output
-    (prior + correction, smoothed over the fluid)."""
-    rho_p, uz_p = prior
-    y = y32.reshape(-1, C_OUT)[:, :4].cpu().numpy().astype(np.float64)
-    shape = mask.shape
-    rho = rho_p + (y[:, 0] * inlet / RHO_SCALE).reshape(shape)
-    u = [(y[:, 1 + c] * inlet / U_SCALE).reshape(shape) for c in range(3)]
-    u[2] = u[2] + uz_p
-    if smooth:
-        rho = 1.0 + smooth_masked(mask, rho - 1.0, smooth)
-        u = [smooth_masked(mask, c, smooth) for c in u]
-    fl = mask.reshape(-1) > 0
-    r = rho.reshape(-1)[fl].astype(np.float32)
-    uu = np.stack([c.reshape(-1)[fl] for c in u], 1).astype(np.float32)
-    return r, uu
+    """prediction_to_device read back to the host: rho (nact) and u
+    (nact, 3), FP32."""
+    rho, u = prediction_to_device(y32, prior, smooth)
+    return rho.cpu().numpy(), u.cpu().numpy().reshape(-1, 3)
+
+
+def zero_output(prior):
+    """A zero network output: prediction_to_device of it is the prior alone."""
+    torch = _torch()
+    return torch.zeros(prior.n * C_OUT, dtype=torch.float32, device=prior.dev)
 
 
 def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4):
@@ -428,6 +426,52 @@ def steps_to_converge(solver, tol=1e-6, check=100, max_steps=60000):
     return n, r
 
 
+def converge_with_history(solver, tol=1e-6, check=100, max_steps=60000):
+    """steps_to_converge that also keeps the wall shear stress after every
+    `check` steps; returns (steps, last residual, [(step, wss)])."""
+    step = residual_runner(solver, check)
+    n, r, hist = 0, float("inf"), []
+    while n < max_steps:
+        r = step()
+        n += check
+        hist.append((n, solver.wss()["wss"].copy()))
+        if r < tol:
+            break
+    return n, r, hist
+
+
+def wss_error(w, ref):
+    return float(np.linalg.norm(w - ref) / max(np.linalg.norm(ref), 1e-300))
+
+
+def first_within(hist, ref, tol=0.01):
+    """First step of a (step, wss) history from which the WSS error against
+    `ref` stays below `tol` (None if it never settles there)."""
+    ok = None
+    for n, w in hist:
+        if wss_error(w, ref) < tol:
+            ok = n if ok is None else ok
+        else:
+            ok = None
+    return ok
+
+
+def steps_to_wss(solver, ref, tol=0.01, check=100, max_steps=60000, hold=3):
+    """Steps until the WSS error against `ref` is below `tol` at `hold`
+    consecutive checks (the first of them counts); None if not reached."""
+    n, run = 0, 0
+    while n < max_steps:
+        if wss_error(solver.wss()["wss"], ref) < tol:
+            run += 1
+            if run == hold:
+                return n - (hold - 1) * check
+        else:
+            run = 0
+        solver.step(check)
+        n += check
+    return None
+
+
 def single_lattice(member, tau=0.8, precision="f64", device=0):
     """One member as its own lattice with a constant inlet (steady problem)."""
     tri = member["surface"].tri12()
@@ -446,11 +490,9 @@ def single_lattice(member, tau=0.8, precision="f64", device=0):
 
 def make_sample(mask, member, rho, u, tau=0.8, device=0):
     """(input, target, device mask, 1 / (4 * fluid voxels)) for training."""
-    torch = _torch()
     x, prior = features(mask, member["inlet_mean"], member["period"], tau, device)
     t = make_target(mask, rho, u, member["inlet_mean"], prior, device)
-    m = torch.from_numpy(np.ascontiguousarray(mask.reshape(-1), np.uint8)).to(torch.device("cuda", device))
-    return x, t, m, 1.0 / (4.0 * max(1, int(mask.sum())))
+    return x, t, prior.mask, 1.0 / (4.0 * max(1, int(mask.sum())))
 
 
 def train(net, samples, iters=400, lr=2e-3, batch=4, log=None):

@@ -212,3 +212,79 @@ def test_gpu_network_gradient_vs_cpu_autograd(gpu_lib):
     assert cos > 0.999 and rel < 0.05, (cos, rel)
     gb_ref = torch.cat([params[k][1].grad for k in net.meta])
     assert float((gb_ref - net.gb.cpu().double()).norm() / gb_ref.norm()) < 0.05
+
+
+def _vessel_mask(D=32, H=24, W=16):
+    z, y, x = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
+    r = 5.0 + 1.5 * np.sin(z / 4.0)
+    m = (((x - 7.3) ** 2 / 0.8 + (y - 11.1) ** 2) < r ** 2).astype(np.uint8)
+    m[0] = 0
+    m[-1] = 0
+    return m
+
+
+def test_gpu_ws_prior_matches_host(gpu_lib):
+    """lbm_ws_prior: the jump-flooded in-slice distance against the exact one
+    (the same tolerance as the 3D field), and the prior against its FP64
+    restatement evaluated on the device's distance."""
+    from helpers import poiseuille_prior, slice_distance
+    from pv_dec_original_gb300 import warmstart as WS
+    mask = _vessel_mask()
+    U, tau = 0.025, 0.55
+    pr = WS.Prior(mask, U, tau)
+    dist = pr.dist.cpu().numpy().astype(np.float64).reshape(mask.shape)
+    ref = slice_distance(mask)
+    err = np.abs(dist - ref)
+    assert np.all(dist[mask == 0] == 0.0)
+    assert err.max() <= 1.0 and err.mean() <= 0.02, (err.max(), err.mean())
+    drho, uz = poiseuille_prior(mask, U, tau, s=dist)
+    np.testing.assert_allclose(pr.uz.cpu().numpy().reshape(mask.shape), uz, rtol=1e-5, atol=1e-6 * U)
+    np.testing.assert_allclose(pr.drho.cpu().numpy().reshape(mask.shape), drho, rtol=1e-5, atol=1e-9)
+    # fluid voxels in raster order
+    np.testing.assert_array_equal(pr.idx.cpu().numpy(), np.flatnonzero(mask.reshape(-1)))
+
+
+def test_gpu_ws_output_smooth_gather(gpu_lib):
+    """Network output -> prior + correction -> masked smoothing -> per-node
+    rho / u, against the FP64 host restatement."""
+    from helpers import smooth_masked
+    from pv_dec_original_gb300 import warmstart as WS
+    mask = _vessel_mask()
+    U, tau = 0.03, 0.6
+    pr = WS.Prior(mask, U, tau)
+    rng = np.random.default_rng(5)
+    y = rng.normal(0.0, 0.3, (mask.size, WS.C_OUT)).astype(np.float32)
+    rho, u = WS.prediction_to_device(torch.from_numpy(y.reshape(-1)).cuda(), pr, smooth=2)
+    drho_p = pr.drho.cpu().numpy().astype(np.float64).reshape(mask.shape)
+    uz_p = pr.uz.cpu().numpy().astype(np.float64).reshape(mask.shape)
+    yy = y.astype(np.float64).reshape(mask.shape + (WS.C_OUT,))
+    f = [drho_p + yy[..., 0] * U / WS.RHO_SCALE] + [yy[..., 1 + c] * U / WS.U_SCALE for c in range(3)]
+    f[3] = f[3] + uz_p
+    f = [smooth_masked(mask, v, 2) for v in f]
+    fl = mask.reshape(-1) > 0
+    np.testing.assert_allclose(rho.cpu().numpy(), 1.0 + f[0].reshape(-1)[fl], rtol=0, atol=1e-6)
+    uu = u.cpu().numpy().reshape(-1, 3)
+    for c in range(3):
+        np.testing.assert_allclose(uu[:, c], f[1 + c].reshape(-1)[fl], rtol=0, atol=1e-6 * U + 1e-8)
+    # the host read-back is the same data
+    r2, u2 = WS.prediction_to_macro(mask, torch.from_numpy(y.reshape(-1)).cuda(), U, pr)
+    np.testing.assert_array_equal(r2, rho.cpu().numpy())
+    np.testing.assert_array_equal(u2, uu)
+
+
+def test_gpu_init_from_macro_device_matches_host(gpu_lib):
+    """lbm_init_from_macro_device builds the same state as lbm_init_from_macro."""
+    from pv_dec_original_gb300 import warmstart as WS
+    m = WS.vessel_members(1, seed=7)[0]
+    s1, mask = WS.single_lattice(m, tau=0.6, precision="f32")
+    s2, _ = WS.single_lattice(m, tau=0.6, precision="f32")
+    x, pr = WS.features(mask, m["inlet_mean"], m["period"], tau=0.6)
+    rng = np.random.default_rng(3)
+    y = torch.from_numpy(rng.normal(0.0, 0.2, mask.size * WS.C_OUT).astype(np.float32)).cuda()
+    rho, u = WS.prediction_to_device(y, pr)
+    s1.init_from_macro(rho.cpu().numpy(), u.cpu().numpy(), True)
+    s2.init_from_macro_device(rho.data_ptr(), u.data_ptr(), True, torch.cuda.current_stream().cuda_stream)
+    np.testing.assert_array_equal(s1.distributions(), s2.distributions())
+    s1.step(10)
+    s2.step(10)
+    np.testing.assert_array_equal(s1.distributions(), s2.distributions())
