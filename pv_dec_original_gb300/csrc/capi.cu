@@ -48,7 +48,7 @@ struct lbm_handle {
     int64_t nw_stride = 0;                         // plane stride of nw_nf
     int32_t* tile_plan = nullptr;                  // tiled step kernel (physics, FP32-arithmetic formats)
     TileGeom tile{};
-    float* nw_ring = nullptr;                      // [kRingSlots][4][nnw]
+    float* nw_ring = nullptr;                      // float4 [kRingSlots][nnw]
     double* nw_out = nullptr;                      // read-out staging, [5][nnw]
     float2* nw_accf = nullptr;
     bool wss_from_ckpt = false;  // |tau| of the last step comes from a checkpoint (nw_wssf), not the ring
@@ -1150,12 +1150,19 @@ int read_accumulators(lbm_handle* h, std::vector<double>& w, std::vector<double>
         CK(h, cudaStreamSynchronize(h->st));
         return LBM_OK;
     }
-    // folded steps (accumulators) + the steps since the last fold (ring
-    // slots 0 .. steps % kRingSlots - 1); |tau| of the last step from its slot
-    const int pending = (int)(h->steps % kRingSlots);
-    const int last = h->steps == 0 ? -1 : (int)((h->steps - 1) % kRingSlots);
+    // folded steps (accumulators) + the steps since the last fold: the last
+    // step m = steps - 1 was preceded by a fold at step f = m - m % kFoldEvery
+    // (of the kFoldEvery steps before f), so steps f .. m, ring slots
+    // f % kRingSlots .. m % kRingSlots, are pending; |tau| of step m from its slot
+    int first = 0, pending = 0, last = -1;
+    if (h->steps > 0) {
+        const int64_t m = h->steps - 1;
+        last = (int)(m % kRingSlots);
+        pending = (int)(m % kFoldEvery) + 1;
+        first = last - pending + 1;
+    }
     if (!h->nw_out) CK(h, dalloc(h, &h->nw_out, sizeof(double) * 5 * n));
-    CK(h, nw_readout_f32(h->nw_accf, h->nw_ring, n, pending, last, h->wss_from_ckpt ? h->nw_wssf : nullptr,
+    CK(h, nw_readout_f32(h->nw_accf, h->nw_ring, n, first, pending, last, h->wss_from_ckpt ? h->nw_wssf : nullptr,
                          h->nw_out, h->st));
     CK(h, cudaMemcpyAsync(w.data(), h->nw_out, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaMemcpyAsync(a.data(), h->nw_out + n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));

@@ -15,6 +15,7 @@
 #include <iostream>
 #include <map>
 #include <memory>
+#include <stdexcept>
 #include <string>
 
 #include "ComplexGeometry.h"
@@ -44,9 +45,13 @@ int main(int argc, char** argv) {
     opt.Q = (int)num("lattice", 19);
     opt.precision = (int)num("precision", LBM_F64);
     opt.mode = (int)num("mode", LBM_PARITY);
+    using clk = std::chrono::high_resolution_clock;
+    auto secs = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
     try {
         auto velSet = std::make_shared<LatticeModel>(opt.Q);
+        const auto t0 = clk::now();
         Geometry geometry(stl, velSet, spacing, 'z');
+        const auto t1 = clk::now();
         if (num("pv_preset", 0) != 0) geometry.UsePVPreset();
         if (sv.count("inlet_face")) geometry.AddInlet((int)num("inlet_face", 0), (int)num("inlet_plane", -1));
         if (sv.count("outlet_face"))
@@ -59,8 +64,18 @@ int main(int argc, char** argv) {
         sim.output_every = (int)num("output_every", 100);
         sim.output_root = sv.count("output_dir") ? sv["output_dir"] : ".";
         sim.write_output = num("write_output", 1) != 0;
+        lbm_counts c{};
+        if (lbm_get_counts(sim.handle(), &c) != LBM_OK) throw std::runtime_error("lbm_get_counts failed");
+        const auto t2 = clk::now();
         sim.Iterate();
-        std::cout << "steps " << sim.steps() << "\n";
+        const auto t3 = clk::now();
+        const int64_t n = sim.steps();
+        std::cout << "steps " << n << "\n";
+        std::cout << "active " << c.active << " next_to_wall " << c.next_to_wall << "\n";
+        std::cout << std::setprecision(4) << "geometry " << secs(t0, t1) << " s, set-up " << secs(t1, t2)
+                  << " s, iterate " << secs(t2, t3) << " s = "
+                  << (n > 0 ? (double)c.active * (double)n / secs(t2, t3) / 1e6 : 0.0)
+                  << " MLUPS (output included)\n";
     } catch (const std::exception& e) {
         std::cerr << "lbm_run: " << e.what() << "\n";
         return 1;

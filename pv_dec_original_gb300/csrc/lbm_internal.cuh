@@ -74,12 +74,16 @@ struct StepParams {
     double* nw_accm;
     // FP32-arithmetic formats keep their next-to-wall data in FP32 (GB300's
     // FP64 rate is a small fraction of FP32): normals, a ring of the last
-    // kRingSlots steps' stresses (write-only in a step), and compensated
-    // two-float accumulators (hi, lo) of tau_x, tau_y, tau_z, |tau| that the
-    // step whose slot is the ring's last folds the whole ring into
+    // kRingSlots steps' stresses (one 16-byte store per node and step), and
+    // compensated two-float accumulators (hi, lo) of tau_x, tau_y, tau_z,
+    // |tau|.  The ring has two halves of kFoldEvery slots: while a step whose
+    // index is a multiple of kFoldEvery writes one half, the first
+    // fold_blocks blocks of its launch fold the other (the previous
+    // kFoldEvery steps, in step order) into the accumulators
     const float* nw_nf;       // [3][nw_stride]
     int64_t nw_stride;        // plane stride of nw_nf (nnw + 1 rounded up to 4)
-    float* nw_ring;           // [kRingSlots][4][nnw]: step s in slot s % kRingSlots
+    float* nw_ring;           // float4 [kRingSlots][nnw]: step s in slot s % kRingSlots
+    int64_t fold_blocks;      // leading blocks of a step launch that fold the ring (set by the launcher)
     float2* nw_accf;          // [4][nnw]
     void* nw_prev;            // parity: rho, ux, uy, uz of the previous collision, [4][nnw]
     double tau;
@@ -117,7 +121,8 @@ constexpr int kStepThreads = 256;
 
 // Launchers (one per translation unit family).  kind: 0 step, 1 prologue
 // (collide the initial state), 2 materialize (post-boundary f + sums).
-constexpr int kRingSlots = 16;  // steps between folds of the FP32 stress ring
+constexpr int kRingSlots = 32;  // FP32 stress ring: two halves of kFoldEvery steps
+constexpr int kFoldEvery = 16;  // steps between folds of the FP32 stress ring
 constexpr int kNumVariants = 6;  // launch-shape variants of the step kernel (step_kernels.cuh)
 cudaError_t launch_step_f64(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 cudaError_t launch_step_f32(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
@@ -169,7 +174,7 @@ constexpr int kDeltaRow = (Q + 3) / 4 * 4;
 // Next-to-wall read-out of the FP32 formats into doubles [5][nnw]: |tau| of
 // step `last` (ring slot; -1: none, wss_ckpt: restored values), then the
 // accumulators of tau_x, tau_y, tau_z, |tau| plus ring slots 0 .. pending-1.
-cudaError_t nw_readout_f32(const float2* accf, const float* ring, int64_t nnw, int pending, int last,
+cudaError_t nw_readout_f32(const float2* accf, const float* ring, int64_t nnw, int first, int pending, int last,
                            const float* wss_ckpt, double* out, cudaStream_t st);
 
 // Message returned by lbm_last_global_error() (capi.cu).

@@ -446,18 +446,40 @@ __device__ __forceinline__ void comp_add(float2& acc, float v) {
     acc.y += c;
 }
 
-// Every kRingSlots-th step: add the ring's slots 0 .. kRingSlots-2 and this
-// step's stresses t, in step order, to next-to-wall node nw's accumulators.
-static __device__ __noinline__ void fold_ring(const StepParams& P, int nw, const float (&t)[4]) {
-#pragma unroll 1
-    for (int k = 0; k < 4; ++k) {
-        float2 acc = P.nw_accf[k * P.nnw + nw];
-#pragma unroll 5
-        for (int j = 0; j < kRingSlots - 1; ++j) comp_add(acc, P.nw_ring[((int64_t)j * 4 + k) * P.nnw + nw]);
-        comp_add(acc, t[k]);
-        P.nw_accf[k * P.nnw + nw] = acc;
+// Fold one half of the FP32 stress ring (slots half * kFoldEvery ..
+// + kFoldEvery - 1, i.e. kFoldEvery consecutive steps in step order) into
+// next-to-wall node nw's compensated accumulators.
+__device__ __forceinline__ void fold_half(const StepParams& P, int64_t nw, int half) {
+    const float4* __restrict__ ring = reinterpret_cast<const float4*>(P.nw_ring);
+    float2 acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = P.nw_accf[k * P.nnw + nw];
+#pragma unroll 4
+    for (int j = 0; j < kFoldEvery; ++j) {
+        const float4 v = ring[(int64_t)(half * kFoldEvery + j) * P.nnw + nw];
+        comp_add(acc[0], v.x);
+        comp_add(acc[1], v.y);
+        comp_add(acc[2], v.z);
+        comp_add(acc[3], v.w);
     }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) P.nw_accf[k * P.nnw + nw] = acc[k];
 }
+
+// The fold blocks of a step launch (the first P.fold_blocks blocks, BT
+// threads each): at a step whose index is a multiple of kFoldEvery, fold
+// the half of the ring this step does not write.
+__device__ __forceinline__ void fold_blocks_work(const StepParams& P, int64_t block, int bt) {
+    const int64_t step = *P.step_base;
+    if (step % kFoldEvery != 0) return;
+    const int64_t nw = block * bt + threadIdx.x;
+    if (nw >= P.nnw) return;
+    const int writing = (int)((step % kRingSlots) / kFoldEvery);
+    fold_half(P, nw, 1 - writing);
+}
+
+// The same as a kernel of its own, after a step launch without fold blocks.
+static __global__ void k_fold_ring(const StepParams P) { fold_blocks_work(P, blockIdx.x, blockDim.x); }
 
 // ---------------------------------------------------------------------------
 // Block reduction of the read-out sums (rho - 1, momentum, per-BC flux).
@@ -622,12 +644,8 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
                     wss_stress<Q>(g, r, ux, uy, uz, nr, P.wss_phys_f, t);
                 }
                 t[3] = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-                // this step's slot of the ring; the ring's last slot folds
-                // all kRingSlots steps, in step order, into the accumulators
-                float* __restrict__ ring = P.nw_ring + (int64_t)slot * 4 * P.nnw + nw;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) ring[k * P.nnw] = t[k];
-                if (slot == kRingSlots - 1) fold_ring(P, nw, t);
+                // this step's slot of the ring (folded kFoldEvery steps later)
+                reinterpret_cast<float4*>(P.nw_ring)[(int64_t)slot * P.nnw + nw] = make_float4(t[0], t[1], t[2], t[3]);
             }
         }
         if constexpr (MODE == MODE_PARITY) {
@@ -741,16 +759,25 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
 #pragma unroll
         for (int k = 0; k < kPartialStride; ++k) part[k] = 0.0;
     }
-    const int64_t a = (int64_t)blockIdx.x * BT + threadIdx.x;
+    int64_t blk = blockIdx.x;
+    if constexpr (KIND == KIND_STEP) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
+        if constexpr (Store<S>::offset) {
+            // leading blocks: the stress ring's fold (FP32-arithmetic formats)
+            if (blk < P.fold_blocks) {
+                fold_blocks_work(P, blk, BT);
+                return;
+            }
+            blk -= P.fold_blocks;
+        }
+    }
+    const int64_t a = blk * BT + threadIdx.x;
     if (a < P.nact) {
         // the node's word and its boundary-list entry (-1 for most nodes),
         // loaded side by side
         const uint64_t word = __ldg(P.act_word + a);
         const int32_t sp_entry = __ldg(P.sp_of_act + a);
         node_update<Q, S, MODE, KIND, WIDE>(P, a, word, sp_entry, part);
-    }
-    if constexpr (KIND == KIND_STEP) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
     }
     if constexpr (KIND == KIND_READOUT) block_partials<BT>(part, P.partials);
 }
@@ -769,14 +796,17 @@ constexpr Variant kVariants[kFlatVariants] = {{128, 12}, {128, 10}, {128, 8}, {2
 template <int Q, typename S, int MODE, int V>
 cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
     constexpr int BT = kVariants[V].bt, MB = kVariants[V].minb;
-    const int64_t nblocks = ceil_div(p.nact, BT);
-    if (nblocks <= 0) return cudaSuccess;
+    const bool narrow = (int64_t)Q * p.stride < ((int64_t)1 << 31);
+    const int bt = narrow ? BT : kStepThreads;  // beyond 32-bit offsets: one 64-bit shape for every variant
+    StepParams q = p;
+    q.fold_blocks = Store<S>::offset ? ceil_div(p.nnw, bt) : 0;
+    const int64_t nblocks = q.fold_blocks + ceil_div(p.nact, bt);
+    if (ceil_div(p.nact, bt) <= 0) return cudaSuccess;
     if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    if ((int64_t)Q * p.stride < ((int64_t)1 << 31))
-        step_kernel<Q, S, MODE, KIND_STEP, BT, MB, false><<<(unsigned)nblocks, BT, 0, st>>>(p);
-    else  // beyond 32-bit offsets: one 64-bit shape for every variant
-        step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true>
-            <<<(unsigned)ceil_div(p.nact, kStepThreads), kStepThreads, 0, st>>>(p);
+    if (narrow)
+        step_kernel<Q, S, MODE, KIND_STEP, BT, MB, false><<<(unsigned)nblocks, BT, 0, st>>>(q);
+    else
+        step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true><<<(unsigned)nblocks, kStepThreads, 0, st>>>(q);
     return cudaGetLastError();
 }
 
@@ -998,7 +1028,13 @@ cudaError_t launch_tile_ns(const StepParams& p, cudaStream_t st) {
 
 template <int Q, typename S>
 cudaError_t launch_tile(const StepParams& p, cudaStream_t st) {
-    return p.tile.nstage == 3 ? launch_tile_ns<Q, S, 3>(p, st) : launch_tile_ns<Q, S, 2>(p, st);
+    cudaError_t e = p.tile.nstage == 3 ? launch_tile_ns<Q, S, 3>(p, st) : launch_tile_ns<Q, S, 2>(p, st);
+    // the tiled kernel has no fold blocks: the stress ring's fold follows it
+    if (e == cudaSuccess && p.nnw > 0) {
+        k_fold_ring<<<(unsigned)ceil_div(p.nnw, 256), 256, 0, st>>>(p);
+        e = cudaGetLastError();
+    }
+    return e;
 }
 
 template <int Q, typename S, int MODE>
