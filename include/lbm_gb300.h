@@ -243,6 +243,17 @@ lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3);
  * may be NULL. */
 lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3,
                        double* acc_mag, double* osi, double* tawss);
+/* Surface read-out (the reference's commented-out design,
+ * OutputFile.cpp:431-488, FindClosestLatticePoint /
+ * InterpolateAttributesToSTLVertices): for each of nv points xyz (physical
+ * coordinates, 3 per point, e.g. STL vertices) the index into lbm_get_wss's
+ * arrays of the nearest next-to-wall node (the nodes that carry WSS, OSI
+ * and TAWSS here; the reference searched its wall-node list, whose WSS it
+ * never sets), by Euclidean distance between lattice point coordinates,
+ * ties to the lower index; -1 when none lies within max_radius lattice
+ * spacings.  distance (may be NULL) receives the physical distance. */
+lbm_status lbm_nearest_next_to_wall(lbm_handle* h, const double* xyz, int64_t nv, int max_radius, int64_t* nw_index,
+                                    double* distance);
 /* FP64 sums over the post-boundary distributions: total mass, momentum, and
  * per boundary condition the momentum along its face axis (flux). */
 lbm_status lbm_get_conservation(lbm_handle* h, double* mass, double* mom3, double* flux);

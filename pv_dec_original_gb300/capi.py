@@ -69,7 +69,7 @@ EXPORTS = [
     "lbm_moment_sums_noalloc",
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
     "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
-    "lbm_init_from_macro_device",
+    "lbm_init_from_macro_device", "lbm_nearest_next_to_wall",
 ]
 NUM_VARIANTS = 6
 
@@ -141,6 +141,7 @@ def load(build_if_missing: bool = True):
     L.lbm_ws_output.argtypes = [P, C.c_int, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, P, P]
     L.lbm_ws_gather.argtypes = [P, C.c_int64, P, C.c_int64, P, P, P]
     L.lbm_init_from_macro_device.argtypes = [P, P, P, C.c_int, P]
+    L.lbm_nearest_next_to_wall.argtypes = [P, P, C.c_int64, C.c_int, P, P]
     _lib = L
     return L
 
@@ -335,6 +336,28 @@ class Solver:
                                    _ptr(tawss)))
         return {"pt": pt, "normal": nrm.reshape(-1, 3), "wss": w, "acc": acc.reshape(-1, 3), "acc_mag": accm,
                 "osi": osi, "tawss": tawss}
+
+    def nearest_next_to_wall(self, xyz, max_radius=32):
+        """(index into wss() arrays or -1, physical distance) of the nearest
+        next-to-wall node of each point (physical coordinates, n x 3)."""
+        p = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        idx = np.zeros(len(p), np.int64)
+        dist = np.zeros(len(p), np.float64)
+        self._c(load().lbm_nearest_next_to_wall(self.h, _ptr(p), len(p), int(max_radius), _ptr(idx), _ptr(dist)))
+        return idx, dist
+
+    def wss_at_points(self, xyz, max_radius=32):
+        """WSS, OSI and TAWSS at points (e.g. STL vertices) from their nearest
+        next-to-wall node (NaN where none lies within max_radius)."""
+        idx, dist = self.nearest_next_to_wall(xyz, max_radius)
+        w = self.wss()
+        ok = idx >= 0
+        out = {"index": idx, "distance": dist}
+        for k in ("wss", "osi", "tawss"):
+            v = np.full(len(idx), np.nan)
+            v[ok] = w[k][idx[ok]]
+            out[k] = v
+        return out
 
     def conservation(self):
         m, p, fl = np.zeros(1), np.zeros(3), np.zeros(MAX_BC)

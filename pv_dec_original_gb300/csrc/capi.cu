@@ -1232,6 +1232,34 @@ lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss,
     return LBM_OK;
 }
 
+lbm_status lbm_nearest_next_to_wall(lbm_handle* h, const double* xyz, int64_t nv, int max_radius, int64_t* nw_index,
+                                    double* distance) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, nv >= 0 && (nv == 0 || (xyz && nw_index)), LBM_ERR_ARG, "null points or output");
+    REQUIRE(h, max_radius >= 1 && max_radius <= 1024, LBM_ERR_ARG, "max_radius must be in [1, 1024]");
+    if (nv == 0) return LBM_OK;
+    CK(h, cudaSetDevice(h->d.device));
+    double *d_xyz = nullptr, *d_dist = nullptr;
+    int64_t* d_idx = nullptr;
+    CK(h, cudaMalloc(&d_xyz, sizeof(double) * 3 * nv));
+    cudaError_t e = cudaMalloc(&d_idx, sizeof(int64_t) * nv);
+    if (e == cudaSuccess) e = cudaMalloc(&d_dist, sizeof(double) * nv);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess)
+        e = nearest_next_to_wall(d_xyz, nv, h->g, h->nx, h->ny, h->nz, h->d.origin, h->d.spacing, max_radius, d_idx,
+                                 d_dist, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nw_index, d_idx, sizeof(int64_t) * nv, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess && distance)
+        e = cudaMemcpyAsync(distance, d_dist, sizeof(double) * nv, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(d_xyz);
+    if (d_idx) cudaFree(d_idx);
+    if (d_dist) cudaFree(d_dist);
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("nearest_next_to_wall: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
 lbm_status lbm_get_conservation(lbm_handle* h, double* mass, double* mom3, double* flux) {
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     CK(h, cudaSetDevice(h->d.device));

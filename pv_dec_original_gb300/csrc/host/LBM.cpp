@@ -8,6 +8,7 @@
 //   end_time <t>       output_every <n>   output_dir <dir>  lattice 19|27
 //   precision 0..3 (f64, f32, f16, bf16)  mode 0|1 (parity, physics)
 //   pv_preset 1        (the reference's PV.stl inlet / outlet coordinates)
+//   write_output 0|1   write_vertices 0|1 (WSS / OSI / TAWSS at the STL's vertices)
 //   inlet_face <f> inlet_plane <p>  outlet_face <f> outlet_plane <p>
 // Defaults reproduce the reference: FP64, parity semantics, D3Q19.
 #include <chrono>
@@ -64,6 +65,7 @@ int main(int argc, char** argv) {
         sim.output_every = (int)num("output_every", 100);
         sim.output_root = sv.count("output_dir") ? sv["output_dir"] : ".";
         sim.write_output = num("write_output", 1) != 0;
+        sim.write_vertices = num("write_vertices", 0) != 0;
         lbm_counts c{};
         if (lbm_get_counts(sim.handle(), &c) != LBM_OK) throw std::runtime_error("lbm_get_counts failed");
         const auto t2 = clk::now();

@@ -5,6 +5,8 @@
 #include <cmath>
 #include <fstream>
 #include <iostream>
+#include <limits>
+#include <stdexcept>
 #include <vector>
 
 #include "Simulation.h"
@@ -93,6 +95,53 @@ bool OutputFile::WriteSurfaceAttribute(Simulation& sim, int iter) {
         const int64_t n = pt[p];
         const Point x = g.PointAt((int)(n % g.nx), (int)((n / g.nx) % g.ny), (int)(n / ((int64_t)g.nx * g.ny)));
         outfile << x.x << "," << x.y << "," << x.z << "," << wss[p] << "," << osi[p] << "," << tawss[p] << "\n";
+    }
+    return (bool)outfile;
+}
+
+std::vector<VertexAttributes> OutputFile::InterpolateAttributesToSTLVertices(Simulation& sim,
+                                                                            const std::vector<Triangle>& tris) {
+    std::vector<double> xyz(9 * tris.size());
+    for (size_t t = 0; t < tris.size(); ++t) {
+        const Triangle& T = tris[t];
+        const double v[9] = {T.x1, T.y1, T.z1, T.x2, T.y2, T.z2, T.x3, T.y3, T.z3};
+        for (int k = 0; k < 9; ++k) xyz[9 * t + k] = v[k];
+    }
+    std::vector<int64_t> idx(3 * tris.size());
+    if (lbm_nearest_next_to_wall(sim.handle(), xyz.data(), (int64_t)idx.size(), 32, idx.data(), nullptr) != LBM_OK)
+        throw std::runtime_error(std::string("lbm_nearest_next_to_wall: ") + lbm_last_error(sim.handle()));
+    std::vector<int64_t> pt;
+    std::vector<double> wss, osi, tawss;
+    sim.WallShearStress(pt, wss, osi, tawss);
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    std::vector<VertexAttributes> out(tris.size());
+    for (size_t t = 0; t < tris.size(); ++t)
+        for (int k = 0; k < 3; ++k) {
+            const int64_t e = idx[3 * t + k];
+            out[t].wss[k] = e >= 0 ? wss[e] : nan;
+            out[t].osi[k] = e >= 0 ? osi[e] : nan;
+            out[t].tawss[k] = e >= 0 ? tawss[e] : nan;
+        }
+    return out;
+}
+
+bool OutputFile::WriteSTLVertexAttribute(Simulation& sim, const std::vector<Triangle>& tris, int iter) {
+    const std::string folder = join(root, "STL_Vertices");
+    mkdir(folder.c_str(), 0777);
+    const std::string name = folder + "/" + std::to_string(iter) + "_Vertices.csv";
+    const std::vector<VertexAttributes> va = InterpolateAttributesToSTLVertices(sim, tris);
+    std::ofstream outfile(name);
+    if (!outfile.is_open()) {
+        std::cerr << "Unable to open file " << name << std::endl;
+        return false;
+    }
+    outfile << "X,Y,Z,WSS,OSI,TAWSS\n";
+    for (size_t t = 0; t < tris.size(); ++t) {
+        const Triangle& T = tris[t];
+        const double p[3][3] = {{T.x1, T.y1, T.z1}, {T.x2, T.y2, T.z2}, {T.x3, T.y3, T.z3}};
+        for (int k = 0; k < 3; ++k)
+            outfile << p[k][0] << "," << p[k][1] << "," << p[k][2] << "," << va[t].wss[k] << "," << va[t].osi[k]
+                    << "," << va[t].tawss[k] << "\n";
     }
     return (bool)outfile;
 }

@@ -8,10 +8,24 @@
 //   WriteSurfaceAttribute: FlowHemodynamics/<iter>_FlowHemodynamics.csv with
 //     "X,Y,Z,WSS,OSI,TAWSS" per next-to-wall node (OutputFile.cpp:867-938),
 //     rows in increasing lattice index.
+//   InterpolateAttributesToSTLVertices / WriteSTLVertexAttribute: the
+//     reference's commented-out surface read-out (OutputFile.cpp:431-488):
+//     every STL triangle vertex takes WSS, OSI and TAWSS from its nearest
+//     next-to-wall node (lbm_nearest_next_to_wall); written as
+//     STL_Vertices/<iter>_Vertices.csv, "X,Y,Z,WSS,OSI,TAWSS", three rows per
+//     triangle in file order.
 #pragma once
 #include <string>
+#include <vector>
+
+#include "Struct.h"
 
 class Simulation;
+
+// WSS, OSI, TAWSS at the three vertices of a triangle.
+struct VertexAttributes {
+    double wss[3], osi[3], tawss[3];
+};
 
 class OutputFile {
 public:
@@ -20,6 +34,9 @@ public:
     std::string root = ".";
     bool WriteVTK_Collective(Simulation& sim);
     bool WriteSurfaceAttribute(Simulation& sim, int iter);
+    static std::vector<VertexAttributes> InterpolateAttributesToSTLVertices(Simulation& sim,
+                                                                            const std::vector<Triangle>& tris);
+    bool WriteSTLVertexAttribute(Simulation& sim, const std::vector<Triangle>& tris, int iter);
 
 private:
     int m_outputIdx = 0;

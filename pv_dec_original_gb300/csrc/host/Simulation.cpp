@@ -166,6 +166,7 @@ void Simulation::WriteOutput(int iter) {
     file.root = output_root;
     file.WriteVTK_Collective(*this);
     file.WriteSurfaceAttribute(*this, iter);
+    if (write_vertices) file.WriteSTLVertexAttribute(*this, SubDomain_.Geometry_.globalTriangles, iter);
 }
 
 void Simulation::Macro(std::vector<double>& rho, std::vector<double>& u3) {

@@ -39,6 +39,7 @@ public:
     double end_time = 2.7;      // Iterate(): while (total_runtime <= end_time)
     int output_every = 100;     // WriteOutput cadence (Simulation.cpp:589)
     bool write_output = true;
+    bool write_vertices = false;  // also STL_Vertices/<iter>_Vertices.csv (WSS at the STL's vertices)
     bool verbose = false;
     std::string output_root = ".";
 

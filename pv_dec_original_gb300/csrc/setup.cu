@@ -415,6 +415,60 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
     return cudaSuccess;
 }
 
+// Nearest next-to-wall node of each query point (the lattice carries WSS,
+// OSI and TAWSS on those nodes).  With g the point in lattice units and c =
+// round(g), the cube of half-width R around c holds every lattice point
+// closer than R + 0.5; the cube grows (R = 1, 2, 4, ...) until the best
+// node found lies within that bound, so the result is the exact nearest
+// (ties to the lower next-to-wall index), or -1 beyond rmax.
+__global__ void k_nearest_nw(const double* __restrict__ xyz, int64_t nv, const int32_t* __restrict__ act_idx,
+                             const int32_t* __restrict__ sp_of_act, int64_t nnw, int nx, int ny, int nz, double ox,
+                             double oy, double oz, double sp, int rmax, int64_t* __restrict__ out_idx,
+                             double* __restrict__ out_dist) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const double g[3] = {(xyz[3 * v] - ox) / sp, (xyz[3 * v + 1] - oy) / sp, (xyz[3 * v + 2] - oz) / sp};
+    const int dims[3] = {nx, ny, nz};
+    int c[3];
+    for (int d = 0; d < 3; ++d) {
+        double r = rint(g[d]);
+        r = r < 0.0 ? 0.0 : (r > dims[d] - 1 ? (double)(dims[d] - 1) : r);
+        c[d] = (int)r;
+    }
+    int64_t best = -1;
+    double best_d2 = 0.0;
+    for (int R = 1; R <= rmax; R *= 2) {
+        const int lo[3] = {max(c[0] - R, 0), max(c[1] - R, 0), max(c[2] - R, 0)};
+        const int hi[3] = {min(c[0] + R, nx - 1), min(c[1] + R, ny - 1), min(c[2] + R, nz - 1)};
+        for (int k = lo[2]; k <= hi[2]; ++k)
+            for (int j = lo[1]; j <= hi[1]; ++j)
+                for (int i = lo[0]; i <= hi[0]; ++i) {
+                    const int32_t a = act_idx[((int64_t)k * ny + j) * nx + i];
+                    if (a < 0) continue;
+                    const int32_t e = sp_of_act[a];
+                    if (e < 0 || e >= nnw) continue;
+                    const double dx = i - g[0], dy = j - g[1], dz = k - g[2];
+                    const double d2 = dx * dx + dy * dy + dz * dz;
+                    if (best < 0 || d2 < best_d2 || (d2 == best_d2 && e < best)) {
+                        best = e;
+                        best_d2 = d2;
+                    }
+                }
+        if (best >= 0 && sqrt(best_d2) <= R + 0.5) break;
+    }
+    out_idx[v] = best;
+    if (out_dist) out_dist[v] = best >= 0 ? sqrt(best_d2) * sp : -1.0;
+}
+
+cudaError_t nearest_next_to_wall(const double* d_xyz, int64_t nv, const GeometryLists& g, int nx, int ny, int nz,
+                                 const double origin[3], double spacing, int rmax, int64_t* d_idx, double* d_dist,
+                                 cudaStream_t st) {
+    if (nv <= 0) return cudaSuccess;
+    k_nearest_nw<<<blocks(nv, 128), 128, 0, st>>>(d_xyz, nv, g.act_idx, g.sp_of_act, g.nnw, nx, ny, nz, origin[0],
+                                                 origin[1], origin[2], spacing, rmax, d_idx, d_dist);
+    return cudaGetLastError();
+}
+
 cudaError_t surface_normals(const double* d_tri, int64_t ntri, const int64_t* d_pts, int64_t npts, int nx, int ny,
                             const double origin[3], double spacing, double* d_out, cudaStream_t st) {
     if (npts <= 0) return cudaSuccess;

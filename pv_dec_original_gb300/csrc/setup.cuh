@@ -41,4 +41,11 @@ cudaError_t build_geometry(int Q, const uint8_t* d_mask, int nx, int ny, int nz,
                            const double origin[3], double spacing, const int32_t* d_seg_of_act, GeometryLists& out,
                            cudaStream_t st, std::string& err);
 
+// Nearest next-to-wall node (index into the next-to-wall list, -1 if none
+// within rmax lattice spacings) and its distance of each of nv points xyz
+// (physical coordinates, 3 per point).
+cudaError_t nearest_next_to_wall(const double* d_xyz, int64_t nv, const GeometryLists& g, int nx, int ny, int nz,
+                                 const double origin[3], double spacing, int rmax, int64_t* d_idx, double* d_dist,
+                                 cudaStream_t st);
+
 }  // namespace lbm

@@ -65,7 +65,7 @@ def test_lbm_run_end_to_end_vs_oracle(tmp_path, gpu_lib, oracle_lib):
     cfg = tmp_path / "run.cfg"
     cfg.write_text(f"stl {stl}\nspacing 1.0\ntau 0.8\ndt {dt!r}\nend_time {end!r}\noutput_every 30\n"
                    f"output_dir {tmp_path}\nprecision 0\nmode 0\ninlet_face 0\ninlet_plane -1\n"
-                   f"outlet_face 4\noutlet_plane -1\n")
+                   f"outlet_face 4\noutlet_plane -1\nwrite_vertices 1\n")
     r = subprocess.run([os.path.join(BUILD, "lbm_run"), str(cfg)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "steps 31" in r.stdout
@@ -86,3 +86,15 @@ def test_lbm_run_end_to_end_vs_oracle(tmp_path, gpu_lib, oracle_lib):
     assert len(csv) == len(nw["pt"])
     np.testing.assert_allclose(csv[:, 3], nw["wss"], rtol=2e-5, atol=1e-12)
     np.testing.assert_allclose(csv[:, 5], nw["tawss"], rtol=2e-5, atol=1e-12)
+    # the STL-vertex read-out: each vertex takes its nearest next-to-wall node's values
+    vx = np.loadtxt(str(tmp_path / "STL_Vertices" / "30_Vertices.csv"), delimiter=",", skiprows=1)
+    assert len(vx) == 3 * len(tri)
+    verts = tri[:, :9].reshape(-1, 3)
+    np.testing.assert_allclose(vx[:, :3], verts, rtol=1e-5, atol=1e-5)  # the CSV prints 6 digits
+    nx_, ny_, _ = dims
+    pt = np.asarray(nw["pt"])
+    ijk = np.stack([pt % nx_, (pt // nx_) % ny_, pt // (nx_ * ny_)], 1).astype(np.float64)
+    g = (verts - np.array([bb[0], bb[2], bb[4]])) / 1.0
+    near = np.argmin(((ijk[None] - g[:, None]) ** 2).sum(-1), 1)
+    np.testing.assert_array_equal(vx[:, 3], csv[near, 3])
+    np.testing.assert_array_equal(vx[:, 5], csv[near, 5])
