@@ -182,6 +182,22 @@ lbm_status lbm_set_normals_from_surface(lbm_handle* h, const double* tri12, int6
 lbm_status lbm_set_normals_from_surface_box(lbm_handle* h, const double* tri12, int64_t ntri, const double lo[3],
                                             const double hi[3]);
 
+/* Interpolated bounce-back (physics mode; the reference computes the wall
+ * distances, Geometry::CalculateWallDistances, ComplexGeometry.cpp:550-608,
+ * but never uses them).  For every missing link of the boundary list, the
+ * fraction q in [0, 1] of the link at which it meets the surface (segment-
+ * triangle intersection; the reference divides by the spacing instead of
+ * the link length, which exceeds 1 on diagonal links) replaces half-way
+ * bounce-back by the rule of Bouzidi, Firdaouss and Lallemand (2001):
+ *   q < 1/2:  f_q(x) = 2q f*_i(x) + (1 - 2q) f*_i(x + c_q)
+ *   q >= 1/2: f_q(x) = f*_i(x) / (2q) + (1 - 1/(2q)) f*_q(x)
+ * (i = opp q, the link x -> x + c_i crossing the wall; a link without a
+ * triangle, or with q < 1/2 and no fluid node at x + c_q, keeps half-way
+ * bounce-back).  ntri == 0 returns to half-way bounce-back. */
+lbm_status lbm_set_wall_distances(lbm_handle* h, const double* tri12, int64_t ntri);
+/* Boundary-list points (pt[nsp], may be NULL) and their wall distances
+ * q[nsp * Q] (entry-major; 0.5 where no link is missing or none is set). */
+lbm_status lbm_get_wall_distances(lbm_handle* h, int64_t* pt, float* q);
 /* Inlet amplitude per step: step s uses amp[s % n] (times the node's
  * profile factor and the spec's value).  Replaces InletVelocity_ =
  * getInletVelocity(t, 0.9) (Simulation.cpp:580). */

@@ -338,6 +338,7 @@ struct oracle_sim {
     oracle_bc bc[16];
     int nbc;
     int regularized;   /* physics mode: regularized collision instead of BGK */
+    float* wq;         /* physics mode: wall distance per (active, arriving q), or NULL (half-way) */
     double* amp;
     int64_t namp, step;
     double C, tawss_div;
@@ -445,7 +446,7 @@ void oracle_sim_destroy(oracle_sim* s) {
     free(s->pt); free(s->cls); free(s->nbr); free(s->f); free(s->fnew); free(s->feq);
     free(s->rho); free(s->u); free(s->prof); free(s->nw); free(s->wall); free(s->nw_n);
     free(s->wall_n); free(s->wss); free(s->acc); free(s->accm); free(s->osi); free(s->tawss);
-    free(s->amp); free(s);
+    free(s->amp); free(s->wq); free(s);
 }
 
 void oracle_sim_set_amplitude(oracle_sim* s, const double* amp, int64_t n) {
@@ -678,6 +679,76 @@ static void regularize_node(int Q, double tau, const double* f, double* fnew, co
 
 void oracle_sim_set_collision(oracle_sim* s, int regularized) { s->regularized = regularized; }
 
+/* Segment P0 -> P0 + d against one triangle (Moller and Trumbore 1997), in
+ * the library's operation order: the fraction t in [0, 1] of the segment. */
+static int seg_tri(const double* P0, const double* d, const double* T, double* t) {
+    const double e1[3] = {T[3] - T[0], T[4] - T[1], T[5] - T[2]};
+    const double e2[3] = {T[6] - T[0], T[7] - T[1], T[8] - T[2]};
+    const double pv[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2], d[0] * e2[1] - d[1] * e2[0]};
+    const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+    if (fabs(det) < 1e-300) return 0;
+    const double inv = 1.0 / det;
+    const double tv[3] = {P0[0] - T[0], P0[1] - T[1], P0[2] - T[2]};
+    const double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) * inv;
+    if (u < 0.0 || u > 1.0) return 0;
+    const double qv[3] = {tv[1] * e1[2] - tv[2] * e1[1], tv[2] * e1[0] - tv[0] * e1[2], tv[0] * e1[1] - tv[1] * e1[0]};
+    const double v = (d[0] * qv[0] + d[1] * qv[1] + d[2] * qv[2]) * inv;
+    if (v < 0.0 || u + v > 1.0) return 0;
+    *t = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) * inv;
+    return *t >= 0.0 && *t <= 1.0;
+}
+
+/* Wall distances for the interpolated bounce-back (no reference counterpart
+ * in use: Geometry::CalculateWallDistances, ComplexGeometry.cpp:550-608,
+ * computes such distances and never applies them; it divides by the spacing
+ * rather than the link length).  For active node a and arriving population
+ * q whose source x + c_i (i = opp q) is not active: the smallest fraction
+ * t in [0, 1] of the link x -> x + c_i at which a triangle (file order) is
+ * met; 0.5 where none is, and where the source exists. */
+void oracle_sim_set_wall_distances(oracle_sim* s, const double* tri12, int64_t ntri) {
+    const int Q = s->Q;
+    free(s->wq);
+    s->wq = NULL;
+    if (ntri <= 0) return;
+    int c[27 * 3];
+    double w[27];
+    int op[27];
+    oracle_lattice(Q, c, w, op);
+    s->wq = (float*)malloc(sizeof(float) * (size_t)(s->nact * Q + 1));
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t a = 0; a < s->nact; ++a) {
+        const int64_t n = s->pt[a];
+        const int i = (int)(n % s->nx), j = (int)((n / s->nx) % s->ny), k = (int)(n / ((int64_t)s->nx * s->ny));
+        const double P0[3] = {s->org[0] + i * s->spacing, s->org[1] + j * s->spacing, s->org[2] + k * s->spacing};
+        for (int q = 0; q < Q; ++q) {
+            float qw = 0.5f;
+            const int ci = op[q];
+            if (s->nbr[a * Q + ci] < 0) {
+                const double d[3] = {c[3 * ci] * s->spacing, c[3 * ci + 1] * s->spacing, c[3 * ci + 2] * s->spacing};
+                const double lo[3] = {fmin(P0[0], P0[0] + d[0]), fmin(P0[1], P0[1] + d[1]), fmin(P0[2], P0[2] + d[2])};
+                const double hi[3] = {fmax(P0[0], P0[0] + d[0]), fmax(P0[1], P0[1] + d[1]), fmax(P0[2], P0[2] + d[2])};
+                double best = 2.0;
+                for (int64_t r = 0; r < ntri; ++r) {
+                    const double* T = tri12 + 12 * r;
+                    if (fmax(T[0], fmax(T[3], T[6])) < lo[0] || fmin(T[0], fmin(T[3], T[6])) > hi[0] ||
+                        fmax(T[1], fmax(T[4], T[7])) < lo[1] || fmin(T[1], fmin(T[4], T[7])) > hi[1] ||
+                        fmax(T[2], fmax(T[5], T[8])) < lo[2] || fmin(T[2], fmin(T[5], T[8])) > hi[2])
+                        continue;
+                    double t;
+                    if (seg_tri(P0, d, T, &t) && t < best) best = t;
+                }
+                if (best <= 1.0) qw = (float)best;
+            }
+            s->wq[a * Q + q] = qw;
+        }
+    }
+}
+
+void oracle_sim_get_wall_distances(const oracle_sim* s, float* q) {
+    const int64_t n = s->nact * s->Q;
+    for (int64_t k = 0; k < n; ++k) q[k] = s->wq ? s->wq[k] : 0.5f;
+}
+
 /* Library physics semantics: traction of the viscous stress
  * -(1 - 1/(2 tau)) sum_a f_neq c c, projected on the wall plane; f_neq from
  * the same post-boundary f (no time lag). */
@@ -731,7 +802,22 @@ void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads) {
             for (int64_t b = 0; b < na; ++b)
                 for (int q = 0; q < Q; ++q) {
                     int32_t src = s->nbr[b * Q + opp_of(Q, q)];
-                    g[b * Q + q] = src >= 0 ? s->fnew[(int64_t)src * Q + q] : s->fnew[b * Q + opp_of(Q, q)];
+                    double v = src >= 0 ? s->fnew[(int64_t)src * Q + q] : s->fnew[b * Q + opp_of(Q, q)];
+                    if (src < 0 && s->wq) {
+                        /* interpolated bounce-back (Bouzidi, Firdaouss and Lallemand 2001) */
+                        const double qw = (double)s->wq[b * Q + q];
+                        const int32_t behind = s->nbr[b * Q + q];
+                        if (qw < 0.5) {
+                            if (behind >= 0) {
+                                const double A = 2.0 * qw;
+                                v = A * v + (1.0 - A) * s->fnew[(int64_t)behind * Q + opp_of(Q, q)];
+                            }
+                        } else {
+                            const double A = 1.0 / (2.0 * qw);
+                            v = A * v + (1.0 - A) * s->fnew[b * Q + q];
+                        }
+                    }
+                    g[b * Q + q] = v;
                 }
             memcpy(s->f, g, sizeof(double) * (size_t)(na * Q));
         }

@@ -72,6 +72,10 @@ void oracle_sim_compute_normals(oracle_sim* s, const double* tri12, int64_t ntri
 void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads);
 /* Physics mode: regularized collision (1) instead of BGK (0, default). */
 void oracle_sim_set_collision(oracle_sim* s, int regularized);
+/* physics mode: interpolated bounce-back with wall distances from the
+ * triangles (ntri = 0: half-way); distances per (active node, arriving q) */
+void oracle_sim_set_wall_distances(oracle_sim* s, const double* tri12, int64_t ntri);
+void oracle_sim_get_wall_distances(const oracle_sim* s, float* q);
 
 int64_t oracle_sim_nactive(const oracle_sim* s);
 int64_t oracle_sim_nnw(const oracle_sim* s);

@@ -61,6 +61,8 @@ def lib():
         L.oracle_sim_compute_normals.argtypes = [C.c_void_p, P(d), C.c_int64, C.c_int]
         L.oracle_sim_step.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.oracle_sim_set_collision.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_sim_set_wall_distances.argtypes = [C.c_void_p, np.ctypeslib.ndpointer(np.float64), C.c_int64]
+        L.oracle_sim_get_wall_distances.argtypes = [C.c_void_p, np.ctypeslib.ndpointer(np.float32)]
         L.oracle_sim_nactive.argtypes = [C.c_void_p]
         L.oracle_sim_nactive.restype = C.c_int64
         L.oracle_sim_nnw.argtypes = [C.c_void_p]
@@ -158,6 +160,18 @@ class Sim:
     def set_collision(self, regularized):
         """Physics mode: regularized collision (True) or BGK (False)."""
         lib().oracle_sim_set_collision(self.h, int(bool(regularized)))
+
+    def set_wall_distances(self, tri12):
+        """Physics mode: interpolated bounce-back with wall distances from
+        the triangles (an empty array: half-way bounce-back)."""
+        t = np.ascontiguousarray(tri12, np.float64).reshape(-1, 12)
+        lib().oracle_sim_set_wall_distances(self.h, t if len(t) else np.zeros((1, 12)), len(t))
+
+    def wall_distances(self):
+        """Wall distance per (active node, arriving population), [nact, Q]."""
+        q = np.zeros(self.nactive * self.Q, np.float32)
+        lib().oracle_sim_get_wall_distances(self.h, q)
+        return q.reshape(-1, self.Q)
 
     @property
     def nactive(self):

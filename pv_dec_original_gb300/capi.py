@@ -69,7 +69,7 @@ EXPORTS = [
     "lbm_moment_sums_noalloc",
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
     "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
-    "lbm_init_from_macro_device", "lbm_nearest_next_to_wall",
+    "lbm_init_from_macro_device", "lbm_nearest_next_to_wall", "lbm_set_wall_distances", "lbm_get_wall_distances",
 ]
 NUM_VARIANTS = 6
 
@@ -142,6 +142,8 @@ def load(build_if_missing: bool = True):
     L.lbm_ws_gather.argtypes = [P, C.c_int64, P, C.c_int64, P, P, P]
     L.lbm_init_from_macro_device.argtypes = [P, P, P, C.c_int, P]
     L.lbm_nearest_next_to_wall.argtypes = [P, P, C.c_int64, C.c_int, P, P]
+    L.lbm_set_wall_distances.argtypes = [P, P, C.c_int64]
+    L.lbm_get_wall_distances.argtypes = [P, P, P]
     _lib = L
     return L
 
@@ -336,6 +338,20 @@ class Solver:
                                    _ptr(tawss)))
         return {"pt": pt, "normal": nrm.reshape(-1, 3), "wss": w, "acc": acc.reshape(-1, 3), "acc_mag": accm,
                 "osi": osi, "tawss": tawss}
+
+    def set_wall_distances(self, tri12):
+        """Interpolated bounce-back (physics mode) with wall distances from
+        the surface; an empty array returns to half-way bounce-back."""
+        t = np.ascontiguousarray(tri12, np.float64).reshape(-1, 12)
+        self._c(load().lbm_set_wall_distances(self.h, _ptr(t) if len(t) else None, len(t)))
+
+    def wall_distances(self):
+        """(boundary-list points, wall distance per entry and arriving population [nsp, Q])."""
+        n = self.counts()["special"]
+        pt = np.zeros(n, np.int64)
+        q = np.zeros(n * self.Q, np.float32)
+        self._c(load().lbm_get_wall_distances(self.h, _ptr(pt), _ptr(q)))
+        return pt, q.reshape(n, self.Q)
 
     def nearest_next_to_wall(self, xyz, max_radius=32):
         """(index into wss() arrays or -1, physical distance) of the nearest

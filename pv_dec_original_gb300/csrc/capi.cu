@@ -47,6 +47,7 @@ struct lbm_handle {
     float *nw_nf = nullptr, *nw_wssf = nullptr;  // FP32-arithmetic formats
     int64_t nw_stride = 0;                         // plane stride of nw_nf
     int32_t* tile_plan = nullptr;                  // tiled step kernel (physics, FP32-arithmetic formats)
+    float* sp_q = nullptr;                         // interpolated bounce-back: wall distances [Q][nsp]
     TileGeom tile{};
     float* nw_ring = nullptr;                      // float4 [kRingSlots][nnw]
     double* nw_out = nullptr;                      // read-out staging, [5][nnw]
@@ -181,7 +182,7 @@ void free_geometry(lbm_handle* h) {
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
                     h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf, h->tile_plan,
-                    h->nw_ring, h->nw_out};
+                    h->nw_ring, h->nw_out, h->sp_q};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     g = GeometryLists();
@@ -194,6 +195,7 @@ void free_geometry(lbm_handle* h) {
     h->nw_nf = h->nw_wssf = nullptr;
     h->tile_plan = nullptr;
     h->tile = TileGeom{};
+    h->sp_q = nullptr;
     h->nw_accf = nullptr;
     h->nw_ring = nullptr;
     h->nw_out = nullptr;
@@ -256,6 +258,7 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.nbc = h->nbc;
     p.sp_bc = h->g.sp_bc;
     p.sp_flux = h->sp_flux;
+    p.sp_q = h->d.mode == LBM_PHYSICS ? h->sp_q : nullptr;
     p.flags = h->flags;
     p.act_idx = h->g.act_idx;
     p.partials = h->partials;
@@ -949,6 +952,48 @@ lbm_status lbm_set_normals_from_surface_box(lbm_handle* h, const double* tri12, 
     cudaFree(d_pt);
     cudaFree(d_out);
     if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("normals: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+lbm_status lbm_set_wall_distances(lbm_handle* h, const double* tri12, int64_t ntri) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, h->d.mode == LBM_PHYSICS, LBM_ERR_ARG, "interpolated bounce-back is a physics-mode rule");
+    REQUIRE(h, ntri >= 0 && (ntri == 0 || tri12), LBM_ERR_ARG, "null triangles");
+    CK(h, cudaSetDevice(h->d.device));
+    CK(h, cudaStreamSynchronize(h->st));
+    drop_graph(h);  // the table pointer is baked into captured launches
+    if (ntri == 0) {
+        if (h->sp_q) cudaFree(h->sp_q);
+        h->sp_q = nullptr;
+        return LBM_OK;
+    }
+    if (!h->sp_q) CK(h, dalloc(h, &h->sp_q, sizeof(float) * h->d.Q * (h->g.nsp + 1)));
+    double* d_tri = nullptr;
+    CK(h, cudaMalloc(&d_tri, sizeof(double) * 12 * ntri));
+    cudaError_t e = cudaMemcpyAsync(d_tri, tri12, sizeof(double) * 12 * ntri, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess)
+        e = wall_distances(h->d.Q, d_tri, ntri, h->g, h->nx, h->ny, h->d.origin, h->d.spacing, h->sp_q, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(d_tri);
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("wall distances: ") + cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_wall_distances(lbm_handle* h, int64_t* pt, float* q) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    CK(h, cudaSetDevice(h->d.device));
+    const int64_t n = h->g.nsp;
+    const int Q = h->d.Q;
+    if (pt && n) CK(h, cudaMemcpyAsync(pt, h->g.sp_pt, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, h->st));
+    std::vector<float> planes((size_t)Q * n, 0.5f);
+    if (q && n && h->sp_q)
+        CK(h, cudaMemcpyAsync(planes.data(), h->sp_q, sizeof(float) * Q * n, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    if (q)
+        for (int64_t e = 0; e < n; ++e)
+            for (int k = 0; k < Q; ++k) q[e * Q + k] = planes[(size_t)k * n + e];
     return LBM_OK;
 }
 

@@ -65,6 +65,7 @@ struct StepParams {
     const double* sp_prof;    // inlet profile factor
     const int32_t* sp_bc;     // boundary-condition rule of a boundary-list entry (-1: none)
     double* sp_flux;          // read-out: momentum along the rule's face axis, per entry
+    const float* sp_q;        // physics: wall distance of each missing link, [Q][nsp] (null: half-way bounce-back)
     void* stale;              // parity: previous post-boundary f, [q][nsp] in the arithmetic type
     // next-to-wall accumulators
     int64_t nnw;

@@ -469,6 +469,77 @@ cudaError_t nearest_next_to_wall(const double* d_xyz, int64_t nv, const Geometry
     return cudaGetLastError();
 }
 
+// Wall distance of every missing link of the boundary list, for the
+// interpolated bounce-back: for entry s and arriving population q whose
+// source x - c_q (= x + c_i, i = opp q) is not active, the fraction t in
+// [0, 1] along the link x -> x + c_i at which it first meets a triangle
+// (segment-triangle intersection after Moller and Trumbore, 1997, in FP64),
+// stored as q[qi * nsp + s]; 0.5 (half-way) where no link is missing or no
+// triangle crosses it.  Triangles are tested in file order; the smallest t
+// wins.  tri: ntri rows of x1 y1 z1 x2 y2 z2 x3 y3 z3 nx ny nz.
+__device__ __forceinline__ bool seg_tri(const double* P0, const double* d, const double* T, double& t) {
+    const double e1[3] = {T[3] - T[0], T[4] - T[1], T[5] - T[2]};
+    const double e2[3] = {T[6] - T[0], T[7] - T[1], T[8] - T[2]};
+    const double pv[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2], d[0] * e2[1] - d[1] * e2[0]};
+    const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+    if (fabs(det) < 1e-300) return false;
+    const double inv = 1.0 / det;
+    const double tv[3] = {P0[0] - T[0], P0[1] - T[1], P0[2] - T[2]};
+    const double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) * inv;
+    if (u < 0.0 || u > 1.0) return false;
+    const double qv[3] = {tv[1] * e1[2] - tv[2] * e1[1], tv[2] * e1[0] - tv[0] * e1[2], tv[0] * e1[1] - tv[1] * e1[0]};
+    const double v = (d[0] * qv[0] + d[1] * qv[1] + d[2] * qv[2]) * inv;
+    if (v < 0.0 || u + v > 1.0) return false;
+    t = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) * inv;
+    return t >= 0.0 && t <= 1.0;
+}
+
+template <int Q>
+__global__ void k_wall_q(const int64_t* __restrict__ sp_pt, const uint32_t* __restrict__ sp_miss, int64_t nsp,
+                         int nx, int ny, double ox, double oy, double oz, double sp, const double* __restrict__ tri,
+                         int64_t ntri, float* __restrict__ out) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nsp) return;
+    const int64_t n = sp_pt[e];
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+    const double P0[3] = {ox + i * sp, oy + j * sp, oz + k * sp};
+    const uint32_t miss = sp_miss[e];
+    for (int q = 0; q < Q; ++q) {
+        float qw = 0.5f;
+        const int ci = Lat<Q>::opp(q);
+        if ((miss >> ci) & 1u) {
+            const double d[3] = {Lat<Q>::cx(ci) * sp, Lat<Q>::cy(ci) * sp, Lat<Q>::cz(ci) * sp};
+            const double lo[3] = {fmin(P0[0], P0[0] + d[0]), fmin(P0[1], P0[1] + d[1]), fmin(P0[2], P0[2] + d[2])};
+            const double hi[3] = {fmax(P0[0], P0[0] + d[0]), fmax(P0[1], P0[1] + d[1]), fmax(P0[2], P0[2] + d[2])};
+            double best = 2.0;
+            for (int64_t r = 0; r < ntri; ++r) {
+                const double* T = tri + 12 * r;
+                // bounding-box rejection (exact: a hit lies in both boxes)
+                if (fmax(T[0], fmax(T[3], T[6])) < lo[0] || fmin(T[0], fmin(T[3], T[6])) > hi[0] ||
+                    fmax(T[1], fmax(T[4], T[7])) < lo[1] || fmin(T[1], fmin(T[4], T[7])) > hi[1] ||
+                    fmax(T[2], fmax(T[5], T[8])) < lo[2] || fmin(T[2], fmin(T[5], T[8])) > hi[2])
+                    continue;
+                double t;
+                if (seg_tri(P0, d, T, t) && t < best) best = t;
+            }
+            if (best <= 1.0) qw = (float)best;
+        }
+        out[(int64_t)q * nsp + e] = qw;
+    }
+}
+
+cudaError_t wall_distances(int Q, const double* d_tri, int64_t ntri, const GeometryLists& g, int nx, int ny,
+                           const double origin[3], double spacing, float* d_q, cudaStream_t st) {
+    if (g.nsp <= 0) return cudaSuccess;
+    if (Q == 19)
+        k_wall_q<19><<<blocks(g.nsp, 128), 128, 0, st>>>(g.sp_pt, g.sp_miss, g.nsp, nx, ny, origin[0], origin[1],
+                                                        origin[2], spacing, d_tri, ntri, d_q);
+    else
+        k_wall_q<27><<<blocks(g.nsp, 128), 128, 0, st>>>(g.sp_pt, g.sp_miss, g.nsp, nx, ny, origin[0], origin[1],
+                                                        origin[2], spacing, d_tri, ntri, d_q);
+    return cudaGetLastError();
+}
+
 cudaError_t surface_normals(const double* d_tri, int64_t ntri, const int64_t* d_pts, int64_t npts, int nx, int ny,
                             const double origin[3], double spacing, double* d_out, cudaStream_t st) {
     if (npts <= 0) return cudaSuccess;

@@ -48,4 +48,9 @@ cudaError_t nearest_next_to_wall(const double* d_xyz, int64_t nv, const Geometry
                                  const double origin[3], double spacing, int rmax, int64_t* d_idx, double* d_dist,
                                  cudaStream_t st);
 
+// Wall distances of the boundary list's missing links (interpolated
+// bounce-back): d_q [Q][nsp], see k_wall_q.
+cudaError_t wall_distances(int Q, const double* d_tri, int64_t ntri, const GeometryLists& g, int nx, int ny,
+                           const double origin[3], double spacing, float* d_q, cudaStream_t st);
+
 }  // namespace lbm

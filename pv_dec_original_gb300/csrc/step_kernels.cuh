@@ -678,6 +678,38 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
     }
 }
 
+// Interpolated bounce-back (Bouzidi, Firdaouss and Lallemand 2001) for the
+// missing links of node a, whose g[q] holds the half-way value f*_opp(q)(x):
+//   q_w < 1/2: g[q] = 2 q_w f*_i(x) + (1 - 2 q_w) f*_i(x + c_q)
+//   q_w >= 1/2: g[q] = f*_i(x) / (2 q_w) + (1 - 1/(2 q_w)) f*_q(x),  i = opp q.
+// Out of line: only nodes next to a wall take it, and inlined it would
+// cost every node registers.
+template <int Q, typename S, bool WIDE>
+static __device__ __noinline__ void interpolate_walls(const StepParams& P, int64_t a, uint64_t word, int32_t e,
+                                                       uint32_t miss, typename Store<S>::real (&g)[Q]) {
+    using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
+    using R = typename Store<S>::real;
+    constexpr int DR = kDeltaRow<Q>;
+    const S* __restrict__ fin_a = static_cast<const S*>(P.fin) + (I)a;
+    const I st = (I)P.stride;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (q == Lat<Q>::REST || !((miss >> Lat<Q>::opp(q)) & 1u)) continue;
+        const float qw = __ldg(P.sp_q + (int64_t)q * P.nsp + e);
+        R A, X;
+        if (qw < 0.5f) {
+            if ((miss >> q) & 1u) continue;  // no fluid node at x + c_q: half-way
+            A = (R)2 * (R)qw;
+            const int32_t dq = __ldg(P.seg_delta + word_segment(word) * DR + Lat<Q>::opp(q));
+            X = Store<S>::template load<Q>(fin_a + (I)(Lat<Q>::opp(q) * st + dq), q);
+        } else {
+            A = (R)1 / ((R)2 * (R)qw);
+            X = Store<S>::template load<Q>(fin_a + (I)(q * st), q);
+        }
+        g[q] = A * g[q] + ((R)1 - A) * X;
+    }
+}
+
 // One node's update: pull, boundary rules, wall shear stress, collision and
 // store (or the read-out sums).
 template <int Q, typename S, int MODE, int KIND, bool WIDE>
@@ -743,6 +775,10 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
                 off = q * st + (src_missing ? 0 : dl[q]);
             }
             g[q] = Store<S>::template load<Q>(fin_a + off, q);  // w_opp(q) == w_q: same decode
+        }
+        if constexpr (MODE == MODE_PHYSICS) {
+            // interpolated bounce-back where wall distances are set
+            if (miss != 0 && P.sp_q != nullptr) interpolate_walls<Q, S, WIDE>(P, a, word, sp_entry, miss, g);
         }
     }
 
@@ -1047,9 +1083,10 @@ cudaError_t launch_family(int kind, int variant, const StepParams& p, cudaStream
             case 4: return launch_step_variant<Q, S, MODE, 4>(p, st);
             case 5:
                 // the tiled kernel where a plan exists (physics, FP32-arithmetic
-                // formats, 32-bit offsets); the default shape elsewhere
+                // formats, 32-bit offsets, half-way bounce-back); the default
+                // shape elsewhere
                 if constexpr (Store<S>::offset && MODE == MODE_PHYSICS) {
-                    if (p.tile.ntiles > 0 && p.tile_plan && (int64_t)Q * p.stride < ((int64_t)1 << 31))
+                    if (p.tile.ntiles > 0 && p.tile_plan && !p.sp_q && (int64_t)Q * p.stride < ((int64_t)1 << 31))
                         return launch_tile<Q, S>(p, st);
                 }
                 return launch_step_variant<Q, S, MODE, Store<S>::offset ? 0 : 4>(p, st);

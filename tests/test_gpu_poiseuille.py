@@ -67,3 +67,48 @@ def test_gpu_c1_poiseuille(gpu_lib):
     wa = 2.0 * nu * umax * rn / R ** 2
     rel = np.abs(w["wss"][sel] / (rho.mean() * wa) - 1.0)
     assert np.median(rel) < 0.15, np.median(rel)
+
+
+def _c1_profile_error(capi, walls, steps=5000):
+    """u_z L2 error over the middle third of C1 against the Poiseuille profile
+    of the true radius R carrying the measured flux,
+    u = 2 Qf / (pi R^2) (1 - r^2/R^2): the shape error the wall rule causes
+    (the staircase inlet sets the flux itself)."""
+    from pv_dec_original_gb300 import geometry as G
+    surf = G.config_c1_cylinder()
+    tri = surf.tri12()
+    mask, desc = capi.voxelize(tri, 1.0)
+    bb = np.array(desc.bbox[:])
+    org = (bb[0], bb[2], bb[4])
+    fl = np.argwhere(mask > 0)
+    kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
+    cx, cy = surf.meta["center"]
+    R, umax, tau = 10.0, 0.05, 0.8
+    s = capi.Solver(19, capi.LBM_F64, capi.LBM_PHYSICS, tau, 1.0, org, 1.0, 1.0)
+    s.set_geometry(mask, [capi.bc_spec(capi.LBM_BC_VELOCITY, "z-", kin, umax, 1, cx, cy, R),
+                          capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)])
+    s.set_normals(tri)
+    s.set_inlet_table([1.0])
+    if walls:
+        s.set_wall_distances(tri)
+    s.step(steps)
+    _, u = s.macro()
+    x = fl[:, 2] + org[0] - cx
+    y = fl[:, 1] + org[1] - cy
+    r2 = x * x + y * y
+    kmid = (fl[:, 0] > kin + 33) & (fl[:, 0] < kout - 33)
+    ks = np.unique(fl[kmid, 0])
+    Qf = np.mean([u[kmid][fl[kmid, 0] == k, 2].sum() for k in ks])  # unit cell area
+    ua = 2.0 * Qf / (np.pi * R ** 2) * np.clip(1.0 - r2[kmid] / R ** 2, 0.0, None)
+    return float(np.linalg.norm(u[kmid, 2] - ua) / np.linalg.norm(ua))
+
+
+def test_gpu_c1_interpolated_walls_more_accurate(gpu_lib):
+    """Interpolated bounce-back places the wall where the surface is, so the
+    profile's shape error against the true radius drops below half-way
+    bounce-back's (which puts the wall half a spacing outside the last fluid
+    node, i.e. on the staircase, not on the circle)."""
+    e_half = _c1_profile_error(gpu_lib, False)
+    e_int = _c1_profile_error(gpu_lib, True)
+    print("C1 profile shape error: half-way", e_half, "interpolated", e_int)
+    assert e_int < 0.7 * e_half, (e_half, e_int)

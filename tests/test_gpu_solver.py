@@ -73,8 +73,9 @@ def test_gpu_low_precision_parity_vs_fp64(gpu_lib, prec, tol):
     assert np.max(np.abs(g_rho - r_rho)) <= 10 * tol
 
 
-def _physics_case(capi, oracle, Q, precision, nsteps=40, tau=0.7, collision=0):
-    """A stenosed tube with velocity inlet (z-min) and pressure outlet (z-max)."""
+def _physics_case(capi, oracle, Q, precision, nsteps=40, tau=0.7, collision=0, walls=False):
+    """A stenosed tube with velocity inlet (z-min) and pressure outlet (z-max);
+    walls=True: interpolated bounce-back with the surface's wall distances."""
     from pv_dec_original_gb300 import geometry as G
     surf = G.stenosed_tube(5.0, 40.0, 0.5, 0.2, center=(7.3, 7.1), z0=1.6, h=1.4, seed=3)
     surf = G.add_bbox_anchors(surf, (0.0, 0.0, 0.0), (14.0, 14.0, 44.0))
@@ -91,11 +92,15 @@ def _physics_case(capi, oracle, Q, precision, nsteps=40, tau=0.7, collision=0):
     s.set_geometry(mask, [capi.bc_spec(**b) for b in bcs])
     s.set_normals(tri)
     s.set_inlet_table(amp)
+    if walls:
+        s.set_wall_distances(tri)
     s.step(nsteps)
     cls = classify(mask, [(2, kin), (2, kout)], Q)
     o = oracle.Sim(Q, oracle.PHYSICS, cls, org, 1.0, tau, bcs)
     o.set_amplitude(amp)
     o.set_collision(collision)
+    if walls:
+        o.set_wall_distances(tri)
     o.set_wss(1.0, 1.0)
     o.compute_normals(tri)
     o.step(nsteps)
@@ -298,3 +303,42 @@ def test_gpu_regularized_stable_where_bgk_diverges(gpu_lib):
     assert out[capi.LBM_COLLISION_BGK] is None
     umax, rmin, rmax = out[capi.LBM_COLLISION_REGULARIZED]
     assert umax < 0.15 and 0.95 < rmin and rmax < 1.05, out
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+def test_gpu_interpolated_walls_match_oracle(gpu_lib, oracle_lib, Q):
+    """Interpolated bounce-back: the wall distances (segment-triangle
+    intersections in FP64, rounded to FP32) are bit-identical to the
+    oracle's, and FP64 distributions after 40 steps agree to 1e-13."""
+    s, o = _physics_case(gpu_lib, oracle_lib, Q, gpu_lib.LBM_F64, walls=True)
+    pt, q = s.wall_distances()
+    opt, _ = o.active()
+    qo = o.wall_distances()
+    row = {int(p): a for a, p in enumerate(opt)}
+    ref = qo[[row[int(p)] for p in pt]]
+    assert np.array_equal(q, ref)
+    # a real share of the missing links found the surface (not all half-way)
+    assert np.mean((q != 0.5) & (q >= 0.0)) > 0.05
+    f = s.distributions()
+    fo, _, _ = o.f()
+    assert np.max(np.abs(f - fo)) <= 1e-13
+    # and the walls change the flow (the rule is in effect)
+    h, _ = _physics_case(gpu_lib, oracle_lib, Q, gpu_lib.LBM_F64, walls=False)
+    assert np.max(np.abs(h.distributions() - f)) > 1e-6
+
+
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-5), ("f16", 4e-3)])
+def test_gpu_interpolated_walls_precision(gpu_lib, oracle_lib, prec, tol):
+    s, o = _physics_case(gpu_lib, oracle_lib, 19, prec, walls=True)
+    _, u = s.macro()
+    fo, _, _ = o.f()
+    c, _, _ = oracle_lib.lattice(19)
+    u_o = (fo @ c) / fo.sum(axis=1)[:, None]  # moments of the same post-boundary state
+    assert np.linalg.norm(u - u_o) / np.linalg.norm(u_o) <= tol
+
+
+def test_gpu_wall_distances_need_physics_mode(gpu_lib):
+    d = load(fixtures("sim")[0])
+    s, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64, split=0)
+    with pytest.raises(gpu_lib.LbmError):
+        s.set_wall_distances(d["tri12"])
