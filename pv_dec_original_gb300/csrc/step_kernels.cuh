@@ -682,10 +682,10 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
 // missing links of node a, whose g[q] holds the half-way value f*_opp(q)(x):
 //   q_w < 1/2: g[q] = 2 q_w f*_i(x) + (1 - 2 q_w) f*_i(x + c_q)
 //   q_w >= 1/2: g[q] = f*_i(x) / (2 q_w) + (1 - 1/(2 q_w)) f*_q(x),  i = opp q.
-// Out of line: only nodes next to a wall take it, and inlined it would
-// cost every node registers.
+// Compiled only into the kernels launched when wall distances are set
+// (WALLS), so the half-way kernels carry none of it.
 template <int Q, typename S, bool WIDE>
-static __device__ __noinline__ void interpolate_walls(const StepParams& P, int64_t a, uint64_t word, int32_t e,
+__device__ __forceinline__ void interpolate_walls(const StepParams& P, int64_t a, uint64_t word, int32_t e,
                                                        uint32_t miss, typename Store<S>::real (&g)[Q]) {
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
     using R = typename Store<S>::real;
@@ -712,7 +712,7 @@ static __device__ __noinline__ void interpolate_walls(const StepParams& P, int64
 
 // One node's update: pull, boundary rules, wall shear stress, collision and
 // store (or the read-out sums).
-template <int Q, typename S, int MODE, int KIND, bool WIDE>
+template <int Q, typename S, int MODE, int KIND, bool WIDE, bool WALLS = false>
 __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a, const uint64_t word,
                                             const int32_t sp_entry, double (&part)[kPartialStride]) {
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
@@ -776,9 +776,9 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
             }
             g[q] = Store<S>::template load<Q>(fin_a + off, q);  // w_opp(q) == w_q: same decode
         }
-        if constexpr (MODE == MODE_PHYSICS) {
-            // interpolated bounce-back where wall distances are set
-            if (miss != 0 && P.sp_q != nullptr) interpolate_walls<Q, S, WIDE>(P, a, word, sp_entry, miss, g);
+        if constexpr (MODE == MODE_PHYSICS && WALLS) {
+            // interpolated bounce-back (the launcher picks this kernel when wall distances are set)
+            if (miss != 0) interpolate_walls<Q, S, WIDE>(P, a, word, sp_entry, miss, g);
         }
     }
 
@@ -788,7 +788,8 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
 // WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
 // lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
 // One thread per active node.
-template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1, bool WIDE = true>
+template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1, bool WIDE = true,
+          bool WALLS = false>
 __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
     double part[kPartialStride];
     if constexpr (KIND == KIND_READOUT) {
@@ -813,7 +814,7 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
         // loaded side by side
         const uint64_t word = __ldg(P.act_word + a);
         const int32_t sp_entry = __ldg(P.sp_of_act + a);
-        node_update<Q, S, MODE, KIND, WIDE>(P, a, word, sp_entry, part);
+        node_update<Q, S, MODE, KIND, WIDE, WALLS>(P, a, word, sp_entry, part);
     }
     if constexpr (KIND == KIND_READOUT) block_partials<BT>(part, P.partials);
 }
@@ -834,15 +835,27 @@ cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
     constexpr int BT = kVariants[V].bt, MB = kVariants[V].minb;
     const bool narrow = (int64_t)Q * p.stride < ((int64_t)1 << 31);
     const int bt = narrow ? BT : kStepThreads;  // beyond 32-bit offsets: one 64-bit shape for every variant
+    constexpr bool PHYS = MODE == MODE_PHYSICS;
+    const bool walls = PHYS && p.sp_q != nullptr;  // interpolated bounce-back: one shape, (128, 8)
+    const int bw = walls && narrow ? 128 : bt;
     StepParams q = p;
-    q.fold_blocks = Store<S>::offset ? ceil_div(p.nnw, bt) : 0;
-    const int64_t nblocks = q.fold_blocks + ceil_div(p.nact, bt);
-    if (ceil_div(p.nact, bt) <= 0) return cudaSuccess;
+    q.fold_blocks = Store<S>::offset ? ceil_div(p.nnw, bw) : 0;
+    const int64_t nblocks = q.fold_blocks + ceil_div(p.nact, bw);
+    if (ceil_div(p.nact, bw) <= 0) return cudaSuccess;
     if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    if (narrow)
+    if (walls) {
+        if constexpr (PHYS) {
+            if (narrow)
+                step_kernel<Q, S, MODE, KIND_STEP, 128, 8, false, true><<<(unsigned)nblocks, 128, 0, st>>>(q);
+            else
+                step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true, true>
+                    <<<(unsigned)nblocks, kStepThreads, 0, st>>>(q);
+        }
+    } else if (narrow) {
         step_kernel<Q, S, MODE, KIND_STEP, BT, MB, false><<<(unsigned)nblocks, BT, 0, st>>>(q);
-    else
+    } else {
         step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true><<<(unsigned)nblocks, kStepThreads, 0, st>>>(q);
+    }
     return cudaGetLastError();
 }
 
@@ -1097,10 +1110,16 @@ cudaError_t launch_family(int kind, int variant, const StepParams& p, cudaStream
     const int64_t nblocks = ceil_div(p.nact, kStepThreads);
     if (nblocks <= 0) return cudaSuccess;
     if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    if (kind == KIND_PROLOGUE)
+    if (kind == KIND_PROLOGUE) {
         step_kernel<Q, S, MODE, KIND_PROLOGUE><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p);
-    else
+    } else if (MODE == MODE_PHYSICS && p.sp_q != nullptr) {
+        // the read-out's pull applies the same interpolated bounce-back
+        if constexpr (MODE == MODE_PHYSICS)
+            step_kernel<Q, S, MODE, KIND_READOUT, kStepThreads, 1, true, true>
+                <<<(unsigned)nblocks, kStepThreads, 0, st>>>(p);
+    } else {
         step_kernel<Q, S, MODE, KIND_READOUT><<<(unsigned)nblocks, kStepThreads, 0, st>>>(p);
+    }
     return cudaGetLastError();
 }
 
