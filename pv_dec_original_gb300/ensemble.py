@@ -33,9 +33,10 @@ from . import waveform
 
 class Ensemble:
     def __init__(self, members, Q=19, precision="f16", tau=0.55, gap=1, tawss_div=1.0, device=0, periods=None,
-                 steady=False):
+                 steady=False, collision=0):
         """members: dicts with "surface" (geometry.Surface), "center" (tube axis
         x, y in surface coordinates), "radius", "inlet_mean", "period".
+        collision: capi.LBM_COLLISION_BGK or LBM_COLLISION_REGULARIZED.
         steady: a constant inlet at each member's mean instead of its waveform."""
         self.members = members
         parts = []
@@ -71,7 +72,8 @@ class Ensemble:
             oz += nz + gap
         self.mask = packed
         self.member_masks = [p[1] for p in parts]
-        self.solver = capi.Solver(Q, precision, capi.LBM_PHYSICS, tau, 1.0, (0.0, 0.0, 0.0), 1.0, tawss_div, device)
+        self.solver = capi.Solver(Q, precision, capi.LBM_PHYSICS, tau, 1.0, (0.0, 0.0, 0.0), 1.0, tawss_div, device,
+                                  collision=collision)
         self.solver.set_geometry(packed, bcs)
         for idx, (t, m) in enumerate(zip(self.tri, members)):
             lo = (-1e30, -1e30, self.z0[idx] - 0.5)

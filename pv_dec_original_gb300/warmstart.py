@@ -352,22 +352,25 @@ def zero_output(prior):
 
 def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4):
     """Seeded stenosed tubes (and every k-th a small Y-bifurcation) filling
-    a fixed box (x, y, z) between an inlet at z = 0 and an outlet at z = top."""
+    a fixed box (x, y, z) between an inlet at z = 0 and an outlet at z = top;
+    radii scale with the box width (4-9 lattice units for tubes, 4-5.5 for
+    bifurcation parents at a width of 32)."""
     from . import geometry as G
     rng = np.random.default_rng(seed)
     nx, ny, nz = box
+    sc = nx / 32.0
     out = []
     for m in range(n):
         mean = float(rng.uniform(0.01, 0.04))
         period = float(rng.uniform(2000.0, 6000.0))
         cx, cy = 0.5 * (nx - 1) + 0.173, 0.5 * (ny - 1) + 0.061
         if bifurcation_every and m % bifurcation_every == bifurcation_every - 1:
-            r = float(rng.uniform(4.0, 5.5))
+            r = float(rng.uniform(4.0, 5.5)) * sc
             s = G.y_bifurcation(r, 0.72 * r, float(rng.uniform(8.0, 14.0)), z_in=1.3, z_out=nz - 1.4,
                                 z_split=0.5 * nz, center=(cx, cy), seed=seed * 1000 + m, h=1.0)
             kind = "bifurcation"
         else:
-            r = float(rng.uniform(4.0, 9.0))
+            r = float(rng.uniform(4.0, 9.0)) * sc
             s = G.stenosed_tube(r, nz - 2.7, float(rng.uniform(0.2, 0.7)), float(rng.uniform(0.0, 0.3)),
                                 center=(cx, cy), z0=1.3, seed=seed * 1000 + m, h=max(1.0, r / 8.0))
             kind = "stenosed_tube"
@@ -382,11 +385,11 @@ def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4):
     return out
 
 
-def steady_ensemble(members, tau=0.8, steps=40000, precision="f32", device=0):
+def steady_ensemble(members, tau=0.8, steps=40000, precision="f32", device=0, collision=0):
     """Steady solutions (constant inlet at each member's mean) of all members
     advanced as one packed lattice; returns per member (mask, rho, u)."""
     from .ensemble import Ensemble
-    ens = Ensemble(members, 19, precision, tau, device=device, steady=True)
+    ens = Ensemble(members, 19, precision, tau, device=device, steady=True, collision=collision)
     ens.solver.set_graph_steps(32)
     ens.step(steps)
     rho, u, mem = ens.macro()
@@ -472,14 +475,15 @@ def steps_to_wss(solver, ref, tol=0.01, check=100, max_steps=60000, hold=3):
     return None
 
 
-def single_lattice(member, tau=0.8, precision="f64", device=0):
+def single_lattice(member, tau=0.8, precision="f64", device=0, collision=0):
     """One member as its own lattice with a constant inlet (steady problem)."""
     tri = member["surface"].tri12()
     mask, vd = capi.voxelize(tri, 1.0)
     bb = np.array(vd.bbox[:])
     fl = np.argwhere(mask > 0)
     kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
-    s = capi.Solver(19, precision, capi.LBM_PHYSICS, tau, 1.0, (bb[0], bb[2], bb[4]), 1.0, 1.0, device)
+    s = capi.Solver(19, precision, capi.LBM_PHYSICS, tau, 1.0, (bb[0], bb[2], bb[4]), 1.0, 1.0, device,
+                    collision=collision)
     s.set_geometry(mask, [capi.bc_spec(capi.LBM_BC_VELOCITY, "z-", kin, 1.0, 1, member["center"][0],
                                        member["center"][1], member["radius"]),
                           capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)])
