@@ -84,6 +84,11 @@ __host__ __device__ constexpr int lat_c(int q, int axis) {
 // The relative scaling by 1/w gives every direction the same range; the
 // factor 1024 keeps FP16 offsets down to ~6e-8 normal while +-0.5 relative
 // offsets stay far below the FP16 maximum.  BF16 has FP32's exponent range.
+// FP16 and BF16 ("scaled") keep their storage units g = d / unit_q through
+// the collision (unit_q = w_q / 1024 and w_q): a load or store is a bare
+// conversion, the moments weight g by unit_q (a multiply-add in place of an
+// add), and the equilibrium in these units, (w_q / unit_q) (B + ...), has
+// the same factor geq (1024, 1) for every direction.
 enum Precision : int { P_F64 = 0, P_F32 = 1, P_F16 = 2, P_BF16 = 3 };
 
 template <typename S> struct Store;
@@ -91,6 +96,7 @@ template <typename S> struct Store;
 template <> struct Store<double> {
     using real = double;
     static constexpr bool offset = false;
+    static constexpr bool scaled = false;
     template <int Q>
     __device__ static __forceinline__ real load(const double* p, int q) { return *p; }
     template <int Q>
@@ -102,6 +108,7 @@ template <> struct Store<double> {
 template <> struct Store<float> {
     using real = float;
     static constexpr bool offset = true;
+    static constexpr bool scaled = false;
     template <int Q>
     __device__ static __forceinline__ real load(const float* p, int q) { return __ldg(p); }
     template <int Q>
@@ -113,36 +120,34 @@ template <> struct Store<float> {
 template <> struct Store<__half> {
     using real = float;
     static constexpr bool offset = true;
+    static constexpr bool scaled = true;
     static constexpr float S = 1024.0f;
+    static constexpr float geq = S;  // w_q / unit_q
     template <int Q>
-    __device__ static __forceinline__ real load(const __half* p, int q) {
-        return __half2float(__ldg(p)) * ((float)Lat<Q>::w(q) * (1.0f / S));
-    }
+    __host__ __device__ static constexpr float unit(int q) { return (float)(Lat<Q>::w(q) / 1024.0); }
     template <int Q>
-    __device__ static __forceinline__ real decode(__half v, int q) {
-        return __half2float(v) * ((float)Lat<Q>::w(q) * (1.0f / S));
-    }
+    __device__ static __forceinline__ real load(const __half* p, int q) { return __half2float(__ldg(p)); }
     template <int Q>
-    __device__ static __forceinline__ __half pack(real d, int q) {
-        return __float2half_rn(d * (S / (float)Lat<Q>::w(q)));
-    }
+    __device__ static __forceinline__ real decode(__half v, int q) { return __half2float(v); }
+    template <int Q>
+    __device__ static __forceinline__ __half pack(real g, int q) { return __float2half_rn(g); }
 };
 
 template <> struct Store<__nv_bfloat16> {
     using real = float;
     static constexpr bool offset = true;
+    static constexpr bool scaled = true;
+    static constexpr float geq = 1.0f;
+    template <int Q>
+    __host__ __device__ static constexpr float unit(int q) { return (float)Lat<Q>::w(q); }
     template <int Q>
     __device__ static __forceinline__ real load(const __nv_bfloat16* p, int q) {
-        return __bfloat162float(__ldg(p)) * (float)Lat<Q>::w(q);
+        return __bfloat162float(__ldg(p));
     }
     template <int Q>
-    __device__ static __forceinline__ real decode(__nv_bfloat16 v, int q) {
-        return __bfloat162float(v) * (float)Lat<Q>::w(q);
-    }
+    __device__ static __forceinline__ real decode(__nv_bfloat16 v, int q) { return __bfloat162float(v); }
     template <int Q>
-    __device__ static __forceinline__ __nv_bfloat16 pack(real d, int q) {
-        return __float2bfloat16_rn(d * (1.0f / (float)Lat<Q>::w(q)));
-    }
+    __device__ static __forceinline__ __nv_bfloat16 pack(real g, int q) { return __float2bfloat16_rn(g); }
 };
 
 }  // namespace lbm

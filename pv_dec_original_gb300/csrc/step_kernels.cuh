@@ -241,11 +241,8 @@ __device__ __forceinline__ void relax_regularized(R (&f)[Q], R r, R A, R ux, R u
 // second-order equilibrium on D3Q19 and D3Q27): tau = C (Pi n - (n.Pi n) n),
 // the per-direction sum of Simulation.cpp:880-898 regrouped.  (r, u) are the
 // moments the equilibrium is taken at.
-template <int Q>
-__device__ __forceinline__ void wss_stress(const float (&d)[Q], float r, float ux, float uy, float uz,
-                                           const float n[3], float C, float t[3]) {
-    float m[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    second_moments<Q>(d, m);
+__device__ __forceinline__ void wss_from_moments(const float (&m)[6], float r, float ux, float uy, float uz,
+                                                 const float n[3], float C, float t[3]) {
     const float A = 1.0f + r, r3 = r * (1.0f / 3.0f);
     const float Axx = m[0] - (r3 + A * ux * ux), Ayy = m[1] - (r3 + A * uy * uy), Azz = m[2] - (r3 + A * uz * uz);
     const float Axy = m[3] - A * ux * uy, Axz = m[4] - A * ux * uz, Ayz = m[5] - A * uy * uz;
@@ -256,6 +253,88 @@ __device__ __forceinline__ void wss_stress(const float (&d)[Q], float r, float u
     t[0] = C * (px - nn * n[0]);
     t[1] = C * (py - nn * n[1]);
     t[2] = C * (pz - nn * n[2]);
+}
+
+template <int Q>
+__device__ __forceinline__ void wss_stress(const float (&d)[Q], float r, float ux, float uy, float uz,
+                                           const float n[3], float C, float t[3]) {
+    float m[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    second_moments<Q>(d, m);
+    wss_from_moments(m, r, ux, uy, uz, n, C, t);
+}
+
+// ---------------------------------------------------------------------------
+// Scaled formats (FP16, BF16): arithmetic on the storage units g = d / unit_q.
+
+template <int Q, typename S>
+__device__ __forceinline__ void units_to_offsets(float (&g)[Q]) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) g[q] *= Store<S>::template unit<Q>(q);
+}
+
+template <int Q, typename S>
+__device__ __forceinline__ void offsets_to_units(float (&g)[Q]) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) g[q] *= 1.0f / Store<S>::template unit<Q>(q);
+}
+
+// r = rho - 1 = sum unit_q g_q and u = (sum unit_q c_q g_q) / (1 + r).
+template <int Q, typename S>
+__device__ __forceinline__ void moments_units(const float (&g)[Q], float& r, float& ux, float& uy, float& uz) {
+    float d = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float u = Store<S>::template unit<Q>(q);
+        d = fmaf(u, g[q], d);
+        if (Lat<Q>::cx(q) != 0) px = fmaf((float)Lat<Q>::cx(q) * u, g[q], px);
+        if (Lat<Q>::cy(q) != 0) py = fmaf((float)Lat<Q>::cy(q) * u, g[q], py);
+        if (Lat<Q>::cz(q) != 0) pz = fmaf((float)Lat<Q>::cz(q) * u, g[q], pz);
+    }
+    const float inv = __frcp_rn(1.0f + d);
+    ux = px * inv; uy = py * inv; uz = pz * inv;
+    r = d;
+}
+
+// Second moments sum_q unit_q g_q c_qa c_qb from the pair sums.
+template <int Q, typename S, int q = 0>
+__device__ __forceinline__ void second_moments_units(const float (&g)[Q], float (&m)[6]) {
+    if constexpr (q < Q) {
+        constexpr int o = Lat<Q>::opp(q);
+        if constexpr (q < o) {
+            constexpr int cx = Lat<Q>::cx(q), cy = Lat<Q>::cy(q), cz = Lat<Q>::cz(q);
+            constexpr float u = Store<S>::template unit<Q>(q);
+            const float p = g[q] + g[o];
+            if constexpr (cx * cx != 0) m[0] = fmaf(u, p, m[0]);
+            if constexpr (cy * cy != 0) m[1] = fmaf(u, p, m[1]);
+            if constexpr (cz * cz != 0) m[2] = fmaf(u, p, m[2]);
+            if constexpr (cx * cy != 0) m[3] = fmaf((float)(cx * cy) * u, p, m[3]);
+            if constexpr (cx * cz != 0) m[4] = fmaf((float)(cx * cz) * u, p, m[4]);
+            if constexpr (cy * cz != 0) m[5] = fmaf((float)(cy * cz) * u, p, m[5]);
+        }
+        second_moments_units<Q, S, q + 1>(g, m);
+    }
+}
+
+// BGK relaxation in storage units, pairs (q, opp q): with K = omega geq,
+// g* = (1 - omega) g + K (B + 4.5 A du^2 +|- 3 A du)  -- relax_pairs with the
+// per-direction weight gone (geq is the same for every q).
+template <int Q, int q = 0>
+__device__ __forceinline__ void relax_pairs_units(float (&g)[Q], float A, float B, float ux, float uy, float uz,
+                                                  float K, float K3, float om1) {
+    if constexpr (q < Q) {
+        constexpr int o = Lat<Q>::opp(q);
+        if constexpr (q == Lat<Q>::REST) {
+            g[q] = om1 * g[q] + K * B;
+        } else if constexpr (q < o) {
+            const float du = cdot<Q, q, float>(ux, uy, uz);
+            const float t = A * du;
+            const float sym = K * ((4.5f * t) * du + B);
+            const float anti = K3 * t;
+            g[q] = om1 * g[q] + (sym + anti);
+            g[o] = om1 * g[o] + (sym - anti);
+        }
+        relax_pairs_units<Q, q + 1>(g, A, B, ux, uy, uz, K, K3, om1);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -542,10 +621,21 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
     using R = typename Store<S>::real;
     constexpr bool OFF = Store<S>::offset;
+    constexpr bool SC = Store<S>::scaled;  // g in storage units (FP16, BF16)
     S* __restrict__ fout = static_cast<S*>(P.fout);
     const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
     constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
     const I ai = (I)a, st = (I)P.stride;
+    // f == 0 in the values g holds
+    auto exact_zero = [](R v, int q) {
+        if constexpr (SC) return v == -(R)Store<S>::geq;
+        else return is_exact_zero<Q, R, OFF>(v, q);
+    };
+    // rho - 1 (or rho) and u of g
+    auto mom = [](const R (&v)[Q], R& r, R& ux, R& uy, R& uz) {
+        if constexpr (SC) moments_units<Q, S>(v, r, ux, uy, uz);
+        else moments<Q, R, OFF>(v, r, ux, uy, uz);
+    };
     int nw = -1;  // next-to-wall index: boundary-list entries below nnw
     if (lng) {
         // ---- boundary-list node: history, boundary rules
@@ -558,7 +648,7 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
             } else if (!direct) {
 #pragma unroll
                 for (int q = 0; q < Q; ++q)
-                    if (((miss >> Lat<Q>::opp(q)) & 1u) || is_exact_zero<Q, R, OFF>(g[q], q))
+                    if (((miss >> Lat<Q>::opp(q)) & 1u) || exact_zero(g[q], q))
                         g[q] = stale[q * P.nsp + s];
             }
         }
@@ -572,7 +662,9 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
                     if (t < 0) t += len;
                     amp = __ldg(P.amp + __ldg(P.wave_off + B.wave) + t);
                 }
+                if constexpr (SC) units_to_offsets<Q, S>(g);
                 apply_bc<Q, R, OFF>(g, B, amp, __ldg(P.sp_prof + s));
+                if constexpr (SC) offsets_to_units<Q, S>(g);
             } else if (MODE == MODE_PARITY && c == CLS_WALL) {
                 // ApplyWallBc: in place, direction order (Simulation.cpp:846-861)
 #pragma unroll
@@ -583,7 +675,7 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
         if constexpr (KIND == KIND_READOUT) {
             if (c >= CLS_BC0) {
                 R r, ux, uy, uz;
-                moments<Q, R, OFF>(g, r, ux, uy, uz);
+                mom(g, r, ux, uy, uz);
                 const double rho = OFF ? 1.0 + (double)r : (double)r;
                 const double j[3] = {rho * ux, rho * uy, rho * uz};
                 P.sp_flux[s] = j[bc_axis(P.bct[__ldg(P.sp_bc + s)])];
@@ -593,26 +685,31 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
     } else if constexpr (MODE == MODE_PARITY && KIND == KIND_STEP) {
         bool zero = false;
 #pragma unroll
-        for (int q = 0; q < Q; ++q) zero |= is_exact_zero<Q, R, OFF>(g[q], q);
+        for (int q = 0; q < Q; ++q) zero |= exact_zero(g[q], q);
         if (zero) atomicOr(P.flags, FLAG_EXACT_ZERO);
     }
 
     if constexpr (KIND == KIND_READOUT) {
         R r, ux, uy, uz;
-        moments<Q, R, OFF>(g, r, ux, uy, uz);
+        mom(g, r, ux, uy, uz);
         const double rho = OFF ? 1.0 + (double)r : (double)r;
         part[0] = OFF ? (double)r : rho - 1.0;
         part[1] = rho * ux; part[2] = rho * uy; part[3] = rho * uz;
         if (P.out_f) {
 #pragma unroll
-            for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
+            for (int q = 0; q < Q; ++q) {
+                if constexpr (SC)
+                    P.out_f[a * Q + q] = Lat<Q>::w(q) + (double)Store<S>::template unit<Q>(q) * (double)g[q];
+                else
+                    P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
+            }
         }
     } else {
         // ---- moments of the post-boundary populations: they serve the
         // wall shear stress (physics), the next step's lagged stress
         // (parity) and the collision
         R r, ux, uy, uz;
-        moments<Q, R, OFF>(g, r, ux, uy, uz);
+        mom(g, r, ux, uy, uz);
         R* __restrict__ prev = static_cast<R*>(P.nw_prev);
         if (KIND == KIND_STEP && nw >= 0) {
             if constexpr (!OFF) {
@@ -637,11 +734,14 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
             } else {
                 // FP32 arithmetic end to end
                 float t[4];
+                float m[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                if constexpr (SC) second_moments_units<Q, S>(g, m);
+                else second_moments<Q>(g, m);
                 if constexpr (MODE == MODE_PARITY) {
-                    wss_stress<Q>(g, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw], prev[3 * P.nnw + nw], nr,
-                                  P.wss_C_f, t);
+                    wss_from_moments(m, prev[nw], prev[P.nnw + nw], prev[2 * P.nnw + nw], prev[3 * P.nnw + nw], nr,
+                                     P.wss_C_f, t);
                 } else {
-                    wss_stress<Q>(g, r, ux, uy, uz, nr, P.wss_phys_f, t);
+                    wss_from_moments(m, r, ux, uy, uz, nr, P.wss_phys_f, t);
                 }
                 t[3] = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
                 // this step's slot of the ring (folded kFoldEvery steps later)
@@ -661,8 +761,21 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
         }
         // ---- collide and store (every lane)
         if (MODE == MODE_PHYSICS && P.collision == LBM_COLLISION_REGULARIZED) {
-            if constexpr (OFF) relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f);
-            else relax_regularized<Q, R>(g, r, r, ux, uy, uz, (R)P.inv_tau);
+            if constexpr (SC) {
+                units_to_offsets<Q, S>(g);
+                relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f);
+                offsets_to_units<Q, S>(g);
+            } else if constexpr (OFF) {
+                relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f);
+            } else {
+                relax_regularized<Q, R>(g, r, r, ux, uy, uz, (R)P.inv_tau);
+            }
+        } else if constexpr (SC) {
+            const float om = P.inv_tau_f;
+            const float A = 1.0f + r;
+            const float B = r - 1.5f * A * (ux * ux + uy * uy + uz * uz);
+            const float K = om * Store<S>::geq;
+            relax_pairs_units<Q>(g, A, B, ux, uy, uz, K, 3.0f * K, 1.0f - om);
         } else if constexpr (OFF) {
             const float om = P.inv_tau_f;
             const float A = 1.0f + r;
@@ -1139,8 +1252,12 @@ cudaError_t launch_typed(int Q, int mode, int kind, int variant, const StepParam
 template <int Q, typename S>
 __device__ __forceinline__ S encode_full(double f, int q) {
     using R = typename Store<S>::real;
-    if constexpr (Store<S>::offset) return Store<S>::template pack<Q>((R)(f - Lat<Q>::w(q)), q);
-    else return Store<S>::template pack<Q>((R)f, q);
+    if constexpr (Store<S>::scaled)
+        return Store<S>::template pack<Q>((R)((f - Lat<Q>::w(q)) / (double)Store<S>::template unit<Q>(q)), q);
+    else if constexpr (Store<S>::offset)
+        return Store<S>::template pack<Q>((R)(f - Lat<Q>::w(q)), q);
+    else
+        return Store<S>::template pack<Q>((R)f, q);
 }
 
 // Every plane entry of every active node := f = w (Node.cpp:30-37).
