@@ -823,19 +823,27 @@ __device__ __forceinline__ void interpolate_walls(const StepParams& P, int64_t a
     }
 }
 
-// One node's update: pull, boundary rules, wall shear stress, collision and
-// store (or the read-out sums).
+// What the pull of a node leaves for node_finish besides its populations.
+struct Pulled {
+    bool lng;        // boundary-list work
+    int c;           // class
+    uint32_t miss;   // missing-link mask
+    int64_t s;       // boundary-list entry (lng)
+    float nr[3];     // next-to-wall normal (FP32-arithmetic formats)
+    int slot;        // stress-ring slot
+};
+
+// The pull of node a: its populations after streaming (and, with WALLS,
+// interpolated bounce-back) into g, plus its boundary-list data.
 template <int Q, typename S, int MODE, int KIND, bool WIDE, bool WALLS = false>
-__device__ __forceinline__ void node_update(const StepParams& P, const int64_t a, const uint64_t word,
-                                            const int32_t sp_entry, double (&part)[kPartialStride]) {
+__device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, const uint64_t word,
+                                          const int32_t sp_entry, typename Store<S>::real (&g)[Q], Pulled& pl) {
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
     using R = typename Store<S>::real;
     constexpr bool OFF = Store<S>::offset;
     constexpr int DR = kDeltaRow<Q>;
     const S* __restrict__ fin = static_cast<const S*>(P.fin);
-    S* __restrict__ fout = static_cast<S*>(P.fout);
     const bool direct = (KIND == KIND_PROLOGUE) || (KIND == KIND_READOUT && P.direct);
-    constexpr bool parity_readout = (KIND == KIND_READOUT && MODE == MODE_PARITY);
     const uint32_t miss = word_miss(word);  // zero on interior nodes
     const int c = word_class(word);
     // Boundary-list work: in parity mode every boundary-list node (history
@@ -864,7 +872,6 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
     const I ai = (I)a, st = (I)P.stride;
     // the node's own entry of plane 0; plane q is q * stride further
     const S* __restrict__ fin_a = fin + ai;
-    R g[Q];
     if (direct) {
 #pragma unroll
         for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin_a + q * st, q);
@@ -895,7 +902,23 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
         }
     }
 
-    node_finish<Q, S, MODE, KIND, WIDE>(P, a, word, s, lng, c, miss, g, nr, slot, part);
+    pl.lng = lng;
+    pl.c = c;
+    pl.miss = miss;
+    pl.s = s;
+    pl.nr[0] = nr[0]; pl.nr[1] = nr[1]; pl.nr[2] = nr[2];
+    pl.slot = slot;
+}
+
+// One node's update: pull, boundary rules, wall shear stress, collision and
+// store (or the read-out sums).
+template <int Q, typename S, int MODE, int KIND, bool WIDE, bool WALLS = false>
+__device__ __forceinline__ void node_update(const StepParams& P, const int64_t a, const uint64_t word,
+                                            const int32_t sp_entry, double (&part)[kPartialStride]) {
+    typename Store<S>::real g[Q];
+    Pulled pl;
+    pull_node<Q, S, MODE, KIND, WIDE, WALLS>(P, a, word, sp_entry, g, pl);
+    node_finish<Q, S, MODE, KIND, WIDE>(P, a, word, pl.s, pl.lng, pl.c, pl.miss, g, pl.nr, pl.slot, part);
 }
 
 // WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
