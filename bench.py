@@ -525,6 +525,12 @@ def max_over_ranks(dist, x, backend_device=None):
     return float(t.item())
 
 
+def aggregate_mlups(ws, units_per_rank, steps, seconds_max):
+    """Whole-job MLUPS: every rank advances its own replica (units_per_rank
+    active nodes, `steps` steps); the slowest rank's time counts."""
+    return ws * units_per_rank * steps / seconds_max / 1e6
+
+
 def run_ours(args):
     ws, rank, local, dist = dist_setup("nccl")
     from pv_dec_original_gb300 import capi
@@ -564,7 +570,7 @@ def run_ours(args):
     total_ms = sum(ms)
     total_ms_max = max_over_ranks(dist, total_ms, dev_t)
     mean_ms = total_ms / len(ms)
-    value = ws * active * args.steps / (total_ms_max * 1e-3) / 1e6
+    value = aggregate_mlups(ws, active, args.steps, total_ms_max * 1e-3)
     bpl = BYTES_PER_LU[(args.Q, args.precision)]
     peak, peak_kind = read_peaks()
     achieved = active * bpl / (mean_ms * 1e-3) / 1e9
@@ -572,7 +578,10 @@ def run_ours(args):
 
     # secondary: FP16-offset storage on the same lattice (the precision config's storage)
     extra = {}
-    if args.precision == "f32" and not args.quick:
+    # the secondary measurements run at N = 1 only (a multi-GPU run reports
+    # the replicated headline)
+    extras = ws == 1 and not args.quick
+    if args.precision == "f32" and extras:
         s16, _ = make_solver(capi, mask, surf, tri, args.Q, "f16", origin, local)
         s16.step(args.warmup)
         if args.variant is not None:
@@ -588,13 +597,13 @@ def run_ours(args):
 
     # batched ensemble (64 seeded stenosed tubes, FP16 storage): one packed
     # lattice, one launch per step, vs the same members as 64 lattices
-    if not args.quick and args.Q == 19:
+    if extras and args.Q == 19:
         extra["d3q27"] = d3q27_extra(capi, cr, mask, surf, tri, origin, local, flush, args.steps)
-    if not args.quick and not args.no_precision:
+    if extras and not args.no_precision:
         extra["precision_c3"] = precision_extra(capi, cr, local)
-    if not args.quick and not args.no_ensemble:
+    if extras and not args.no_ensemble:
         extra["ensemble_c4"] = ensemble_extra(capi, cr, local, args.Q)
-    if not args.quick and not args.no_warmstart:
+    if extras and not args.no_warmstart:
         extra["warmstart_c5"] = warmstart_extra(local)
 
     # end to end through the C ABI: per e2e step, H2D of a 100-step inlet
@@ -663,7 +672,7 @@ def run_ours(args):
                          "bytes_per_lu": bpl, "peak_source": peak_kind,
                          "kernel": f"lbm::step_kernel<{args.Q}, {args.precision}, physics, step>"},
             "cpu_baseline": cpu,
-            "e2e": {"value": ws * active * B / e2e_t / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
+            "e2e": {"value": aggregate_mlups(ws, active, B, e2e_t), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "step": f"{B} LBM steps per call batch + WSS/OSI/TAWSS and rho/u read-back (pinned host buffers)"},
             "gpu_launches": launches,
