@@ -944,6 +944,15 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
             blk -= P.fold_blocks;
         }
     }
+    if constexpr (KIND == KIND_STEP) {
+        // blocks from both ends of the active-node order first, meeting in
+        // the middle: a vessel along the slowest lattice axis has its inlet
+        // and outlet planes (the slowest blocks) at the two ends, and
+        // starting them first keeps them out of the launch's tail
+        // (bifurcation: FP32 step -6%, FP16 -4.5%)
+        const int64_t nm = (P.nact + BT - 1) / BT;
+        blk = (blk & 1) ? nm - 1 - (blk >> 1) : (blk >> 1);
+    }
     const int64_t a = blk * BT + threadIdx.x;
     if (a < P.nact) {
         // the node's word and its boundary-list entry (-1 for most nodes),
