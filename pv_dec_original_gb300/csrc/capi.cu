@@ -51,6 +51,7 @@ struct lbm_handle {
     TileGeom tile{};
     float* nw_ring = nullptr;                      // float4 [kRingSlots][nnw]
     double* nw_out = nullptr;                      // read-out staging, [5][nnw]
+    double* nw_fields = nullptr;                   // lbm_get_wss outputs, assembled on the device
     float2* nw_accf = nullptr;
     bool wss_from_ckpt = false;  // |tau| of the last step comes from a checkpoint (nw_wssf), not the ring
     // inlet waveforms: host tables, device concatenation with per-wave offset / length
@@ -182,7 +183,7 @@ void free_geometry(lbm_handle* h) {
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
                     h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf, h->tile_plan,
-                    h->nw_ring, h->nw_out, h->sp_q};
+                    h->nw_ring, h->nw_out, h->sp_q, h->nw_fields};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     g = GeometryLists();
@@ -199,6 +200,7 @@ void free_geometry(lbm_handle* h) {
     h->nw_accf = nullptr;
     h->nw_ring = nullptr;
     h->nw_out = nullptr;
+    h->nw_fields = nullptr;
     drop_graph(h);
     h->has_geo = h->has_state = false;
     h->geo_bytes = 0;
@@ -1166,13 +1168,17 @@ lbm_status lbm_get_distributions(lbm_handle* h, double* f) {
 lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3) {
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     CK(h, cudaSetDevice(h->d.device));
-    int rc = readout(h, true);
-    if (rc) return rc;
+    REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state: call lbm_init_equilibrium / lbm_set_geometry first");
     const int64_t na = h->g.nact;
     if (!h->macro) CK(h, dalloc(h, &h->macro, sizeof(double) * 4 * (na + 1)));
     double* d_rho = h->macro;
     double* d_u = h->macro + (na + 1);
-    CK(h, macro_from_f(h->d.Q, h->out_f, na, d_rho, d_u, h->st));
+    // the read-out launch computes rho and u itself (no FP64 copy of f)
+    StepParams p = make_params(h, 2);
+    p.out_rho = d_rho;
+    p.out_u = d_u;
+    CK(h, launch(h, 2, p));
+    CK(h, reduce_partials(h->partials, h->nblocks, h->sums, h->st));
     if (rho) CK(h, cudaMemcpyAsync(rho, d_rho, sizeof(double) * na, cudaMemcpyDeviceToHost, h->st));
     if (u3) CK(h, cudaMemcpyAsync(u3, d_u, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
@@ -1182,6 +1188,20 @@ lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3) {
 }  // extern "C"
 
 namespace {
+
+// FP32 stress ring: folded steps are in the accumulators; the last step
+// m = steps - 1 was preceded by a fold at step f = m - m % kFoldEvery (of
+// the kFoldEvery steps before f), so steps f .. m, ring slots f % kRingSlots
+// .. m % kRingSlots, are pending; |tau| of step m is in slot `last`.
+void ring_pending(const lbm_handle* h, int& first, int& pending, int& last) {
+    first = 0; pending = 0; last = -1;
+    if (h->steps > 0) {
+        const int64_t m = h->steps - 1;
+        last = (int)(m % kRingSlots);
+        pending = (int)(m % kFoldEvery) + 1;
+        first = last - pending + 1;
+    }
+}
 
 // Next-to-wall accumulators as doubles: |tau| (n), tau (3n, [3][n]), |tau| sum (n).
 int read_accumulators(lbm_handle* h, std::vector<double>& w, std::vector<double>& a, std::vector<double>& am) {
@@ -1195,17 +1215,8 @@ int read_accumulators(lbm_handle* h, std::vector<double>& w, std::vector<double>
         CK(h, cudaStreamSynchronize(h->st));
         return LBM_OK;
     }
-    // folded steps (accumulators) + the steps since the last fold: the last
-    // step m = steps - 1 was preceded by a fold at step f = m - m % kFoldEvery
-    // (of the kFoldEvery steps before f), so steps f .. m, ring slots
-    // f % kRingSlots .. m % kRingSlots, are pending; |tau| of step m from its slot
-    int first = 0, pending = 0, last = -1;
-    if (h->steps > 0) {
-        const int64_t m = h->steps - 1;
-        last = (int)(m % kRingSlots);
-        pending = (int)(m % kFoldEvery) + 1;
-        first = last - pending + 1;
-    }
+    int first, pending, last;
+    ring_pending(h, first, pending, last);
     if (!h->nw_out) CK(h, dalloc(h, &h->nw_out, sizeof(double) * 5 * n));
     CK(h, nw_readout_f32(h->nw_accf, h->nw_ring, n, first, pending, last, h->wss_from_ckpt ? h->nw_wssf : nullptr,
                          h->nw_out, h->st));
@@ -1252,28 +1263,34 @@ lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss,
                        double* osi, double* tawss) {
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    CK(h, cudaSetDevice(h->d.device));
     const int64_t n = h->g.nnw;
-    std::vector<double> nn(3 * n), w, a, am;
-    int rc = read_accumulators(h, w, a, am);
-    if (rc) return rc;
-    if (n) {
-        CK(h, cudaMemcpyAsync(nn.data(), h->nw_n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
-        if (pt) CK(h, cudaMemcpyAsync(pt, h->g.nw_pt, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, h->st));
+    if (n == 0) return LBM_OK;
+    // accumulators as doubles on the device, then the outputs assembled there
+    // and copied straight into the caller's buffers
+    const double *w, *a, *am;
+    if (h->d.precision == LBM_F64) {
+        w = h->nw_wss; a = h->nw_acc; am = h->nw_accm;
+    } else {
+        int first, pending, last;
+        ring_pending(h, first, pending, last);
+        if (!h->nw_out) CK(h, dalloc(h, &h->nw_out, sizeof(double) * 5 * n));
+        CK(h, nw_readout_f32(h->nw_accf, h->nw_ring, n, first, pending, last,
+                             h->wss_from_ckpt ? h->nw_wssf : nullptr, h->nw_out, h->st));
+        w = h->nw_out; a = h->nw_out + n; am = h->nw_out + 4 * n;
     }
+    if (!h->nw_fields) CK(h, dalloc(h, &h->nw_fields, sizeof(double) * 10 * n));
+    double* o = h->nw_fields;
+    CK(h, wss_outputs(w, a, am, h->nw_n, n, h->d.tawss_div, o, h->st));
+    const size_t b1 = sizeof(double) * n, b3 = 3 * b1;
+    if (pt) CK(h, cudaMemcpyAsync(pt, h->g.nw_pt, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, h->st));
+    if (wss) CK(h, cudaMemcpyAsync(wss, o, b1, cudaMemcpyDeviceToHost, h->st));
+    if (normal3) CK(h, cudaMemcpyAsync(normal3, o + n, b3, cudaMemcpyDeviceToHost, h->st));
+    if (acc3) CK(h, cudaMemcpyAsync(acc3, o + 4 * n, b3, cudaMemcpyDeviceToHost, h->st));
+    if (acc_mag) CK(h, cudaMemcpyAsync(acc_mag, o + 7 * n, b1, cudaMemcpyDeviceToHost, h->st));
+    if (osi) CK(h, cudaMemcpyAsync(osi, o + 8 * n, b1, cudaMemcpyDeviceToHost, h->st));
+    if (tawss) CK(h, cudaMemcpyAsync(tawss, o + 9 * n, b1, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
-    for (int64_t p = 0; p < n; ++p) {
-        const double a0 = a[p], a1 = a[n + p], a2 = a[2 * n + p];
-        if (normal3) { normal3[3 * p] = nn[p]; normal3[3 * p + 1] = nn[n + p]; normal3[3 * p + 2] = nn[2 * n + p]; }
-        if (wss) wss[p] = w[p];
-        if (acc3) { acc3[3 * p] = a0; acc3[3 * p + 1] = a1; acc3[3 * p + 2] = a2; }
-        if (acc_mag) acc_mag[p] = am[p];
-        // ComputeOSIAndTAWSS (Simulation.cpp:899-905)
-        if (tawss) tawss[p] = am[p] / h->d.tawss_div;
-        if (osi) {
-            double norm = std::sqrt(std::pow(a0, 2) + std::pow(a1, 2) + std::pow(a2, 2));
-            osi[p] = 0.5 * (1.0 - (norm / am[p]));
-        }
-    }
     return LBM_OK;
 }
 

@@ -113,6 +113,8 @@ struct StepParams {
     unsigned* flags;
     // readout (materialize) outputs
     double* out_f;            // [a*Q + q] FP64, or null
+    double* out_rho;          // rho per node (FP64 moments of the full f), or null
+    double* out_u;            // u per node, 3 per node, or null
     const int32_t* act_idx;   // per point active index (readout only)
     double* partials;         // per block: mass - nact, mom3
 };
@@ -138,10 +140,11 @@ cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, const doubl
 cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact,
                             cudaStream_t s);
 
-// Read-out helpers (step_f64.cu): ordered FP64 sum of per-block partials,
-// and rho/u from read-out distributions.
+// Read-out helpers (step_f64.cu): ordered FP64 sum of per-block partials;
+// next-to-wall outputs [wss | normal n x 3 | acc n x 3 | acc_mag | osi | tawss].
+cudaError_t wss_outputs(const double* w, const double* a, const double* am, const double* nrm, int64_t n,
+                        double tawss_div, double* out, cudaStream_t st);
 cudaError_t reduce_partials(const double* partials, int64_t nblocks, double* out, cudaStream_t s);
-cudaError_t macro_from_f(int Q, const double* f, int64_t nact, double* rho, double* u3, cudaStream_t s);
 // Warm start: f = f_eq(rho, u) (+ regularised non-equilibrium part from
 // finite-difference velocity gradients), FP64 per active node.
 cudaError_t warm_start_f(int Q, const float* rho, const float* u, const int32_t* act_idx, const int64_t* act_pt,

@@ -46,19 +46,6 @@ __global__ void k_reduce_partials(const double* __restrict__ part, int64_t nbloc
     if (threadIdx.x < kPartialStride) out[threadIdx.x] = red[0][threadIdx.x];
 }
 
-template <int Q>
-__global__ void k_macro(const double* __restrict__ f, int64_t nact, double* __restrict__ rho, double* __restrict__ u) {
-    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= nact) return;
-    double g[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) g[q] = f[a * Q + q];
-    double r, ux, uy, uz;
-    moments<Q, double, false>(g, r, ux, uy, uz);
-    if (rho) rho[a] = r;
-    if (u) { u[3 * a] = ux; u[3 * a + 1] = uy; u[3 * a + 2] = uz; }
-}
-
 // f = f_eq(rho, u) + f_neq, f_neq_i = -3 tau w_i rho sum_ab (c_ia c_ib - d_ab/3) S_ab,
 // S = (grad u + grad u^T)/2 from central differences (one-sided next to solid).
 template <int Q>
@@ -112,11 +99,31 @@ cudaError_t reduce_partials(const double* partials, int64_t nblocks, double* out
     return cudaGetLastError();
 }
 
-cudaError_t macro_from_f(int Q, const double* f, int64_t nact, double* rho, double* u3, cudaStream_t st) {
-    if (nact <= 0) return cudaSuccess;
-    const unsigned g = (unsigned)ceil_div(nact, 256);
-    if (Q == 19) k_macro<19><<<g, 256, 0, st>>>(f, nact, rho, u3);
-    else k_macro<27><<<g, 256, 0, st>>>(f, nact, rho, u3);
+// Next-to-wall outputs from the accumulators (w = |tau| of the last step,
+// a = accumulated traction [3][n], am = accumulated |tau|): out holds
+// wss[n], normal[n][3], acc[n][3], acc_mag[n], osi[n], tawss[n]
+// (ComputeOSIAndTAWSS, Simulation.cpp:899-905, with pow(x, 2) as x * x).
+__global__ void k_wss_out(const double* __restrict__ w, const double* __restrict__ a,
+                          const double* __restrict__ am, const double* __restrict__ nrm, int64_t n, double tawss_div,
+                          double* __restrict__ out) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const double a0 = a[p], a1 = a[n + p], a2 = a[2 * n + p], m = am[p];
+    out[p] = w[p];
+    double* nr = out + n;
+    nr[3 * p] = nrm[p]; nr[3 * p + 1] = nrm[n + p]; nr[3 * p + 2] = nrm[2 * n + p];
+    double* ac = out + 4 * n;
+    ac[3 * p] = a0; ac[3 * p + 1] = a1; ac[3 * p + 2] = a2;
+    out[7 * n + p] = m;
+    const double norm = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+    out[8 * n + p] = 0.5 * (1.0 - (norm / m));
+    out[9 * n + p] = m / tawss_div;
+}
+
+cudaError_t wss_outputs(const double* w, const double* a, const double* am, const double* nrm, int64_t n,
+                        double tawss_div, double* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_wss_out<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(w, a, am, nrm, n, tawss_div, out);
     return cudaGetLastError();
 }
 

@@ -695,13 +695,26 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
         const double rho = OFF ? 1.0 + (double)r : (double)r;
         part[0] = OFF ? (double)r : rho - 1.0;
         part[1] = rho * ux; part[2] = rho * uy; part[3] = rho * uz;
-        if (P.out_f) {
+        if (P.out_f || P.out_rho) {
+            double fd[Q];  // the full f in FP64
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 if constexpr (SC)
-                    P.out_f[a * Q + q] = Lat<Q>::w(q) + (double)Store<S>::template unit<Q>(q) * (double)g[q];
+                    fd[q] = Lat<Q>::w(q) + (double)Store<S>::template unit<Q>(q) * (double)g[q];
                 else
-                    P.out_f[a * Q + q] = full_value<Q, R, OFF>(g[q], q);
+                    fd[q] = full_value<Q, R, OFF>(g[q], q);
+            }
+            if (P.out_f) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q) P.out_f[a * Q + q] = fd[q];
+            }
+            if (P.out_rho) {
+                // the FP64 moments of the full f (Collision's formulas), as
+                // the FP64 distributions of lbm_get_distributions would give them
+                double rr, vx, vy, vz;
+                moments<Q, double, false>(fd, rr, vx, vy, vz);
+                P.out_rho[a] = rr;
+                P.out_u[3 * a] = vx; P.out_u[3 * a + 1] = vy; P.out_u[3 * a + 2] = vz;
             }
         }
     } else {
