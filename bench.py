@@ -609,7 +609,9 @@ def run_ours(args):
     # end to end through the C ABI: per e2e step, H2D of a 100-step inlet
     # table slice from pinned memory, 100 LBM steps (graph replay), D2H of
     # the wall shear stress arrays and the rho/u field (the reference's
-    # output cadence, Simulation.cpp:589-591)
+    # output cadence, Simulation.cpp:589-591).  The read-outs are the
+    # asynchronous calls: their copies run on the handle's copy stream while
+    # the next batch steps; the timed region ends when the last copies land.
     from pv_dec_original_gb300 import waveform
     B = 100
     table = waveform.sinusoid_table(U_MEAN, PERIOD, 4000)
@@ -622,21 +624,28 @@ def run_ours(args):
     s.set_graph_steps(B)
     L = capi.load()
     P = lambda a: a.ctypes.data_as(C.c_void_p)
-    e2e_times = []
     nb = max(2, min(5, args.steps // 10))
-    for it in range(nb + 1):
-        s0 = s.counts()["steps"]
-        t0 = time.perf_counter()
+
+    def e2e_batch(k):
+        s0 = k * B + s_base
         idx = np.arange(s0, s0 + B)
         amp_h[idx % B] = table[idx % len(table)]  # step s reads amp[s % B]
         capi._check(L.lbm_set_inlet_table(s.h, amp_h, B), s.h)
         capi._check(L.lbm_step_async(s.h, B), s.h)
-        capi._check(L.lbm_get_wss(s.h, P(pt_h), P(wss_h[1]), P(wss_h[0]), P(wss_h[3]), P(wss_h[2]), P(wss_h[4]),
-                                  P(wss_h[5])), s.h)
-        capi._check(L.lbm_get_macro(s.h, P(rho_h), P(u_h)), s.h)
-        capi._check(L.lbm_check_status(s.h), s.h)
-        if it > 0:  # first batch captures the graph
-            e2e_times.append(time.perf_counter() - t0)
+        capi._check(L.lbm_get_wss_async(s.h, P(pt_h), P(wss_h[1]), P(wss_h[0]), P(wss_h[3]), P(wss_h[2]),
+                                        P(wss_h[4]), P(wss_h[5])), s.h)
+        capi._check(L.lbm_get_macro_async(s.h, P(rho_h), P(u_h)), s.h)
+
+    s_base = s.counts()["steps"]
+    e2e_batch(0)  # captures the graph, allocates the staging buffers
+    capi._check(L.lbm_wait_outputs(s.h), s.h)
+    capi._check(L.lbm_check_status(s.h), s.h)
+    t0 = time.perf_counter()
+    for k in range(1, nb + 1):
+        e2e_batch(k)
+    capi._check(L.lbm_wait_outputs(s.h), s.h)
+    e2e_times = [(time.perf_counter() - t0) / nb]
+    capi._check(L.lbm_check_status(s.h), s.h)
     e2e_t = max_over_ranks(dist, sum(e2e_times) / len(e2e_times), dev_t)
     h2d = B * 8
     d2h = nnw * 8 * (1 + 3 + 1 + 3 + 1 + 1 + 1) + active * 8 * 4
@@ -674,7 +683,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": {"value": aggregate_mlups(ws, active, B, e2e_t), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "step": f"{B} LBM steps per call batch + WSS/OSI/TAWSS and rho/u read-back (pinned host buffers)"},
+                    "step": f"{B} LBM steps per call batch + WSS/OSI/TAWSS and rho/u read-back (pinned host buffers; "
+                            "the read-back copies of one batch overlap the next batch's steps)"},
             "gpu_launches": launches,
             "autotune": {"variant": tuned[0], "ms_per_step_by_variant": tuned[1],
                          "variants": "(block, min blocks/SM): (128,12) (128,10) (128,8) (256,3) (256,1); 5: tiled bulk-copy kernel"},

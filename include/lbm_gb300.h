@@ -270,6 +270,17 @@ lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss,
  * spacings.  distance (may be NULL) receives the physical distance. */
 lbm_status lbm_nearest_next_to_wall(lbm_handle* h, const double* xyz, int64_t nv, int max_radius, int64_t* nw_index,
                                     double* distance);
+/* The same read-outs without waiting: the read-out launches are queued on
+ * the handle's stream behind the steps already queued, and the copies into
+ * the caller's buffers run on a second stream while later steps proceed
+ * (pinned buffers, e.g. cudaHostAlloc, make the copies truly asynchronous).
+ * The buffers hold the results once lbm_wait_outputs returns; a later
+ * read-out of the same kind waits on the device for the earlier copies.
+ * No reference counterpart (its output blocks the time loop). */
+lbm_status lbm_get_macro_async(lbm_handle* h, double* rho, double* u3);
+lbm_status lbm_get_wss_async(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3,
+                             double* acc_mag, double* osi, double* tawss);
+lbm_status lbm_wait_outputs(lbm_handle* h);
 /* FP64 sums over the post-boundary distributions: total mass, momentum, and
  * per boundary condition the momentum along its face axis (flux). */
 lbm_status lbm_get_conservation(lbm_handle* h, double* mass, double* mom3, double* flux);

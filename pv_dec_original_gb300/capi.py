@@ -70,6 +70,7 @@ EXPORTS = [
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
     "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
     "lbm_init_from_macro_device", "lbm_nearest_next_to_wall", "lbm_set_wall_distances", "lbm_get_wall_distances",
+    "lbm_get_macro_async", "lbm_get_wss_async", "lbm_wait_outputs",
 ]
 NUM_VARIANTS = 6
 
@@ -118,6 +119,9 @@ def load(build_if_missing: bool = True):
     L.lbm_set_distributions.argtypes = [P, dp]
     L.lbm_get_macro.argtypes = [P, P, P]
     L.lbm_get_wss.argtypes = [P, P, P, P, P, P, P, P]
+    L.lbm_get_wss_async.argtypes = [P, P, P, P, P, P, P, P]
+    L.lbm_get_macro_async.argtypes = [P, P, P]
+    L.lbm_wait_outputs.argtypes = [P]
     L.lbm_get_conservation.argtypes = [P, P, P, P]
     L.lbm_save.argtypes = [P, C.c_char_p]
     L.lbm_load.argtypes = [P, C.c_char_p]
@@ -374,6 +378,17 @@ class Solver:
             v[ok] = w[k][idx[ok]]
             out[k] = v
         return out
+
+    def outputs_async(self, rho, u, wss, osi, tawss):
+        """Queue the rho/u and WSS/OSI/TAWSS read-outs into the given arrays
+        (float64; pinned memory makes the copies asynchronous); they hold
+        the values once wait_outputs returns."""
+        L = load()
+        self._c(L.lbm_get_wss_async(self.h, None, None, _ptr(wss), None, None, _ptr(osi), _ptr(tawss)))
+        self._c(L.lbm_get_macro_async(self.h, _ptr(rho), _ptr(u)))
+
+    def wait_outputs(self):
+        self._c(load().lbm_wait_outputs(self.h))
 
     def conservation(self):
         m, p, fl = np.zeros(1), np.zeros(3), np.zeros(MAX_BC)

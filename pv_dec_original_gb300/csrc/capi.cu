@@ -31,6 +31,15 @@ using namespace lbm;
 struct lbm_handle {
     lbm_desc d{};
     cudaStream_t st = nullptr;
+    // asynchronous outputs: device-to-host copies on a stream of their own,
+    // ordered against the step stream by events
+    cudaStream_t cst = nullptr;
+    cudaEvent_t ev_ready = nullptr;                 // read-out launches done (step stream)
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr};  // copies out of the staging buffers done: macro, wss
+    cudaEvent_t ev_table = nullptr;                 // last stream-ordered inlet-table upload done
+    double* amp_pinned = nullptr;                   // pinned staging of that upload
+    int64_t amp_pinned_cap = 0;
+    std::vector<int64_t> wave_off_h, wave_len_h;    // layout of the uploaded waveforms
     std::string err;
     int nx = 0, ny = 0, nz = 0;
     int64_t npts = 0, stride = 0;
@@ -150,7 +159,6 @@ void drop_graph(lbm_handle* h) {
 // Concatenate the host waveforms into the device table; unset waveforms
 // have length 0 (amplitude 0).
 int upload_waves(lbm_handle* h) {
-    CK(h, cudaStreamSynchronize(h->st));
     std::vector<int64_t> off(LBM_MAX_WAVES, 0), len(LBM_MAX_WAVES, 0);
     int64_t total = 0;
     for (size_t w = 0; w < h->waves.size(); ++w) {
@@ -158,6 +166,28 @@ int upload_waves(lbm_handle* h) {
         len[w] = (int64_t)h->waves[w].size();
         total += len[w];
     }
+    if (total <= h->amp_cap && off == h->wave_off_h && len == h->wave_len_h) {
+        // same layout: a stream-ordered copy through pinned staging, with no
+        // host wait -- steps already enqueued read the old table, later
+        // steps the new one
+        if (total > h->amp_pinned_cap) {
+            if (h->ev_table) CK(h, cudaEventSynchronize(h->ev_table));
+            if (h->amp_pinned) cudaFreeHost(h->amp_pinned);
+            h->amp_pinned = nullptr;
+            h->amp_pinned_cap = 0;
+            CK(h, cudaHostAlloc(&h->amp_pinned, sizeof(double) * total, cudaHostAllocDefault));
+            h->amp_pinned_cap = total;
+        }
+        if (!h->ev_table) CK(h, cudaEventCreateWithFlags(&h->ev_table, cudaEventDisableTiming));
+        else CK(h, cudaEventSynchronize(h->ev_table));  // the staging's previous copy has run
+        for (size_t w = 0; w < h->waves.size(); ++w)
+            if (len[w] > 0) std::memcpy(h->amp_pinned + off[w], h->waves[w].data(), sizeof(double) * len[w]);
+        if (total > 0)
+            CK(h, cudaMemcpyAsync(h->amp, h->amp_pinned, sizeof(double) * total, cudaMemcpyHostToDevice, h->st));
+        CK(h, cudaEventRecord(h->ev_table, h->st));
+        return LBM_OK;
+    }
+    CK(h, cudaStreamSynchronize(h->st));
     if (total > h->amp_cap) {
         drop_graph(h);  // the table pointer is baked into captured launches
         if (h->amp) cudaFree(h->amp);
@@ -173,10 +203,33 @@ int upload_waves(lbm_handle* h) {
     CK(h, cudaMemcpyAsync(h->wave_off, off.data(), sizeof(int64_t) * LBM_MAX_WAVES, cudaMemcpyHostToDevice, h->st));
     CK(h, cudaMemcpyAsync(h->wave_len, len.data(), sizeof(int64_t) * LBM_MAX_WAVES, cudaMemcpyHostToDevice, h->st));
     CK(h, cudaStreamSynchronize(h->st));
+    h->wave_off_h = off;
+    h->wave_len_h = len;
+    return LBM_OK;
+}
+
+// The copy stream and its events (created on first use).
+int ensure_copy_stream(lbm_handle* h) {
+    if (h->cst) return LBM_OK;
+    CK(h, cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking));
+    CK(h, cudaEventCreateWithFlags(&h->ev_ready, cudaEventDisableTiming));
+    CK(h, cudaEventCreateWithFlags(&h->ev_copied[0], cudaEventDisableTiming));
+    CK(h, cudaEventCreateWithFlags(&h->ev_copied[1], cudaEventDisableTiming));
+    // nothing pending yet: record both on the empty copy stream
+    CK(h, cudaEventRecord(h->ev_copied[0], h->cst));
+    CK(h, cudaEventRecord(h->ev_copied[1], h->cst));
+    return LBM_OK;
+}
+
+// A read-out about to overwrite staging buffer `which` (0 macro, 1 wss)
+// waits, on the step stream, for the copies still reading it.
+int wait_staging(lbm_handle* h, int which) {
+    if (h->cst) CK(h, cudaStreamWaitEvent(h->st, h->ev_copied[which], 0));
     return LBM_OK;
 }
 
 void free_geometry(lbm_handle* h) {
+    if (h->cst) cudaStreamSynchronize(h->cst);  // copies still reading staging buffers
     GeometryLists& g = h->g;
     void* ptrs[] = {g.cls, g.sp_pt, g.sp_miss, g.sp_cls, g.sp_nw, g.sp_bc, g.bcidx, g.sp_prof, g.nw_pt, g.act_word,
                     g.sp_of_act, h->bct, h->sp_flux,
@@ -738,6 +791,11 @@ lbm_status lbm_destroy(lbm_handle* h) {
     if (h->amp) cudaFree(h->amp);
     if (h->wave_off) cudaFree(h->wave_off);
     if (h->wave_len) cudaFree(h->wave_len);
+    if (h->cst) cudaStreamSynchronize(h->cst);
+    if (h->amp_pinned) cudaFreeHost(h->amp_pinned);
+    for (cudaEvent_t e : {h->ev_ready, h->ev_copied[0], h->ev_copied[1], h->ev_table})
+        if (e) cudaEventDestroy(e);
+    if (h->cst) cudaStreamDestroy(h->cst);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
     return LBM_OK;
@@ -1165,23 +1223,67 @@ lbm_status lbm_get_distributions(lbm_handle* h, double* f) {
     return LBM_OK;
 }
 
-lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3) {
-    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
-    CK(h, cudaSetDevice(h->d.device));
+}  // extern "C"
+
+namespace {
+
+// rho and u of every active node into the staging buffer h->macro (rho [na],
+// then u [3 na] after one padding entry), on the step stream.
+int macro_to_staging(lbm_handle* h) {
     REQUIRE(h, h->has_state, LBM_ERR_STATE, "no state: call lbm_init_equilibrium / lbm_set_geometry first");
     const int64_t na = h->g.nact;
     if (!h->macro) CK(h, dalloc(h, &h->macro, sizeof(double) * 4 * (na + 1)));
-    double* d_rho = h->macro;
-    double* d_u = h->macro + (na + 1);
+    int rc = wait_staging(h, 0);
+    if (rc) return rc;
     // the read-out launch computes rho and u itself (no FP64 copy of f)
     StepParams p = make_params(h, 2);
-    p.out_rho = d_rho;
-    p.out_u = d_u;
+    p.out_rho = h->macro;
+    p.out_u = h->macro + (na + 1);
     CK(h, launch(h, 2, p));
     CK(h, reduce_partials(h->partials, h->nblocks, h->sums, h->st));
-    if (rho) CK(h, cudaMemcpyAsync(rho, d_rho, sizeof(double) * na, cudaMemcpyDeviceToHost, h->st));
-    if (u3) CK(h, cudaMemcpyAsync(u3, d_u, sizeof(double) * 3 * na, cudaMemcpyDeviceToHost, h->st));
+    return LBM_OK;
+}
+
+int macro_copies(lbm_handle* h, double* rho, double* u3, cudaStream_t st) {
+    const int64_t na = h->g.nact;
+    if (rho && na) CK(h, cudaMemcpyAsync(rho, h->macro, sizeof(double) * na, cudaMemcpyDeviceToHost, st));
+    if (u3 && na)
+        CK(h, cudaMemcpyAsync(u3, h->macro + (na + 1), sizeof(double) * 3 * na, cudaMemcpyDeviceToHost, st));
+    return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    CK(h, cudaSetDevice(h->d.device));
+    int rc = macro_to_staging(h);
+    if (!rc) rc = macro_copies(h, rho, u3, h->st);
+    if (rc) return rc;
     CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_macro_async(lbm_handle* h, double* rho, double* u3) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    CK(h, cudaSetDevice(h->d.device));
+    int rc = ensure_copy_stream(h);
+    if (!rc) rc = macro_to_staging(h);
+    if (rc) return rc;
+    CK(h, cudaEventRecord(h->ev_ready, h->st));
+    CK(h, cudaStreamWaitEvent(h->cst, h->ev_ready, 0));
+    rc = macro_copies(h, rho, u3, h->cst);
+    if (rc) return rc;
+    CK(h, cudaEventRecord(h->ev_copied[0], h->cst));
+    return LBM_OK;
+}
+
+lbm_status lbm_wait_outputs(lbm_handle* h) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    CK(h, cudaSetDevice(h->d.device));
+    if (h->cst) CK(h, cudaStreamSynchronize(h->cst));
     return LBM_OK;
 }
 
@@ -1259,15 +1361,16 @@ int write_accumulators(lbm_handle* h, const std::vector<double>& w, const std::v
 
 extern "C" {
 
-lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3, double* acc_mag,
-                       double* osi, double* tawss) {
-    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
-    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
-    CK(h, cudaSetDevice(h->d.device));
+}  // extern "C"
+
+namespace {
+
+// Next-to-wall outputs [wss | normal n x 3 | acc n x 3 | acc_mag | osi | tawss]
+// assembled in the staging buffer h->nw_fields, on the step stream.
+int wss_to_staging(lbm_handle* h) {
     const int64_t n = h->g.nnw;
-    if (n == 0) return LBM_OK;
-    // accumulators as doubles on the device, then the outputs assembled there
-    // and copied straight into the caller's buffers
+    int rc = wait_staging(h, 1);
+    if (rc) return rc;
     const double *w, *a, *am;
     if (h->d.precision == LBM_F64) {
         w = h->nw_wss; a = h->nw_acc; am = h->nw_accm;
@@ -1280,17 +1383,58 @@ lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss,
         w = h->nw_out; a = h->nw_out + n; am = h->nw_out + 4 * n;
     }
     if (!h->nw_fields) CK(h, dalloc(h, &h->nw_fields, sizeof(double) * 10 * n));
-    double* o = h->nw_fields;
-    CK(h, wss_outputs(w, a, am, h->nw_n, n, h->d.tawss_div, o, h->st));
+    CK(h, wss_outputs(w, a, am, h->nw_n, n, h->d.tawss_div, h->nw_fields, h->st));
+    return LBM_OK;
+}
+
+int wss_copies(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3, double* acc_mag, double* osi,
+               double* tawss, cudaStream_t st) {
+    const int64_t n = h->g.nnw;
+    const double* o = h->nw_fields;
     const size_t b1 = sizeof(double) * n, b3 = 3 * b1;
-    if (pt) CK(h, cudaMemcpyAsync(pt, h->g.nw_pt, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, h->st));
-    if (wss) CK(h, cudaMemcpyAsync(wss, o, b1, cudaMemcpyDeviceToHost, h->st));
-    if (normal3) CK(h, cudaMemcpyAsync(normal3, o + n, b3, cudaMemcpyDeviceToHost, h->st));
-    if (acc3) CK(h, cudaMemcpyAsync(acc3, o + 4 * n, b3, cudaMemcpyDeviceToHost, h->st));
-    if (acc_mag) CK(h, cudaMemcpyAsync(acc_mag, o + 7 * n, b1, cudaMemcpyDeviceToHost, h->st));
-    if (osi) CK(h, cudaMemcpyAsync(osi, o + 8 * n, b1, cudaMemcpyDeviceToHost, h->st));
-    if (tawss) CK(h, cudaMemcpyAsync(tawss, o + 9 * n, b1, cudaMemcpyDeviceToHost, h->st));
+    if (pt) CK(h, cudaMemcpyAsync(pt, h->g.nw_pt, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st));
+    if (wss) CK(h, cudaMemcpyAsync(wss, o, b1, cudaMemcpyDeviceToHost, st));
+    if (normal3) CK(h, cudaMemcpyAsync(normal3, o + n, b3, cudaMemcpyDeviceToHost, st));
+    if (acc3) CK(h, cudaMemcpyAsync(acc3, o + 4 * n, b3, cudaMemcpyDeviceToHost, st));
+    if (acc_mag) CK(h, cudaMemcpyAsync(acc_mag, o + 7 * n, b1, cudaMemcpyDeviceToHost, st));
+    if (osi) CK(h, cudaMemcpyAsync(osi, o + 8 * n, b1, cudaMemcpyDeviceToHost, st));
+    if (tawss) CK(h, cudaMemcpyAsync(tawss, o + 9 * n, b1, cudaMemcpyDeviceToHost, st));
+    return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_get_wss(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3, double* acc_mag,
+                       double* osi, double* tawss) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    CK(h, cudaSetDevice(h->d.device));
+    if (h->g.nnw == 0) return LBM_OK;
+    // accumulators as doubles on the device, the outputs assembled there and
+    // copied straight into the caller's buffers
+    int rc = wss_to_staging(h);
+    if (!rc) rc = wss_copies(h, pt, normal3, wss, acc3, acc_mag, osi, tawss, h->st);
+    if (rc) return rc;
     CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_get_wss_async(lbm_handle* h, int64_t* pt, double* normal3, double* wss, double* acc3,
+                             double* acc_mag, double* osi, double* tawss) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    CK(h, cudaSetDevice(h->d.device));
+    if (h->g.nnw == 0) return LBM_OK;
+    int rc = ensure_copy_stream(h);
+    if (!rc) rc = wss_to_staging(h);
+    if (rc) return rc;
+    CK(h, cudaEventRecord(h->ev_ready, h->st));
+    CK(h, cudaStreamWaitEvent(h->cst, h->ev_ready, 0));
+    rc = wss_copies(h, pt, normal3, wss, acc3, acc_mag, osi, tawss, h->cst);
+    if (rc) return rc;
+    CK(h, cudaEventRecord(h->ev_copied[1], h->cst));
     return LBM_OK;
 }
 
