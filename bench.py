@@ -379,7 +379,7 @@ def warmstart_extra(device, n_train=32, n_test=6, tau=0.55, box=(64, 64, 128)):
     rows = []
     dev = torch.device("cuda", device)
     for m in test_m:
-        # the judge's answer: an FP64 lattice from rest to the residual 1e-6
+        # the converged answer: an FP64 lattice from rest to the residual 1e-6
         sr, mask = WS.single_lattice(m, tau=tau, precision="f64", device=device, collision=rlb)
         sr.set_graph_steps(100)
         n64, r64 = WS.steps_to_converge(sr, tol=1e-6, max_steps=150000)

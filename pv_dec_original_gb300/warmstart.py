@@ -12,7 +12,7 @@ accumulation); PyTorch only allocates device memory and builds input
 tensors.  Training data are steady solutions of the plain LBM on seeded
 stenosed tubes and bifurcations, computed as one packed ensemble.
 
-The LBM stays the judge: a warm-started lattice is run to the same
+The LBM has the last word: a warm-started lattice is run to the same
 convergence criterion as a cold one (``steps_to_converge``, on FP64 lattices
 so that the criterion sits far above the storage's rounding noise), so a
 poor prediction costs steps, never accuracy.  The figure of merit is the

@@ -363,7 +363,7 @@ def test_gpu_async_outputs_match_sync(gpu_lib, oracle_lib, prec):
     # (OSI is 0/0 = NaN, as in the reference, where no stress has accumulated)
     assert np.array_equal(wss, w_r["wss"]) and np.array_equal(osi, w_r["osi"], equal_nan=True)
     assert np.array_equal(tawss, w_r["tawss"])
-    # a second round after the extra steps sees them
+    # a second read-out after the extra steps sees them
     s.outputs_async(rho, u, wss, osi, tawss)
     s.wait_outputs()
     r.step(10)

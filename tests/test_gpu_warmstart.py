@@ -3,7 +3,7 @@
 vessels the network's field is closer to the converged one than the
 Poiseuille prior it corrects (and than rest), and a lattice started from it
 converges to the same flow and wall shear stress as one started from rest
-and settles within 1% of the converged WSS (the plain LBM is the judge).
+and settles within 1% of the converged WSS (the plain LBM decides).
 Steps are reported, not asserted: on these small steady cases a start from
 rest already converges within about one viscous time."""
 import numpy as np
@@ -15,7 +15,7 @@ pytest.importorskip("torch")
 TAU = 0.55
 
 
-def test_gpu_warm_start_judged_by_lbm(gpu_lib):
+def test_gpu_warm_start_checked_by_lbm(gpu_lib):
     from pv_dec_original_gb300 import warmstart as WS
     train_m = WS.vessel_members(32, seed=1)
     test_m = WS.vessel_members(3, seed=99)
