@@ -171,9 +171,9 @@ def c2_bcs(capi, surf, mask):
             capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)], (kin, kout)
 
 
-def make_solver(capi, mask, surf, tri, Q, prec, origin, device):
+def make_solver(capi, mask, surf, tri, Q, prec, origin, device, collision=0):
     from pv_dec_original_gb300 import waveform
-    s = capi.Solver(Q, prec, capi.LBM_PHYSICS, TAU, 1.0, origin, 1.0, PERIOD, device)
+    s = capi.Solver(Q, prec, capi.LBM_PHYSICS, TAU, 1.0, origin, 1.0, PERIOD, device, collision=collision)
     bcs, planes = c2_bcs(capi, surf, mask)
     s.set_geometry(mask, bcs)
     s.set_normals(tri)
@@ -282,6 +282,37 @@ def precision_extra(capi, cr, device, steps=1200, timed=200):
         res[prec]["speedup_vs_f32"] = res[prec]["mlups"] / res["f32"]["mlups"]
     return {"lattice": [384, 288, 768], "active_nodes": int(len(fl)), "steps": steps, "tau": TAU,
             "reference": "FP64 run of the same case on the GPU (physics mode)", "formats": res}
+
+
+def periods_extra(capi, mask, surf, tri, origin, device, periods=3):
+    """C2 over three inlet periods (12,000 steps): FP32, FP16 and BF16
+    storage against an FP64 run of the same case on the GPU, regularized
+    collision (BGK diverges near step 2200 at tau = 0.55 on this lattice):
+    velocity and pressure-drop errors at the end, and the TAWSS (time
+    average over the three periods) error."""
+    fl = np.argwhere(mask > 0)
+    steps = int(periods * PERIOD)
+    res, ref = {}, None
+    for prec in ("f64", "f32", "f16", "bf16"):
+        t0 = time.perf_counter()
+        s, (kin, kout) = make_solver(capi, mask, surf, tri, 19, prec, origin, device,
+                                     collision=capi.LBM_COLLISION_REGULARIZED)
+        s.set_graph_steps(100)
+        s.step(steps)
+        rho, u = s.macro()
+        tawss = s.wss()["tawss"]
+        drop = (rho[fl[:, 0] == kin].mean() - rho[fl[:, 0] == kout].mean()) / 3.0
+        row = {"seconds": time.perf_counter() - t0}
+        if ref is None:
+            ref = (u, drop, tawss)
+        else:
+            row["u_l2_rel"] = float(np.linalg.norm(u - ref[0]) / np.linalg.norm(ref[0]))
+            row["pressure_drop_rel"] = float(abs(drop - ref[1]) / abs(ref[1]))
+            row["tawss_l2_rel"] = float(np.linalg.norm(tawss - ref[2]) / np.linalg.norm(ref[2]))
+        res[prec] = row
+        s.close()
+    return {"lattice": [256, 192, 512], "steps": steps, "periods": periods, "tau": TAU,
+            "collision": "regularized", "reference": "FP64 run of the same case on the GPU", "formats": res}
 
 
 def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
@@ -601,6 +632,7 @@ def run_ours(args):
         extra["d3q27"] = d3q27_extra(capi, cr, mask, surf, tri, origin, local, flush, args.steps)
     if extras and not args.no_precision:
         extra["precision_c3"] = precision_extra(capi, cr, local)
+        extra["c2_three_periods"] = periods_extra(capi, mask, surf, tri, origin, local)
     if extras and not args.no_ensemble:
         extra["ensemble_c4"] = ensemble_extra(capi, cr, local, args.Q)
     if extras and not args.no_warmstart:
