@@ -9,6 +9,7 @@
 //   precision 0..3 (f64, f32, f16, bf16)  mode 0|1 (parity, physics)
 //   pv_preset 1        (the reference's PV.stl inlet / outlet coordinates)
 //   write_output 0|1   write_vertices 0|1 (WSS / OSI / TAWSS at the STL's vertices)
+//   interpolated_walls 1 (physics mode: Bouzidi bounce-back from the STL's wall distances)
 //   inlet_face <f> inlet_plane <p>  outlet_face <f> outlet_plane <p>
 // Defaults reproduce the reference: FP64, parity semantics, D3Q19.
 #include <chrono>
@@ -66,6 +67,7 @@ int main(int argc, char** argv) {
         sim.output_root = sv.count("output_dir") ? sv["output_dir"] : ".";
         sim.write_output = num("write_output", 1) != 0;
         sim.write_vertices = num("write_vertices", 0) != 0;
+        if (num("interpolated_walls", 0) != 0) sim.UseInterpolatedWalls(true);
         lbm_counts c{};
         if (lbm_get_counts(sim.handle(), &c) != LBM_OK) throw std::runtime_error("lbm_get_counts failed");
         const auto t2 = clk::now();

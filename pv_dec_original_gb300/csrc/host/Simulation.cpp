@@ -58,6 +58,14 @@ lbm_handle* Simulation::handle() {
     return h_;
 }
 
+void Simulation::UseInterpolatedWalls(bool on) {
+    ensure();
+    const Geometry& g = SubDomain_.Geometry_;
+    std::vector<double> rows = triangles_to_rows(g.globalTriangles);
+    check(lbm_set_wall_distances(h_, on ? rows.data() : nullptr, on ? (int64_t)g.globalTriangles.size() : 0),
+          "lbm_set_wall_distances");
+}
+
 int64_t Simulation::steps() {
     lbm_counts c{};
     check(lbm_get_counts(handle(), &c), "lbm_get_counts");

@@ -74,6 +74,9 @@ public:
     void WallShearStress(std::vector<int64_t>& pt, std::vector<double>& wss, std::vector<double>& osi,
                          std::vector<double>& tawss);
     std::vector<uint8_t> Classes();
+    // Interpolated (Bouzidi) bounce-back with wall distances from the
+    // geometry's triangles (physics mode; off: half-way bounce-back).
+    void UseInterpolatedWalls(bool on = true);
 
 private:
     lbm_handle* h_ = nullptr;

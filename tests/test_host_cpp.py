@@ -98,3 +98,36 @@ def test_lbm_run_end_to_end_vs_oracle(tmp_path, gpu_lib, oracle_lib):
     near = np.argmin(((ijk[None] - g[:, None]) ** 2).sum(-1), 1)
     np.testing.assert_array_equal(vx[:, 3], csv[near, 3])
     np.testing.assert_array_equal(vx[:, 5], csv[near, 5])
+
+
+@pytest.mark.gpu
+def test_lbm_run_interpolated_walls(tmp_path, gpu_lib):
+    """lbm_run's interpolated_walls key: a physics-mode run completes and
+    differs from half-way bounce-back; a parity-mode run is refused with the
+    library's message (a status, not a fault)."""
+    from pv_dec_original_gb300 import build, geometry as G
+    build.build()
+    d = load(fixtures("sim")[0])
+    tri = d["tri12"]
+    stl = str(tmp_path / "e.stl")
+    G.write_stl_ascii(stl, G.Surface(tri[:, :9].reshape(-1, 3, 3).copy(), tri[:, 9:].copy()))
+    runs = {}
+    for name, extra in (("half", "mode 1\n"), ("interp", "mode 1\ninterpolated_walls 1\n"),
+                        ("parity", "mode 0\ninterpolated_walls 1\n")):
+        out = tmp_path / name
+        out.mkdir()
+        cfg = tmp_path / f"{name}.cfg"
+        cfg.write_text(f"stl {stl}\nspacing 1.0\ntau 0.8\ndt 8e-06\nend_time 0.000244\noutput_every 30\n"
+                       f"output_dir {out}\nprecision 1\ninlet_face 0\ninlet_plane -1\noutlet_face 4\n"
+                       f"outlet_plane -1\n" + extra)
+        runs[name] = subprocess.run([os.path.join(BUILD, "lbm_run"), str(cfg)], capture_output=True, text=True,
+                                    timeout=300)
+    assert runs["half"].returncode == 0, runs["half"].stderr
+    assert runs["interp"].returncode == 0, runs["interp"].stderr
+    a = np.loadtxt(str(tmp_path / "half" / "FlowHemodynamics" / "30_FlowHemodynamics.csv"), delimiter=",",
+                   skiprows=1)
+    b = np.loadtxt(str(tmp_path / "interp" / "FlowHemodynamics" / "30_FlowHemodynamics.csv"), delimiter=",",
+                   skiprows=1)
+    assert a.shape == b.shape and not np.array_equal(a[:, 3], b[:, 3])
+    assert runs["parity"].returncode == 1
+    assert "physics-mode" in runs["parity"].stderr
