@@ -378,6 +378,40 @@ def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
             "l2": "not flushed (populations exceed L2)", "launches_total": launches}
 
 
+def small_ensembles_extra(cr, device, sizes=(1, 4, 16, 64), steps=3000):
+    """Launch-bound lattices: 1-64 seeded vessels (32x32x64 boxes, about 6k
+    active nodes each) packed into one lattice, graph-replayed (96 steps a
+    graph) with one step-kernel launch per step against persistent launches
+    (lbm_set_persistent, 32 steps a launch, grid barrier between steps).
+    CUDA events around `steps` steps after 200 warm-up steps; the lattices
+    fit in L2 (no flush: this measures launch and barrier cost)."""
+    from pv_dec_original_gb300 import warmstart as WS
+    from pv_dec_original_gb300.ensemble import Ensemble
+    rows = []
+    for n in sizes:
+        members = WS.vessel_members(n, seed=5)
+        for prec in ("f32", "f16"):
+            us = {}
+            for persist in (0, 32):
+                e = Ensemble(members, 19, prec, 0.6, device=device, steady=True, collision=1)
+                e.solver.set_persistent(persist)
+                e.solver.set_graph_steps(96)
+                st = e.solver.stream()
+                e.step(200)
+                a, b = cr.event(), cr.event()
+                cr.record(a, st)
+                e.step_async(steps)
+                cr.record(b, st)
+                us[persist] = cr.elapsed_ms(a, b) * 1e3 / steps
+                e.solver.check_status()
+                nact = e.active
+                e.solver.close()
+            rows.append({"members": n, "storage": prec, "active_nodes": nact, "flat_us_per_step": us[0],
+                         "persistent_us_per_step": us[32], "flat_mlups": nact / us[0],
+                         "persistent_mlups": nact / us[32]})
+    return {"rows": rows, "timing": f"CUDA events around {steps} steps; L2 not flushed (lattices fit in L2)"}
+
+
 def warmstart_extra(device, n_train=32, n_test=6, tau=0.55, box=(64, 64, 128)):
     """Learned warm start (scaled-down C5: 128x64x64 grids instead of
     128x128x256, 32 training vessels of radius 8-18): train on the device, then on held-out
@@ -637,6 +671,8 @@ def run_ours(args):
         extra["ensemble_c4"] = ensemble_extra(capi, cr, local, args.Q)
     if extras and not args.no_warmstart:
         extra["warmstart_c5"] = warmstart_extra(local)
+    if ws == 1 and args.small_ensembles:
+        extra["small_ensembles"] = small_ensembles_extra(cr, local)
 
     # end to end through the C ABI: per e2e step, H2D of a 100-step inlet
     # table slice from pinned memory, 100 LBM steps (graph replay), D2H of
@@ -788,6 +824,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurement")
     ap.add_argument("--no-precision", action="store_true", help="skip the 384x288x768 precision measurement")
     ap.add_argument("--no-warmstart", action="store_true", help="skip the learned warm-start measurement")
+    ap.add_argument("--small-ensembles", action="store_true",
+                    help="add the launch-bound small-ensemble measurement (flat vs persistent launches)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--variant", type=int, default=None, help="force a launch shape (skips the autotuner)")
     args = ap.parse_args()

@@ -295,6 +295,29 @@ lbm_status lbm_get_stream(lbm_handle* h, void** stream);
 lbm_status lbm_get_launch_count(lbm_handle* h, int64_t* launches);
 /* Steps per captured CUDA graph (0 = launch kernels directly). */
 lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph);
+/* Persistent stepping: each launch of the step kernel runs steps_per_launch
+ * (even, >= 2) steps, one cooperative grid of at most as many blocks as fit
+ * on the GPU at once, threads walking the active nodes with a grid stride
+ * and a grid barrier between steps (0 = one launch per step, the default).
+ * Results are bit-identical to one launch per step.  With graph steps set,
+ * steps_per_graph must be a multiple of steps_per_launch and the graph
+ * replays steps_per_graph / steps_per_launch persistent launches.  For
+ * lattices whose step is shorter than a launch (single small vessels,
+ * ensembles of small vessels); lattices beyond 32-bit population offsets
+ * (Q * stride >= 2^31) are refused (LBM_ERR_UNSUPPORTED) at the next step.
+ * Each barrier wait is bounded (~0.25 s): a wait that gives up ends the
+ * launch and the next lbm_step / lbm_check_status returns LBM_ERR_CUDA.
+ * New interface: the reference has one host loop iteration per step
+ * (Simulation.cpp:560-597). */
+lbm_status lbm_set_persistent(lbm_handle* h, int steps_per_launch);
+/* Testing the bounded barrier: extra arrivals every barrier of the next
+ * persistent launches waits for (0 in normal use).  A count far above any
+ * grid size (e.g. 0x40000000) makes the next persistent launch's first
+ * barrier unreachable: every block's wait gives up (well under a second),
+ * the launch ends, and the next lbm_step / lbm_check_status returns
+ * LBM_ERR_CUDA and clears the barrier; the state is then undefined until the
+ * next lbm_init_*. */
+lbm_status lbm_preset_barrier(lbm_handle* h, unsigned extra_arrivals);
 
 /* Launch-shape variants of the step kernel: one node per thread with
  * (block size, minimum resident blocks per SM) = (128,12) (128,10) (128,8)

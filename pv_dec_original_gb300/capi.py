@@ -65,7 +65,7 @@ EXPORTS = [
     "lbm_set_waveform", "lbm_init_equilibrium",
     "lbm_init_from_macro", "lbm_step", "lbm_step_async", "lbm_check_status", "lbm_sync", "lbm_get_counts", "lbm_get_classes", "lbm_get_distributions",
     "lbm_set_distributions", "lbm_get_macro", "lbm_get_wss", "lbm_get_conservation", "lbm_save", "lbm_load",
-    "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_autotune", "lbm_set_variant",
+    "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_set_persistent", "lbm_preset_barrier", "lbm_autotune", "lbm_set_variant",
     "lbm_moment_sums_noalloc",
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
     "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
@@ -128,6 +128,8 @@ def load(build_if_missing: bool = True):
     L.lbm_get_stream.argtypes = [P, C.POINTER(P)]
     L.lbm_get_launch_count.argtypes = [P, C.POINTER(C.c_int64)]
     L.lbm_set_graph_steps.argtypes = [P, C.c_int]
+    L.lbm_set_persistent.argtypes = [P, C.c_int]
+    L.lbm_preset_barrier.argtypes = [P, C.c_uint]
     L.lbm_autotune.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     L.lbm_set_variant.argtypes = [P, C.c_int]
     L.lbm_moment_sums_noalloc.argtypes = [P, C.c_int64, C.c_int, P, P]
@@ -295,6 +297,14 @@ class Solver:
 
     def set_graph_steps(self, n):
         self._c(load().lbm_set_graph_steps(self.h, int(n)))
+
+    def set_persistent(self, n):
+        """Steps per persistent (cooperative, grid-barrier) launch; 0 = one launch per step."""
+        self._c(load().lbm_set_persistent(self.h, int(n)))
+
+    def preset_barrier(self, extra_arrivals):
+        """Testing: extra arrivals the persistent barrier waits for (see lbm_preset_barrier)."""
+        self._c(load().lbm_preset_barrier(self.h, int(extra_arrivals)))
 
     def autotune(self, trial_steps=10):
         """Time every launch variant on a snapshot of the state; keep the fastest."""

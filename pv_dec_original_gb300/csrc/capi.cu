@@ -85,6 +85,8 @@ struct lbm_handle {
     double* out_f = nullptr;    // read-out scratch, allocated on first use
     double* macro = nullptr;    // rho / u read-out scratch
     int graph_steps = 0;
+    int persist = 0;             // steps per persistent launch (0: one launch per step)
+    unsigned* bar = nullptr;     // grid barrier of persistent launches: arrivals, extra arrivals (tests)
     cudaGraphExec_t gexec = nullptr;
     int gexec_parity = -1;
     int gexec_cur = -1;
@@ -345,6 +347,7 @@ int start_state(lbm_handle* h, bool reset) {
     int64_t sl[2] = {h->steps, h->steps};
     CK(h, cudaMemcpyAsync(h->slots, sl, sizeof(sl), cudaMemcpyHostToDevice, h->st));
     CK(h, cudaMemsetAsync(h->flags, 0, sizeof(unsigned), h->st));
+    if (h->bar) CK(h, cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), h->st));
     StepParams p = make_params(h, 1);
     CK(h, launch(h, 1, p));
     h->cur = 1;
@@ -359,8 +362,15 @@ int check_flags(lbm_handle* h) {
     unsigned f = 0;
     CK(h, cudaMemcpyAsync(&f, h->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
-    if (f & FLAG_TIMEOUT)
-        return fail(h, LBM_ERR_CUDA, "tiled step: a bulk copy did not complete within the wait limit");
+    if (f & FLAG_TIMEOUT) {
+        // a bounded wait gave up; clear the flag and a barrier left half-arrived
+        CK(h, cudaMemsetAsync(h->flags, 0, sizeof(unsigned), h->st));
+        if (h->bar) CK(h, cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), h->st));
+        CK(h, cudaStreamSynchronize(h->st));
+        return fail(h, LBM_ERR_CUDA,
+                    "a step kernel's bounded wait gave up (a tiled step's bulk copy or a persistent launch's grid "
+                    "barrier)");
+    }
     if (f & FLAG_NONFINITE)
         return fail(h, LBM_ERR_NONFINITE, "a density became NaN/Inf: the run diverged (check tau and the inlet)");
     return LBM_OK;
@@ -375,6 +385,32 @@ int one_step(lbm_handle* h) {
     return LBM_OK;
 }
 
+// One persistent launch of h->persist (even) steps: cur and the counter
+// parity come back to where they were.
+int multi_steps(lbm_handle* h) {
+    const int n = h->persist;
+    const StepParams even = make_params(h, 0);
+    h->cur = 1 - h->cur;
+    h->steps++;
+    const StepParams odd = make_params(h, 0);
+    h->cur = 1 - h->cur;
+    h->steps--;
+    cudaError_t e;
+    switch (h->d.precision) {
+        case LBM_F64: e = launch_multi_f64(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
+        case LBM_F32: e = launch_multi_f32(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
+        case LBM_F16: e = launch_multi_f16(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
+        default: e = launch_multi_bf16(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
+    }
+    if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("persistent step launch: ") + cudaGetErrorString(e));
+    h->launches++;
+    h->steps += n;
+    h->since_start += n;
+    return LBM_OK;
+}
+
+bool persist_ok(const lbm_handle* h) { return (int64_t)h->d.Q * h->stride < ((int64_t)1 << 31); }
+
 // Capture graph_steps (even) launches starting at the current parity.
 int build_graph(lbm_handle* h) {
     drop_graph(h);
@@ -382,16 +418,34 @@ int build_graph(lbm_handle* h) {
     const int cur0 = h->cur;
     cudaGraph_t graph = nullptr;
     CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < h->graph_steps; ++k) {
+    for (int k = 0; k < h->graph_steps;) {
+        if (h->persist > 0) {
+            // graph_steps is a multiple of persist (lbm_set_persistent / lbm_set_graph_steps)
+            int rc = multi_steps(h);
+            if (rc) {
+                cudaStreamEndCapture(h->st, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                h->steps = steps0;
+                h->since_start = since0;
+                h->launches = launches0;
+                return rc;
+            }
+            k += h->persist;
+            continue;
+        }
         StepParams p = make_params(h, 0);
         cudaError_t e = launch(h, 0, p);
         if (e != cudaSuccess) {
             cudaStreamEndCapture(h->st, &graph);
             if (graph) cudaGraphDestroy(graph);
+            h->steps = steps0;
+            h->cur = cur0;
+            h->launches = launches0;
             return fail(h, LBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
         }
         h->cur = 1 - h->cur;
         h->steps++;
+        ++k;
     }
     CK(h, cudaStreamEndCapture(h->st, &graph));
     cudaError_t e = cudaGraphInstantiate(&h->gexec, graph, 0);
@@ -788,6 +842,7 @@ lbm_status lbm_destroy(lbm_handle* h) {
     free_geometry(h);
     if (h->slots) cudaFree(h->slots);
     if (h->flags) cudaFree(h->flags);
+    if (h->bar) cudaFree(h->bar);
     if (h->amp) cudaFree(h->amp);
     if (h->wave_off) cudaFree(h->wave_off);
     if (h->wave_len) cudaFree(h->wave_len);
@@ -1154,6 +1209,8 @@ lbm_status lbm_step_async(lbm_handle* h, int nsteps) {
     REQUIRE(h, nsteps >= 0, LBM_ERR_ARG, "negative step count");
     CK(h, cudaSetDevice(h->d.device));
     if (nsteps > 0) h->wss_from_ckpt = false;
+    REQUIRE(h, h->persist == 0 || persist_ok(h), LBM_ERR_UNSUPPORTED,
+            "persistent steps need 32-bit population offsets (Q * stride < 2^31)");
     int left = nsteps;
     // Graph replay: a captured graph bakes the buffer roles (cur) and the
     // counter slot (step parity); both flip every step, so a graph built at
@@ -1171,10 +1228,15 @@ lbm_status lbm_step_async(lbm_handle* h, int nsteps) {
             if (rc) return rc;
         }
         CK(h, cudaGraphLaunch(h->gexec, h->st));
-        h->launches += h->graph_steps;
+        h->launches += h->persist > 0 ? h->graph_steps / h->persist : h->graph_steps;
         h->steps += h->graph_steps;
         h->since_start += h->graph_steps;
         left -= h->graph_steps;  // even count: cur and parity return to the captured pair
+    }
+    while (h->persist > 0 && left >= h->persist) {
+        int rc = multi_steps(h);
+        if (rc) return rc;
+        left -= h->persist;
     }
     for (; left > 0; --left) {
         int rc = one_step(h);
@@ -1192,8 +1254,35 @@ lbm_status lbm_sync(lbm_handle* h) {
 lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph) {
     if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
     REQUIRE(h, steps_per_graph >= 0 && steps_per_graph % 2 == 0, LBM_ERR_ARG, "steps per graph must be even and >= 0");
+    REQUIRE(h, h->persist == 0 || steps_per_graph % h->persist == 0, LBM_ERR_ARG,
+            "steps per graph must be a multiple of the steps per persistent launch");
     drop_graph(h);
     h->graph_steps = steps_per_graph;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_persistent(lbm_handle* h, int steps_per_launch) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, steps_per_launch == 0 || (steps_per_launch >= 2 && steps_per_launch % 2 == 0), LBM_ERR_ARG,
+            "steps per persistent launch must be 0 or even and >= 2");
+    REQUIRE(h, steps_per_launch == 0 || h->graph_steps % steps_per_launch == 0, LBM_ERR_ARG,
+            "steps per graph must be a multiple of the steps per persistent launch");
+    CK(h, cudaSetDevice(h->d.device));
+    if (steps_per_launch > 0 && !h->bar) {
+        CK(h, cudaMalloc(&h->bar, 2 * sizeof(unsigned)));
+        CK(h, cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), h->st));
+    }
+    drop_graph(h);
+    h->persist = steps_per_launch;
+    return LBM_OK;
+}
+
+lbm_status lbm_preset_barrier(lbm_handle* h, unsigned extra_arrivals) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->bar, LBM_ERR_STATE, "no persistent barrier: call lbm_set_persistent first");
+    CK(h, cudaSetDevice(h->d.device));
+    CK(h, cudaMemcpyAsync(h->bar + 1, &extra_arrivals, sizeof(unsigned), cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
     return LBM_OK;
 }
 

@@ -89,6 +89,10 @@ __host__ __device__ constexpr int lat_c(int q, int axis) {
 // conversion, the moments weight g by unit_q (a multiply-add in place of an
 // add), and the equilibrium in these units, (w_q / unit_q) (B + ...), has
 // the same factor geq (1024, 1) for every direction.
+// load<Q, CG>: CG = false reads through the non-coherent (read-only) path,
+// valid while no thread of the launch writes the buffer; CG = true reads
+// from L2 (ld.global.cg), for a persistent launch whose steps read what its
+// earlier steps wrote.
 enum Precision : int { P_F64 = 0, P_F32 = 1, P_F16 = 2, P_BF16 = 3 };
 
 template <typename S> struct Store;
@@ -97,8 +101,8 @@ template <> struct Store<double> {
     using real = double;
     static constexpr bool offset = false;
     static constexpr bool scaled = false;
-    template <int Q>
-    __device__ static __forceinline__ real load(const double* p, int q) { return *p; }
+    template <int Q, bool CG = false>
+    __device__ static __forceinline__ real load(const double* p, int q) { return CG ? __ldcg(p) : *p; }
     template <int Q>
     __device__ static __forceinline__ real decode(double v, int q) { return v; }
     template <int Q>
@@ -109,8 +113,8 @@ template <> struct Store<float> {
     using real = float;
     static constexpr bool offset = true;
     static constexpr bool scaled = false;
-    template <int Q>
-    __device__ static __forceinline__ real load(const float* p, int q) { return __ldg(p); }
+    template <int Q, bool CG = false>
+    __device__ static __forceinline__ real load(const float* p, int q) { return CG ? __ldcg(p) : __ldg(p); }
     template <int Q>
     __device__ static __forceinline__ real decode(float v, int q) { return v; }
     template <int Q>
@@ -125,8 +129,10 @@ template <> struct Store<__half> {
     static constexpr float geq = S;  // w_q / unit_q
     template <int Q>
     __host__ __device__ static constexpr float unit(int q) { return (float)(Lat<Q>::w(q) / 1024.0); }
-    template <int Q>
-    __device__ static __forceinline__ real load(const __half* p, int q) { return __half2float(__ldg(p)); }
+    template <int Q, bool CG = false>
+    __device__ static __forceinline__ real load(const __half* p, int q) {
+        return __half2float(CG ? __ldcg(p) : __ldg(p));
+    }
     template <int Q>
     __device__ static __forceinline__ real decode(__half v, int q) { return __half2float(v); }
     template <int Q>
@@ -140,9 +146,9 @@ template <> struct Store<__nv_bfloat16> {
     static constexpr float geq = 1.0f;
     template <int Q>
     __host__ __device__ static constexpr float unit(int q) { return (float)Lat<Q>::w(q); }
-    template <int Q>
+    template <int Q, bool CG = false>
     __device__ static __forceinline__ real load(const __nv_bfloat16* p, int q) {
-        return __bfloat162float(__ldg(p));
+        return __bfloat162float(CG ? __ldcg(p) : __ldg(p));
     }
     template <int Q>
     __device__ static __forceinline__ real decode(__nv_bfloat16 v, int q) { return __bfloat162float(v); }

@@ -7,4 +7,9 @@ cudaError_t launch_step_f16(int Q, int mode, int kind, int variant, const StepPa
     return launch_typed<__half>(Q, mode, kind, variant, p, st);
 }
 
+cudaError_t launch_multi_f16(int Q, int mode, const StepParams& even, const StepParams& odd, int nsteps,
+                              unsigned* bar, cudaStream_t st) {
+    return launch_multi_typed<__half>(Q, mode, even, odd, nsteps, bar, st);
+}
+
 }  // namespace lbm

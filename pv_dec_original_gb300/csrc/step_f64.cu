@@ -11,6 +11,11 @@ cudaError_t launch_step_f64(int Q, int mode, int kind, int variant, const StepPa
     return launch_typed<double>(Q, mode, kind, variant, p, st);
 }
 
+cudaError_t launch_multi_f64(int Q, int mode, const StepParams& even, const StepParams& odd, int nsteps,
+                              unsigned* bar, cudaStream_t st) {
+    return launch_multi_typed<double>(Q, mode, even, odd, nsteps, bar, st);
+}
+
 cudaError_t init_state_f64(int Q, int what, void* f, int64_t stride, const double* fa, int64_t nact,
                            cudaStream_t st) {
     return init_typed<double>(Q, what, f, stride, fa, nact, st);

@@ -528,6 +528,7 @@ __device__ __forceinline__ void comp_add(float2& acc, float v) {
 // Fold one half of the FP32 stress ring (slots half * kFoldEvery ..
 // + kFoldEvery - 1, i.e. kFoldEvery consecutive steps in step order) into
 // next-to-wall node nw's compensated accumulators.
+template <bool CG = false>
 __device__ __forceinline__ void fold_half(const StepParams& P, int64_t nw, int half) {
     const float4* __restrict__ ring = reinterpret_cast<const float4*>(P.nw_ring);
     float2 acc[4];
@@ -535,7 +536,8 @@ __device__ __forceinline__ void fold_half(const StepParams& P, int64_t nw, int h
     for (int k = 0; k < 4; ++k) acc[k] = P.nw_accf[k * P.nnw + nw];
 #pragma unroll 4
     for (int j = 0; j < kFoldEvery; ++j) {
-        const float4 v = ring[(int64_t)(half * kFoldEvery + j) * P.nnw + nw];
+        const float4* src = ring + (int64_t)(half * kFoldEvery + j) * P.nnw + nw;
+        const float4 v = CG ? __ldcg(src) : *src;
         comp_add(acc[0], v.x);
         comp_add(acc[1], v.y);
         comp_add(acc[2], v.z);
@@ -810,7 +812,7 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
 //   q_w >= 1/2: g[q] = f*_i(x) / (2 q_w) + (1 - 1/(2 q_w)) f*_q(x),  i = opp q.
 // Compiled only into the kernels launched when wall distances are set
 // (WALLS), so the half-way kernels carry none of it.
-template <int Q, typename S, bool WIDE>
+template <int Q, typename S, bool WIDE, bool CG = false>
 __device__ __forceinline__ void interpolate_walls(const StepParams& P, int64_t a, uint64_t word, int32_t e,
                                                        uint32_t miss, typename Store<S>::real (&g)[Q]) {
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
@@ -827,10 +829,10 @@ __device__ __forceinline__ void interpolate_walls(const StepParams& P, int64_t a
             if ((miss >> q) & 1u) continue;  // no fluid node at x + c_q: half-way
             A = (R)2 * (R)qw;
             const int32_t dq = __ldg(P.seg_delta + word_segment(word) * DR + Lat<Q>::opp(q));
-            X = Store<S>::template load<Q>(fin_a + (I)(Lat<Q>::opp(q) * st + dq), q);
+            X = Store<S>::template load<Q, CG>(fin_a + (I)(Lat<Q>::opp(q) * st + dq), q);
         } else {
             A = (R)1 / ((R)2 * (R)qw);
-            X = Store<S>::template load<Q>(fin_a + (I)(q * st), q);
+            X = Store<S>::template load<Q, CG>(fin_a + (I)(q * st), q);
         }
         g[q] = A * g[q] + ((R)1 - A) * X;
     }
@@ -847,8 +849,9 @@ struct Pulled {
 };
 
 // The pull of node a: its populations after streaming (and, with WALLS,
-// interpolated bounce-back) into g, plus its boundary-list data.
-template <int Q, typename S, int MODE, int KIND, bool WIDE, bool WALLS = false>
+// interpolated bounce-back) into g, plus its boundary-list data.  CG: the
+// populations are read from L2 (a persistent launch, see Store::load).
+template <int Q, typename S, int MODE, int KIND, bool WIDE, bool WALLS = false, bool CG = false>
 __device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, const uint64_t word,
                                           const int32_t sp_entry, typename Store<S>::real (&g)[Q], Pulled& pl) {
     using I = typename std::conditional<WIDE, int64_t, int32_t>::type;
@@ -887,7 +890,7 @@ __device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, 
     const S* __restrict__ fin_a = fin + ai;
     if (direct) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q>(fin_a + q * st, q);
+        for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q, CG>(fin_a + q * st, q);
     } else {
         int32_t dl[DR];
         const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
@@ -907,11 +910,11 @@ __device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, 
             } else {
                 off = q * st + (src_missing ? 0 : dl[q]);
             }
-            g[q] = Store<S>::template load<Q>(fin_a + off, q);  // w_opp(q) == w_q: same decode
+            g[q] = Store<S>::template load<Q, CG>(fin_a + off, q);  // w_opp(q) == w_q: same decode
         }
         if constexpr (MODE == MODE_PHYSICS && WALLS) {
             // interpolated bounce-back (the launcher picks this kernel when wall distances are set)
-            if (miss != 0) interpolate_walls<Q, S, WIDE>(P, a, word, sp_entry, miss, g);
+            if (miss != 0) interpolate_walls<Q, S, WIDE, CG>(P, a, word, sp_entry, miss, g);
         }
     }
 
@@ -925,12 +928,12 @@ __device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, 
 
 // One node's update: pull, boundary rules, wall shear stress, collision and
 // store (or the read-out sums).
-template <int Q, typename S, int MODE, int KIND, bool WIDE, bool WALLS = false>
+template <int Q, typename S, int MODE, int KIND, bool WIDE, bool WALLS = false, bool CG = false>
 __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a, const uint64_t word,
                                             const int32_t sp_entry, double (&part)[kPartialStride]) {
     typename Store<S>::real g[Q];
     Pulled pl;
-    pull_node<Q, S, MODE, KIND, WIDE, WALLS>(P, a, word, sp_entry, g, pl);
+    pull_node<Q, S, MODE, KIND, WIDE, WALLS, CG>(P, a, word, sp_entry, g, pl);
     node_finish<Q, S, MODE, KIND, WIDE>(P, a, word, pl.s, pl.lng, pl.c, pl.miss, g, pl.nr, pl.slot, part);
 }
 
@@ -1015,6 +1018,160 @@ cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
         step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true><<<(unsigned)nblocks, kStepThreads, 0, st>>>(q);
     }
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Persistent multi-step kernel (small lattices and ensembles of small
+// vessels, where a step is shorter than a launch): one cooperative launch of
+// at most as many blocks as are resident at once runs nsteps steps, each
+// thread walking the nodes with a grid stride, with a grid barrier between
+// steps.  PP.p[0] / PP.p[1] are the parameters of the launch's even / odd
+// steps (buffer roles and counter slots swap each step).  Populations and
+// the stress ring are read from L2 (Store::load CG): they were written by
+// other SMs earlier in the same launch.  Every barrier wait is bounded: a
+// block that gives up raises FLAG_TIMEOUT and returns, after which every
+// other block gives up at its next barrier too.
+//
+// Barrier word bar[0] counts arrivals over the whole launch: barrier j of a
+// grid of n blocks completes when it reaches (j + 1) n (+ bar[1], zero
+// except when a test asks for a barrier that cannot complete).  Arrival is
+// a release add, the wait an acquire poll: the release orders this block's
+// writes (made visible to its thread 0 by the preceding __syncthreads)
+// before the arrival, the acquire orders the other blocks' writes before
+// this block's next loads.  Each block adds 1 more when it leaves; the last
+// to leave stores 0, so the next launch starts from zero.  The host clears
+// both words when it reads FLAG_TIMEOUT.
+
+constexpr long kBarrierPolls = 1L << 20;  // L2 reads: well under a second
+
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Returns false when the wait gave up.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned target, unsigned* flags) {
+    __shared__ int passed;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        red_release_add(bar, 1u);
+        const unsigned goal = target + ld_acquire(bar + 1);
+        int ok = 0;
+        for (long it = 0; it < kBarrierPolls; ++it) {
+            if ((int)(ld_acquire(bar) - goal) >= 0) {
+                ok = 1;
+                break;
+            }
+        }
+        if (!ok) atomicOr(flags, FLAG_TIMEOUT);
+        passed = ok;
+    }
+    __syncthreads();
+    return passed != 0;
+}
+
+// The launch's last block to leave resets the arrival count.
+__device__ __forceinline__ void grid_leave(unsigned* bar, unsigned total) {
+    if (threadIdx.x == 0 && atomicAdd(bar, 1u) == total - 1) atomicExch(bar, 0u);
+}
+
+struct StepPair {
+    StepParams p[2];
+};
+
+constexpr int kMultiThreads = 256;
+
+// minimum resident blocks per SM: register caps of 255 (FP64), 128 (D3Q27)
+// and 64 (D3Q19 FP32 / FP16 / BF16) registers a thread, the largest blocks
+// per SM that do not spill (the grid-stride loop keeps more live state than
+// the flat kernel's 40 registers)
+template <int Q, typename S>
+constexpr int multi_min_blocks() {
+    return std::is_same<S, double>::value ? 1 : (Q == 27 ? 2 : 4);
+}
+
+template <int Q, typename S, int MODE, bool WALLS>
+__global__ void __launch_bounds__(kMultiThreads, multi_min_blocks<Q, S>())
+    step_kernel_multi(const StepPair PP, int nsteps, unsigned* bar) {
+    double part[kPartialStride];
+    const int64_t T = (int64_t)gridDim.x * kMultiThreads;
+    const int64_t t0 = (int64_t)blockIdx.x * kMultiThreads + threadIdx.x;
+    for (int k = 0; k < nsteps; ++k) {
+        const StepParams& P = PP.p[k & 1];
+        const int64_t step = __ldcg(P.step_base);
+        if (t0 == 0) *P.step_next = step + 1;
+        if constexpr (Store<S>::offset) {
+            // the stress ring's fold, as the fold blocks of a flat launch do it
+            if (step % kFoldEvery == 0) {
+                const int writing = (int)((step % kRingSlots) / kFoldEvery);
+                for (int64_t nw = t0; nw < P.nnw; nw += T) fold_half<true>(P, nw, 1 - writing);
+            }
+        }
+        for (int64_t a = t0; a < P.nact; a += T)
+            node_update<Q, S, MODE, KIND_STEP, false, WALLS, true>(P, a, __ldg(P.act_word + a),
+                                                                  __ldg(P.sp_of_act + a), part);
+        if (k + 1 < nsteps && !grid_barrier(bar, (unsigned)(k + 1) * gridDim.x, P.flags)) return;
+    }
+    grid_leave(bar, (unsigned)nsteps * gridDim.x);
+}
+
+template <int Q, typename S, int MODE, bool WALLS>
+cudaError_t launch_multi_t(const StepPair& pp, int nsteps, unsigned* bar, cudaStream_t st) {
+    auto kern = step_kernel_multi<Q, S, MODE, WALLS>;
+    static int per_sm = 0;  // resident blocks per SM of this instantiation
+    static int sms = 0;
+    if (per_sm == 0) {
+        int dev = 0, v = 0, n = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kMultiThreads, 0);
+        if (e != cudaSuccess) return e;
+        if (v <= 0 || n <= 0) return cudaErrorInvalidConfiguration;
+        sms = n;
+        per_sm = v;
+    }
+    const StepParams& p = pp.p[0];
+    const int64_t work = p.nact > p.nnw ? p.nact : p.nnw;
+    const int64_t need = ceil_div(work, kMultiThreads);
+    const int64_t full = (int64_t)per_sm * sms;
+    const unsigned nb = (unsigned)(need < 1 ? 1 : (need < full ? need : full));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(nb);
+    cfg.blockDim = dim3(kMultiThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, pp, nsteps, bar);
+}
+
+// nsteps steps in one launch; lattices with 32-bit population offsets only.
+template <typename S>
+cudaError_t launch_multi_typed(int Q, int mode, const StepParams& even, const StepParams& odd, int nsteps,
+                               unsigned* bar, cudaStream_t st) {
+    if ((int64_t)Q * even.stride >= ((int64_t)1 << 31) || nsteps < 1) return cudaErrorInvalidValue;
+    if (even.nact <= 0) return cudaSuccess;
+    StepPair pp{};
+    pp.p[0] = even;
+    pp.p[1] = odd;
+    pp.p[0].fold_blocks = pp.p[1].fold_blocks = 0;
+    const bool walls = mode == MODE_PHYSICS && even.sp_q != nullptr;
+    if (Q == 19) {
+        if (mode == MODE_PARITY) return launch_multi_t<19, S, MODE_PARITY, false>(pp, nsteps, bar, st);
+        return walls ? launch_multi_t<19, S, MODE_PHYSICS, true>(pp, nsteps, bar, st)
+                     : launch_multi_t<19, S, MODE_PHYSICS, false>(pp, nsteps, bar, st);
+    }
+    if (mode == MODE_PARITY) return launch_multi_t<27, S, MODE_PARITY, false>(pp, nsteps, bar, st);
+    return walls ? launch_multi_t<27, S, MODE_PHYSICS, true>(pp, nsteps, bar, st)
+                 : launch_multi_t<27, S, MODE_PHYSICS, false>(pp, nsteps, bar, st);
 }
 
 // ---------------------------------------------------------------------------
