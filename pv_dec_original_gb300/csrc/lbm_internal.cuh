@@ -85,6 +85,7 @@ struct StepParams {
     int64_t nw_stride;        // plane stride of nw_nf (nnw + 1 rounded up to 4)
     float* nw_ring;           // float4 [kRingSlots][nnw]: step s in slot s % kRingSlots
     int64_t fold_blocks;      // leading blocks of a step launch that fold the ring (set by the launcher)
+    int pdl_early;            // step launch: let the next launch begin at block start (else at block end)
     float2* nw_accf;          // [4][nnw]
     void* nw_prev;            // parity: rho, ux, uy, uz of the previous collision, [4][nnw]
     double tau;

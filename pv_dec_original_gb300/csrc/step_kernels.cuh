@@ -940,6 +940,20 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
 // WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
 // lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
 // One thread per active node.
+// Programmatic dependent launch: a step kernel is launched with
+// programmatic stream serialization, so it may start while the previous
+// kernel of the stream finishes.  Each block reads its read-only node data,
+// then waits (pdl_wait) for the previous grid to complete and its writes to
+// be visible before it reads or writes any state.  Without a preceding
+// dependent launch the wait returns at once.  The next launch begins once
+// every block has called pdl_trigger: at block start when the grid is
+// larger than one wave of resident blocks (P.pdl_early; the next grid's
+// blocks then take the SMs this grid's tail leaves), at block end otherwise
+// (a grid that fits at once would have the next grid's blocks wait beside
+// its running blocks: 83k-node lattices stepped 12% slower).
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1, bool WIDE = true,
           bool WALLS = false>
 __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
@@ -950,11 +964,14 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
     }
     int64_t blk = blockIdx.x;
     if constexpr (KIND == KIND_STEP) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
+        if (P.pdl_early) pdl_trigger();
         if constexpr (Store<S>::offset) {
             // leading blocks: the stress ring's fold (FP32-arithmetic formats)
             if (blk < P.fold_blocks) {
+                pdl_wait();
+                if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
                 fold_blocks_work(P, blk, BT);
+                if (!P.pdl_early) pdl_trigger();
                 return;
             }
             blk -= P.fold_blocks;
@@ -970,12 +987,22 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
         blk = (blk & 1) ? nm - 1 - (blk >> 1) : (blk >> 1);
     }
     const int64_t a = blk * BT + threadIdx.x;
+    // the node's word and its boundary-list entry (-1 for most nodes),
+    // loaded side by side (read-only: before the dependency wait)
+    uint64_t word = 0;
+    int32_t sp_entry = -1;
     if (a < P.nact) {
-        // the node's word and its boundary-list entry (-1 for most nodes),
-        // loaded side by side
-        const uint64_t word = __ldg(P.act_word + a);
-        const int32_t sp_entry = __ldg(P.sp_of_act + a);
-        node_update<Q, S, MODE, KIND, WIDE, WALLS>(P, a, word, sp_entry, part);
+        word = __ldg(P.act_word + a);
+        sp_entry = __ldg(P.sp_of_act + a);
+    }
+    if constexpr (KIND == KIND_STEP) {
+        pdl_wait();
+        // block 0 is a node block when there are no fold blocks
+        if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
+    }
+    if (a < P.nact) node_update<Q, S, MODE, KIND, WIDE, WALLS>(P, a, word, sp_entry, part);
+    if constexpr (KIND == KIND_STEP) {
+        if (!P.pdl_early) pdl_trigger();
     }
     if constexpr (KIND == KIND_READOUT) block_partials<BT>(part, P.partials);
 }
@@ -990,6 +1017,32 @@ struct Variant {
 };
 constexpr int kFlatVariants = 5;  // 0..4; 5 = tiled
 constexpr Variant kVariants[kFlatVariants] = {{128, 12}, {128, 10}, {128, 8}, {256, 3}, {256, 1}};
+
+// A step-kernel launch with programmatic stream serialization (see
+// pdl_trigger / pdl_wait); minb: the kernel's minimum resident blocks per SM.
+inline cudaError_t launch_dependent(void (*kern)(const StepParams), int64_t nblocks, int bt, int minb,
+                                    const StepParams& p0, cudaStream_t st) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+    }
+    StepParams p = p0;
+    p.pdl_early = nblocks > (int64_t)minb * sms ? 1 : 0;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)nblocks);
+    cfg.blockDim = dim3(bt);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, p);
+}
 
 template <int Q, typename S, int MODE, int V>
 cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
@@ -1007,17 +1060,16 @@ cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
     if (walls) {
         if constexpr (PHYS) {
             if (narrow)
-                step_kernel<Q, S, MODE, KIND_STEP, 128, 8, false, true><<<(unsigned)nblocks, 128, 0, st>>>(q);
-            else
-                step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true, true>
-                    <<<(unsigned)nblocks, kStepThreads, 0, st>>>(q);
+                return launch_dependent(step_kernel<Q, S, MODE, KIND_STEP, 128, 8, false, true>, nblocks, 128, 8, q,
+                                        st);
+            return launch_dependent(step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true, true>, nblocks,
+                                    kStepThreads, 1, q, st);
         }
-    } else if (narrow) {
-        step_kernel<Q, S, MODE, KIND_STEP, BT, MB, false><<<(unsigned)nblocks, BT, 0, st>>>(q);
-    } else {
-        step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true><<<(unsigned)nblocks, kStepThreads, 0, st>>>(q);
+        return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
+    if (narrow) return launch_dependent(step_kernel<Q, S, MODE, KIND_STEP, BT, MB, false>, nblocks, BT, MB, q, st);
+    return launch_dependent(step_kernel<Q, S, MODE, KIND_STEP, kStepThreads, 1, true>, nblocks, kStepThreads, 1, q,
+                            st);
 }
 
 // ---------------------------------------------------------------------------
