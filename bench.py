@@ -441,6 +441,11 @@ def warmstart_extra(device, n_train=32, n_test=6, tau=0.55, box=(64, 64, 128)):
     hist = WS.train(net, samples, iters=2000, lr=2e-3, batch=4)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
+    # the network's forward pass is captured once for the grid size and
+    # replayed for every vessel (capture outside the timed regions)
+    x0, _ = WS.features(sols[0][0], train_m[0]["inlet_mean"], train_m[0]["period"], tau=tau, device=device)
+    net.forward_graphed(x0)
+    torch.cuda.synchronize()
     rows = []
     dev = torch.device("cuda", device)
     for m in test_m:
@@ -466,7 +471,7 @@ def warmstart_extra(device, n_train=32, n_test=6, tau=0.55, box=(64, 64, 128)):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
             x, prior = WS.features(mask, m["inlet_mean"], m["period"], tau=tau, device=device)
-            y = net.forward(x) if arm == "net" else WS.zero_output(prior)
+            y = net.forward_graphed(x) if arm == "net" else WS.zero_output(prior)
             rho, u = WS.prediction_to_device(y, prior)
             sw.init_from_macro_device(rho.data_ptr(), u.data_ptr(), True, torch.cuda.current_stream(dev).cuda_stream)
             t_pred = time.perf_counter() - t0
@@ -508,8 +513,9 @@ def warmstart_extra(device, n_train=32, n_test=6, tau=0.55, box=(64, 64, 128)):
     return {"grid": list(sols[0][0].shape), "train_vessels": n_train, "test_vessels": n_test, "tau": tau,
             "data_s": data_s, "train_s": train_s, "train_iters": 2000, "loss_first_last": [hist[0], hist[-1]],
             "criterion": "FP32 lattice WSS within 1% of the converged (residual 1e-6, FP64, from rest) WSS at 3 "
-                         "checks 100 steps apart; time = prediction (features, network, prior, smoothing, state "
-                         "build) + steps x measured FP32 time per step",
+                         "checks 100 steps apart; time = prediction (features, network forward replayed from a CUDA "
+                         "graph captured once for the grid size, prior, smoothing, state build) + steps x measured "
+                         "FP32 time per step",
             "vessels_reaching_1pct": {k: sum(r[k]["steps_1pct_wss"] is not None for r in rows)
                                       for k in ("cold", "prior", "net")},
             "net_over_cold_time": tot("net", "s_1pct_wss") / tot("cold", "s_1pct_wss"),

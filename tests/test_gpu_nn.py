@@ -288,3 +288,20 @@ def test_gpu_init_from_macro_device_matches_host(gpu_lib):
     s1.step(10)
     s2.step(10)
     np.testing.assert_array_equal(s1.distributions(), s2.distributions())
+
+
+def test_gpu_network_forward_graph_matches_eager(gpu_lib):
+    """The graph-replayed forward gives the eager forward's output bit for
+    bit, for the captured input and for a new input of the same size."""
+    import torch
+    from pv_dec_original_gb300 import warmstart as WS
+    dims = (16, 16, 32)
+    net = WS.WarmStartNet(dims, seed=5)
+    n = dims[0] * dims[1] * dims[2] * WS.C_IN
+    g = torch.Generator(device="cuda").manual_seed(0)
+    for k in range(2):
+        x = (torch.rand(n, device="cuda", generator=g) * 2 - 1).to(torch.bfloat16)
+        eager = net.forward(x).clone()
+        graphed = net.forward_graphed(x).clone()
+        torch.cuda.synchronize()
+        assert torch.equal(eager, graphed), k
