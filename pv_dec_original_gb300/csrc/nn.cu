@@ -472,7 +472,7 @@ int report(const char* what, cudaError_t e) {
     return e == cudaSuccess ? LBM_ERR_ARG : LBM_ERR_CUDA;
 }
 
-bool padded16(int c) { return c > 0 && c % 16 == 0 && c <= 64; }
+bool padded16(int c) { return c == 16 || c == 32 || c == 64; }  // the channel counts the kernels are built for
 
 Conv make_conv(const int dims_in[3], int ci, int co, int ks, int stride) {
     Conv g{};

@@ -31,7 +31,8 @@ def _to_torch_w(w, co, k, ci):
 
 @pytest.mark.parametrize("ci,co,k,s,dims", [(16, 32, 3, 1, (8, 8, 16)), (32, 64, 3, 2, (8, 16, 8)),
                                             (64, 16, 3, 1, (4, 8, 8)), (16, 16, 1, 1, (8, 8, 8)),
-                                            (64, 64, 3, 2, (8, 8, 8))])
+                                            (64, 64, 3, 2, (8, 8, 8)), (32, 32, 3, 1, (6, 10, 7)),
+                                            (16, 64, 3, 2, (5, 9, 6))])
 def test_gpu_conv3d_fwd_bwd(gpu_lib, ci, co, k, s, dims):
     L = gpu_lib.load()
     dev = torch.device("cuda", 0)
@@ -305,3 +306,14 @@ def test_gpu_network_forward_graph_matches_eager(gpu_lib):
         graphed = net.forward_graphed(x).clone()
         torch.cuda.synchronize()
         assert torch.equal(eager, graphed), k
+
+
+def test_gpu_conv_refuses_unbuilt_channel_counts(gpu_lib):
+    """Channel counts other than 16, 32 and 64 are refused before any launch."""
+    L = gpu_lib.load()
+    dev = torch.device("cuda", 0)
+    x = torch.zeros(8 * 8 * 8 * 48, dtype=torch.bfloat16, device=dev)
+    w = torch.zeros(16 * 27 * 48, dtype=torch.bfloat16, device=dev)
+    y = torch.zeros(8 * 8 * 8 * 16, dtype=torch.bfloat16, device=dev)
+    rc = L.lbm_nn_conv3d_fwd(_p(x), _d((8, 8, 8)), 48, _p(w), None, 16, 3, 1, 0, _p(y), None, None)
+    assert rc == -1  # LBM_ERR_ARG
