@@ -378,6 +378,29 @@ def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
             "l2": "not flushed (populations exceed L2)", "launches_total": launches}
 
 
+def voxelizer_extra(capi, tri, spacing=1.0, repeats=3):
+    """The +z ray-parity voxelizer on the bifurcation's STL: ray-triangle
+    tests per second (each test: 13 FP64 adds / multiplies and one FP64
+    division for the plane crossing; the in-triangle test runs only for
+    crossings), host wall clock around lbm_voxelize (triangle upload, column
+    binning, ray kernel, mask copy back), best of `repeats` after one
+    warm-up call."""
+    capi.voxelize(tri, spacing)
+    best, desc = None, None
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        _, desc = capi.voxelize(tri, spacing)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    tests = int(desc.ray_tests)
+    fp64_nominal = 1.25e12  # GB300 FP64 FLOP/s, nominal (no measured FP64 peak is recorded)
+    return {"lattice": list(desc.dims), "triangles": int(len(tri)), "points": int(np.prod(list(desc.dims))),
+            "fluid_points": int(desc.fluid_count), "ray_tests": tests, "seconds": best,
+            "tests_per_s": tests / best, "fp64_flop_per_test": 14,
+            "fp64_frac_of_nominal": tests * 14 / best / fp64_nominal,
+            "timing": "host wall clock around lbm_voxelize, best of %d after a warm-up call" % repeats}
+
+
 def small_ensembles_extra(cr, device, sizes=(1, 4, 16, 64), steps=3000):
     """Launch-bound lattices: 1-64 seeded vessels (32x32x64 boxes, about 6k
     active nodes each) packed into one lattice, graph-replayed (96 steps a
@@ -668,6 +691,11 @@ def run_ours(args):
 
     # batched ensemble (64 seeded stenosed tubes, FP16 storage): one packed
     # lattice, one launch per step, vs the same members as 64 lattices
+    if extras:
+        try:
+            extra["voxelizer"] = voxelizer_extra(capi, tri)
+        except Exception as e:  # a measurement, not the benchmark: record why it is missing
+            extra["voxelizer"] = {"error": str(e)}
     if extras and args.Q == 19:
         extra["d3q27"] = d3q27_extra(capi, cr, mask, surf, tri, origin, local, flush, args.steps)
     if extras and not args.no_precision:
