@@ -937,9 +937,6 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
     node_finish<Q, S, MODE, KIND, WIDE>(P, a, word, pl.s, pl.lng, pl.c, pl.miss, g, pl.nr, pl.slot, part);
 }
 
-// WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
-// lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
-// One thread per active node.
 // Programmatic dependent launch: a step kernel is launched with
 // programmatic stream serialization, so it may start while the previous
 // kernel of the stream finishes.  Each block reads its read-only node data,
@@ -954,6 +951,9 @@ __device__ __forceinline__ void node_update(const StepParams& P, const int64_t a
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// WIDE = false: population offsets q * stride + a in 32-bit arithmetic, for
+// lattices with Q * stride < 2^31 (the launcher checks); WIDE = true: 64-bit.
+// One thread per active node.
 template <int Q, typename S, int MODE, int KIND, int BT = kStepThreads, int MINB = 1, bool WIDE = true,
           bool WALLS = false>
 __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
