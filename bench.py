@@ -573,8 +573,8 @@ def read_traffic(name):
     return None
 
 
-def cpu_baseline(tri, mask, bb, planes, cores, seconds=12.0, mode=None):
-    """The CPU oracle (FP64) on this host: as many C2 steps as fit in ~seconds."""
+def cpu_sim(mask, bb, planes, mode=None):
+    """The CPU oracle (FP64, the reference's algorithm) on the C2 lattice."""
     from oracle import oracle as O
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import classify
@@ -586,14 +586,26 @@ def cpu_baseline(tri, mask, bb, planes, cores, seconds=12.0, mode=None):
            dict(kind=O.BC_PRESSURE, face=5, plane=kout, value=1.0)]
     sim = O.Sim(19, O.PARITY if mode is None else mode, cls, (bb[0], bb[2], bb[4]), 1.0, TAU, bcs)
     sim.set_amplitude(waveform.sinusoid_table(U_MEAN, PERIOD))
-    sim.step(1, cores)  # warm-up (page-in)
+    return sim
+
+
+def cpu_sample(sim, cores, seconds, max_steps=200):
+    """As many full-lattice steps as fit in ~seconds (at least one):
+    (steps, seconds)."""
     n, t0 = 0, time.perf_counter()
     while True:
         sim.step(1, cores)
         n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or n >= 200:
-            break
+        if el >= seconds or n >= max_steps:
+            return n, el
+
+
+def cpu_baseline(tri, mask, bb, planes, cores, seconds=12.0, mode=None):
+    """The CPU oracle (FP64) on this host: as many C2 steps as fit in ~seconds."""
+    sim = cpu_sim(mask, bb, planes, mode)
+    sim.step(1, cores)  # warm-up (page-in)
+    n, el = cpu_sample(sim, cores, seconds)
     return sim.nactive * n / el / 1e6, n, el, sim.nactive
 
 
@@ -815,27 +827,33 @@ def run_reference(args):
     fl = np.argwhere(mask > 0)
     planes = (int(fl[:, 0].min()), int(fl[:, 0].max()))
     cores = os.cpu_count() or 1
-    per = []
-    na = 0
+    # one lattice; each of the W warm-up and K timed "steps" is a bounded
+    # sample of full-lattice LBM steps, sized so that the K samples take
+    # about --cpu-seconds together
+    sim = cpu_sim(mask, bb, planes)
+    na = sim.nactive
+    per_sample = max(0.05, args.cpu_seconds / args.steps)
     for _ in range(args.warmup):
-        cpu_baseline(tri, mask, bb, planes, cores, seconds=0.5)
+        cpu_sample(sim, cores, per_sample, max_steps=1)
     total_n, total_t = 0, 0.0
-    for _ in range(max(1, min(args.steps, 3))):
-        v, n, el, na = cpu_baseline(tri, mask, bb, planes, cores, seconds=args.cpu_seconds / 3)
-        per.append(v)
+    for _ in range(args.steps):
+        n, el = cpu_sample(sim, cores, per_sample)
         total_n += n
         total_t += el
     value = na * total_n / total_t / 1e6
     out = {
         "impl": "reference", "metric": "MLUPS (D3Q19 BGK lattice updates per second, active nodes)",
-        "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": total_n, "warmup": args.warmup,
-        "ms_per_step": 1e3 * total_t / total_n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded Y-bifurcation STL generated in-process)",
         "config": {"workload": "Y-bifurcation 256x192x512, parent r=24, daughters r=17 at +/-30 deg, seed 0",
                    "lattice": "D3Q19", "storage": "f64", "tau": TAU, "active_nodes": na,
-                   "implementation": "reference algorithm restated in C (oracle/lbm_oracle.c), parity semantics"},
+                   "implementation": "reference algorithm restated in C (oracle/lbm_oracle.c), parity semantics",
+                   "step": f"one bounded sample of full-lattice LBM steps (~{per_sample:.2f} s)",
+                   "lbm_steps_timed": total_n, "ms_per_lbm_step": 1e3 * total_t / total_n},
         "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port",
-                         "sample": f"{total_n} full-lattice FP64 steps in {total_t:.1f} s on {cores} threads"},
+                         "sample": f"{total_n} full-lattice FP64 steps in {total_t:.1f} s on {cores} threads, "
+                                   f"{args.steps} samples"},
         "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
