@@ -10,6 +10,8 @@
 //   pv_preset 1        (the reference's PV.stl inlet / outlet coordinates)
 //   write_output 0|1   write_vertices 0|1 (WSS / OSI / TAWSS at the STL's vertices)
 //   interpolated_walls 1 (physics mode: Bouzidi bounce-back from the STL's wall distances)
+//   graph_steps <n>    (even: steps replayed from one captured CUDA graph; 0 = direct launches)
+//   persistent_steps <k> (even: steps per persistent launch, a divisor of graph_steps; 0 = off)
 //   inlet_face <f> inlet_plane <p>  outlet_face <f> outlet_plane <p>
 // Defaults reproduce the reference: FP64, parity semantics, D3Q19.
 #include <chrono>
@@ -68,6 +70,12 @@ int main(int argc, char** argv) {
         sim.write_output = num("write_output", 1) != 0;
         sim.write_vertices = num("write_vertices", 0) != 0;
         if (num("interpolated_walls", 0) != 0) sim.UseInterpolatedWalls(true);
+        auto ck = [&](lbm_status rc, const char* what) {
+            if (rc != LBM_OK) throw std::runtime_error(std::string(what) + ": " + lbm_last_error(sim.handle()));
+        };
+        if (sv.count("persistent_steps"))
+            ck(lbm_set_persistent(sim.handle(), (int)num("persistent_steps", 0)), "persistent_steps");
+        if (sv.count("graph_steps")) ck(lbm_set_graph_steps(sim.handle(), (int)num("graph_steps", 0)), "graph_steps");
         lbm_counts c{};
         if (lbm_get_counts(sim.handle(), &c) != LBM_OK) throw std::runtime_error("lbm_get_counts failed");
         const auto t2 = clk::now();
