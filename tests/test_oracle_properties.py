@@ -1,0 +1,82 @@
+"""Properties of the oracle's physics mode that hold at any size.  The
+reference has parity semantics only, so its golden fixtures pin the
+oracle's parity mode; these pin the physics mode's streaming, half-way
+bounce-back and collisions (BGK and regularized, D3Q19 and D3Q27): a
+closed vessel conserves mass to round-off from any state, the rest state
+is a fixed point, and a mirror-symmetric vessel with a mirror-symmetric
+state stays mirror-symmetric."""
+import numpy as np
+import pytest
+
+
+def _vessel(shape=(14, 11, 9)):
+    """A closed ellipsoidal cavity, cls[k, j, i] (1 fluid, 0 solid),
+    symmetric under i -> nx - 1 - i."""
+    nz, ny, nx = shape
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    cz, cy, cx = (nz - 1) / 2, (ny - 1) / 2 + 0.3, (nx - 1) / 2
+    r = ((k - cz) / (0.45 * nz)) ** 2 + ((j - cy) / (0.42 * ny)) ** 2 + ((i - cx) / (0.44 * nx)) ** 2
+    return (r < 1.0).astype(np.uint8)
+
+
+def _sim(O, Q, regularized, cls, tau=0.7):
+    s = O.Sim(Q, O.PHYSICS, cls, (0.0, 0.0, 0.0), 1.0, tau, [])
+    s.set_collision(regularized)
+    return s
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+@pytest.mark.parametrize("regularized", [False, True])
+def test_closed_vessel_conserves_mass(oracle_lib, Q, regularized):
+    O = oracle_lib
+    s = _sim(O, Q, regularized, _vessel())
+    f, _, _ = s.f()
+    rng = np.random.default_rng(Q + 10 * regularized)
+    s.set_f(f * (1.0 + 0.02 * rng.uniform(-1.0, 1.0, size=f.shape)))
+    m0, _, _ = s.conservation()
+    s.step(60)
+    m1, _, _ = s.conservation()
+    assert abs(m1 - m0) <= 1e-12 * abs(m0), (m0, m1)
+    rho, u = s.macro()
+    assert np.all(np.isfinite(rho)) and np.abs(u).max() < 0.1
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+@pytest.mark.parametrize("regularized", [False, True])
+def test_rest_state_is_a_fixed_point(oracle_lib, Q, regularized):
+    O = oracle_lib
+    s = _sim(O, Q, regularized, _vessel())
+    f0, _, _ = s.f()
+    s.step(25)
+    f1, _, _ = s.f()
+    assert np.abs(f1 - f0).max() <= 1e-15
+    _, u = s.macro()
+    assert np.abs(u).max() <= 1e-15
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+def test_mirror_symmetry_is_kept(oracle_lib, Q):
+    """Mirror i -> nx - 1 - i maps population q to the one with c_x negated;
+    a state built symmetric stays symmetric (to round-off) in a symmetric
+    cavity."""
+    O = oracle_lib
+    cls = _vessel()
+    assert np.array_equal(cls, cls[:, :, ::-1])
+    s = _sim(O, Q, False, cls)
+    c, _, _ = O.lattice(Q)
+    c = np.asarray(c)
+    mirror_q = np.array([int(np.where((c[:, 0] == -c[q, 0]) & (c[:, 1] == c[q, 1]) & (c[:, 2] == c[q, 2]))[0][0])
+                         for q in range(Q)])
+    pt, _ = s.active()
+    nz, ny, nx = cls.shape
+    i, j, k = pt % nx, (pt // nx) % ny, pt // (nx * ny)
+    index = {int(p): a for a, p in enumerate(pt)}
+    partner = np.array([index[int((kk * ny + jj) * nx + (nx - 1 - ii))] for ii, jj, kk in zip(i, j, k)])
+    f, _, _ = s.f()
+    rng = np.random.default_rng(Q)
+    g = f * (1.0 + 0.02 * rng.uniform(-1.0, 1.0, size=f.shape))
+    g = 0.5 * (g + g[partner][:, mirror_q])  # symmetrise
+    s.set_f(g)
+    s.step(40)
+    h, _, _ = s.f()
+    assert np.abs(h - h[partner][:, mirror_q]).max() <= 1e-14
