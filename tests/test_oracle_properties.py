@@ -3,10 +3,14 @@ reference has parity semantics only, so its golden fixtures pin the
 oracle's parity mode; these pin the physics mode's streaming, half-way
 bounce-back and collisions (BGK and regularized, D3Q19 and D3Q27): a
 closed vessel conserves mass to round-off from any state, the rest state
-is a fixed point, and a mirror-symmetric vessel with a mirror-symmetric
-state stays mirror-symmetric."""
+is a fixed point, a mirror-symmetric vessel with a mirror-symmetric
+state stays mirror-symmetric, Zou-He rules impose exactly the prescribed
+inlet profile and outlet density, and a steady tube carries the same mass
+flux through every cross-section."""
 import numpy as np
 import pytest
+
+from helpers import classify
 
 
 def _vessel(shape=(14, 11, 9)):
@@ -80,3 +84,54 @@ def test_mirror_symmetry_is_kept(oracle_lib, Q):
     s.step(40)
     h, _, _ = s.f()
     assert np.abs(h - h[partner][:, mirror_q]).max() <= 1e-14
+
+
+def _tube(O, Q, regularized, u_in=0.02, tau=0.8):
+    """Capped z tube (radius 4.3 in a 12 x 12 section, 38 planes), parabolic
+    velocity inlet on its first fluid plane, density 1 outlet on its last."""
+    nz, ny, nx = 40, 12, 12
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    mask = (((i - 5.5) ** 2 + (j - 5.5) ** 2) < 4.3 ** 2).astype(np.uint8)
+    mask[0] = 0
+    mask[-1] = 0
+    fl = np.argwhere(mask > 0)
+    kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
+    cls = classify(mask, [(2, kin), (2, kout)])
+    bcs = [dict(kind=O.BC_VELOCITY, face=4, plane=kin, value=1.0, profile=1, c1=5.5, c2=5.5, R=4.3),
+           dict(kind=O.BC_PRESSURE, face=5, plane=kout, value=1.0)]
+    s = O.Sim(Q, O.PHYSICS, cls, (0.0, 0.0, 0.0), 1.0, tau, bcs)
+    s.set_collision(regularized)
+    s.set_amplitude([u_in])
+    return s, (nx, ny), (kin, kout)
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+@pytest.mark.parametrize("regularized", [False, True])
+def test_zou_he_imposes_inlet_profile_and_outlet_density(oracle_lib, Q, regularized):
+    O = oracle_lib
+    s, (nx, ny), (kin, kout) = _tube(O, Q, regularized)
+    s.step(300)
+    pt, c = s.active()
+    k, j, i = pt // (nx * ny), (pt // nx) % ny, pt % nx
+    rho, u = s.macro()
+    inlet = (c >= 3) & (k == kin)
+    outlet = (c >= 3) & (k == kout)
+    assert inlet.sum() > 40 and outlet.sum() > 40
+    want = 0.02 * (1.0 - ((i[inlet] - 5.5) ** 2 + (j[inlet] - 5.5) ** 2) / 4.3 ** 2)
+    assert np.abs(u[inlet, 2] - want).max() <= 1e-15
+    assert np.abs(u[inlet, :2]).max() <= 1e-15
+    assert np.abs(rho[outlet] - 1.0).max() <= 1e-15
+
+
+def test_steady_tube_carries_one_mass_flux(oracle_lib):
+    """After the start-up transient has decayed, sum(rho u_z) over each
+    cross-section agrees along the tube (0.23% apart after 2000 steps,
+    0.03% after 16000)."""
+    O = oracle_lib
+    s, (nx, ny), (kin, kout) = _tube(O, 19, False)
+    s.step(12000)
+    pt, _ = s.active()
+    k = pt // (nx * ny)
+    rho, u = s.macro()
+    flux = np.array([(rho[k == z] * u[k == z, 2]).sum() for z in range(kin, kout + 1)])
+    assert (flux.max() - flux.min()) / flux.mean() < 1e-3, flux
