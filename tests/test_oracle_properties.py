@@ -5,8 +5,9 @@ bounce-back and collisions (BGK and regularized, D3Q19 and D3Q27): a
 closed vessel conserves mass to round-off from any state, the rest state
 is a fixed point, a mirror-symmetric vessel with a mirror-symmetric
 state stays mirror-symmetric, Zou-He rules impose exactly the prescribed
-inlet profile and outlet density, and a steady tube carries the same mass
-flux through every cross-section."""
+inlet profile and outlet density, a steady tube carries the same mass
+flux through every cross-section, and interpolated (Bouzidi) bounce-back
+with every wall half a spacing away is half-way bounce-back bit for bit."""
 import numpy as np
 import pytest
 
@@ -135,3 +136,44 @@ def test_steady_tube_carries_one_mass_flux(oracle_lib):
     rho, u = s.macro()
     flux = np.array([(rho[k == z] * u[k == z, 2]).sum() for z in range(kin, kout + 1)])
     assert (flux.max() - flux.min()) / flux.mean() < 1e-3, flux
+
+
+def _box_triangles(lo, hi):
+    """The 12 outward-facing triangles of an axis-aligned box, tri12 rows
+    (three vertices, then the unit normal)."""
+    (x0, y0, z0), (x1, y1, z1) = lo, hi
+    v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], np.float64)
+    faces = [(0, 2, 1), (0, 3, 2), (4, 5, 6), (4, 6, 7), (0, 1, 5), (0, 5, 4),
+             (3, 7, 6), (3, 6, 2), (0, 4, 7), (0, 7, 3), (1, 2, 6), (1, 6, 5)]
+    rows = []
+    for a, b, c in faces:
+        n = np.cross(v[b] - v[a], v[c] - v[a])
+        rows.append(np.concatenate([v[a], v[b], v[c], n / np.linalg.norm(n)]))
+    return np.array(rows)
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+def test_interpolated_walls_at_half_spacing_are_half_way(oracle_lib, Q):
+    """A box cavity whose walls lie half a spacing outside its outer nodes:
+    every missing link has q = 1/2 and the Bouzidi rule reduces to half-way
+    bounce-back exactly; walls a quarter spacing away change the flow."""
+    O = oracle_lib
+    nz, ny, nx = 9, 8, 7
+    cls = np.zeros((nz + 2, ny + 2, nx + 2), np.uint8)
+    cls[1:-1, 1:-1, 1:-1] = 1
+    half = O.Sim(Q, O.PHYSICS, cls, (0.0, 0.0, 0.0), 1.0, 0.7, [])
+    bouzidi = O.Sim(Q, O.PHYSICS, cls, (0.0, 0.0, 0.0), 1.0, 0.7, [])
+    bouzidi.set_wall_distances(_box_triangles((0.5, 0.5, 0.5), (nx + 0.5, ny + 0.5, nz + 0.5)))
+    assert np.array_equal(np.unique(bouzidi.wall_distances()), [0.5])
+    quarter = O.Sim(Q, O.PHYSICS, cls, (0.0, 0.0, 0.0), 1.0, 0.7, [])
+    quarter.set_wall_distances(_box_triangles((0.75, 0.75, 0.75), (nx + 0.25, ny + 0.25, nz + 0.25)))
+    assert 0.25 in np.unique(quarter.wall_distances())
+    f, _, _ = half.f()
+    g = f * (1.0 + 0.02 * np.random.default_rng(Q).uniform(-1.0, 1.0, size=f.shape))
+    for s in (half, bouzidi, quarter):
+        s.set_f(g)
+        s.step(30)
+    fh, fb, fq = half.f()[0], bouzidi.f()[0], quarter.f()[0]
+    assert np.array_equal(fh, fb)
+    assert np.abs(fq - fh).max() > 1e-6
