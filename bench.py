@@ -19,7 +19,15 @@ With --gpus N > 1 (launched by torchrun) every rank advances an independent
 replica of the lattice (the single-domain solver has no inter-GPU exchange);
 value = total lattice updates of all ranks / max rank time.
 --impl reference times the CPU oracle (the reference's algorithm restated in
-C, FP64, parity semantics) on this host's cores on a bounded sample.
+C, FP64, parity semantics) on this host's cores, each of its K steps a
+bounded sample of full-lattice steps.
+
+At N = 1 the line's "extra" object adds secondary measurements (skipped by
+--quick or their --no-* flags): FP16 storage, D3Q27, the voxelizer's ray
+tests per second, the 384x288x768 precision comparison against an FP64 run,
+three inlet periods of the bifurcation, the 64-vessel packed ensemble, the
+learned warm start, and (with --small-ensembles) launch-bound lattices
+stepped one launch per step vs persistent launches.
 """
 from __future__ import annotations
 
