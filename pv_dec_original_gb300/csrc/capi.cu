@@ -385,23 +385,28 @@ int one_step(lbm_handle* h) {
     return LBM_OK;
 }
 
-// One persistent launch of h->persist (even) steps: cur and the counter
-// parity come back to where they were.
-int multi_steps(lbm_handle* h) {
-    const int n = h->persist;
+// A persistent launch of n (even) steps from the current state (n = 0:
+// only the kernel's occupancy query); cur and the counter parity are left
+// as they were.
+cudaError_t multi_launch(lbm_handle* h, int n) {
     const StepParams even = make_params(h, 0);
     h->cur = 1 - h->cur;
     h->steps++;
     const StepParams odd = make_params(h, 0);
     h->cur = 1 - h->cur;
     h->steps--;
-    cudaError_t e;
     switch (h->d.precision) {
-        case LBM_F64: e = launch_multi_f64(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
-        case LBM_F32: e = launch_multi_f32(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
-        case LBM_F16: e = launch_multi_f16(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
-        default: e = launch_multi_bf16(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st); break;
+        case LBM_F64: return launch_multi_f64(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st);
+        case LBM_F32: return launch_multi_f32(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st);
+        case LBM_F16: return launch_multi_f16(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st);
+        default: return launch_multi_bf16(h->d.Q, h->d.mode, even, odd, n, h->bar, h->st);
     }
+}
+
+// One persistent launch of h->persist steps.
+int multi_steps(lbm_handle* h) {
+    const int n = h->persist;
+    const cudaError_t e = multi_launch(h, n);
     if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, std::string("persistent step launch: ") + cudaGetErrorString(e));
     h->launches++;
     h->steps += n;
@@ -417,6 +422,9 @@ int build_graph(lbm_handle* h) {
     const int64_t steps0 = h->steps, since0 = h->since_start, launches0 = h->launches;
     const int cur0 = h->cur;
     cudaGraph_t graph = nullptr;
+    // the persistent kernel's occupancy query runs here, outside the capture
+    // (an error resurfaces at the captured launch)
+    if (h->persist > 0 && multi_launch(h, 0) != cudaSuccess) (void)cudaGetLastError();
     CK(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < h->graph_steps;) {
         if (h->persist > 0) {

@@ -133,7 +133,8 @@ cudaError_t launch_step_f32(int Q, int mode, int kind, int variant, const StepPa
 cudaError_t launch_step_f16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 cudaError_t launch_step_bf16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 // Persistent launch of nsteps steps (even / odd step parameters, grid
-// barrier word bar[2], zero between launches); 32-bit population offsets.
+// barrier word bar[2], zero between launches; nsteps = 0: the kernel's
+// occupancy query only); 32-bit population offsets.
 cudaError_t launch_multi_f64(int Q, int mode, const StepParams& even, const StepParams& odd, int nsteps,
                              unsigned* bar, cudaStream_t s);
 cudaError_t launch_multi_f32(int Q, int mode, const StepParams& even, const StepParams& odd, int nsteps,

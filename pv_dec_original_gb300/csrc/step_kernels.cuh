@@ -1187,6 +1187,7 @@ cudaError_t launch_multi_t(const StepPair& pp, int nsteps, unsigned* bar, cudaSt
         sms = n;
         per_sm = v;
     }
+    if (nsteps == 0) return cudaSuccess;  // the occupancy query alone (before a stream capture)
     const StepParams& p = pp.p[0];
     const int64_t work = p.nact > p.nnw ? p.nact : p.nnw;
     const int64_t need = ceil_div(work, kMultiThreads);
@@ -1205,11 +1206,13 @@ cudaError_t launch_multi_t(const StepPair& pp, int nsteps, unsigned* bar, cudaSt
     return cudaLaunchKernelEx(&cfg, kern, pp, nsteps, bar);
 }
 
-// nsteps steps in one launch; lattices with 32-bit population offsets only.
+// nsteps steps in one launch (0: only the kernel's occupancy query, which
+// is then done outside any stream capture); lattices with 32-bit
+// population offsets only.
 template <typename S>
 cudaError_t launch_multi_typed(int Q, int mode, const StepParams& even, const StepParams& odd, int nsteps,
                                unsigned* bar, cudaStream_t st) {
-    if ((int64_t)Q * even.stride >= ((int64_t)1 << 31) || nsteps < 1) return cudaErrorInvalidValue;
+    if ((int64_t)Q * even.stride >= ((int64_t)1 << 31) || nsteps < 0) return cudaErrorInvalidValue;
     if (even.nact <= 0) return cudaSuccess;
     StepPair pp{};
     pp.p[0] = even;
