@@ -51,6 +51,7 @@ BYTES_PER_LU = {(19, "f32"): 152, (19, "f16"): 76, (19, "bf16"): 76, (19, "f64")
                 (27, "f32"): 216, (27, "f16"): 108, (27, "bf16"): 108, (27, "f64"): 432}
 L2_FLUSH_BYTES = 512 << 20
 L2_READ_BYTES = 256 << 20
+E2E_BATCHES = 20  # timed end-to-end batches of 100 steps (2000 LBM steps), whatever --steps is
 TAU = 0.55
 U_MEAN = 0.03
 PERIOD = 4000.0
@@ -171,22 +172,9 @@ def c2_workload():
     return surf, surf.tri12()
 
 
-def c2_bcs(capi, surf, mask):
-    fl = np.argwhere(mask > 0)  # (k, j, i)
-    kin, kout = int(fl[:, 0].min()), int(fl[:, 0].max())
-    cx, cy = surf.meta["center"]
-    return [capi.bc_spec(capi.LBM_BC_VELOCITY, "z-", kin, 1.0, 1, cx, cy, surf.meta["parent_radius"]),
-            capi.bc_spec(capi.LBM_BC_PRESSURE, "z+", kout, 1.0)], (kin, kout)
-
-
 def make_solver(capi, mask, surf, tri, Q, prec, origin, device, collision=0):
-    from pv_dec_original_gb300 import waveform
-    s = capi.Solver(Q, prec, capi.LBM_PHYSICS, TAU, 1.0, origin, 1.0, PERIOD, device, collision=collision)
-    bcs, planes = c2_bcs(capi, surf, mask)
-    s.set_geometry(mask, bcs)
-    s.set_normals(tri)
-    s.set_inlet_table(waveform.sinusoid_table(U_MEAN, PERIOD))
-    return s, planes
+    from pv_dec_original_gb300 import workloads as W
+    return W.bifurcation_solver(capi, mask, surf, tri, Q, prec, origin, device, collision)
 
 
 class L2Flush:
@@ -301,10 +289,19 @@ def periods_extra(capi, mask, surf, tri, origin, device, periods=3):
     fl = np.argwhere(mask > 0)
     steps = int(periods * PERIOD)
     res, ref = {}, None
-    for prec in ("f64", "f32", "f16", "bf16"):
+    # "f64_1ulp": FP64 from an initial state moved by one ulp per value
+    # (random sign, seeded): the flow's own amplification of a rounding-size
+    # difference, the yardstick of the other formats' errors
+    for name in ("f64", "f64_1ulp", "f32", "f16", "bf16"):
+        prec = "f64" if name.startswith("f64") else name
         t0 = time.perf_counter()
         s, (kin, kout) = make_solver(capi, mask, surf, tri, 19, prec, origin, device,
                                      collision=capi.LBM_COLLISION_REGULARIZED)
+        if name == "f64_1ulp":
+            f0 = s.distributions()
+            rng = np.random.default_rng(7)
+            s.set_distributions(np.where(rng.random(f0.shape) < 0.5, np.nextafter(f0, -np.inf),
+                                         np.nextafter(f0, np.inf)))
         s.set_graph_steps(100)
         s.step(steps)
         rho, u = s.macro()
@@ -317,10 +314,12 @@ def periods_extra(capi, mask, surf, tri, origin, device, periods=3):
             row["u_l2_rel"] = float(np.linalg.norm(u - ref[0]) / np.linalg.norm(ref[0]))
             row["pressure_drop_rel"] = float(abs(drop - ref[1]) / abs(ref[1]))
             row["tawss_l2_rel"] = float(np.linalg.norm(tawss - ref[2]) / np.linalg.norm(ref[2]))
-        res[prec] = row
+        res[name] = row
         s.close()
     return {"lattice": [256, 192, 512], "steps": steps, "periods": periods, "tau": TAU,
-            "collision": "regularized", "reference": "FP64 run of the same case on the GPU", "formats": res}
+            "collision": "regularized", "reference": "FP64 run of the same case on the GPU",
+            "f64_1ulp": "FP64 started from the initial state moved by one ulp per value (random sign)",
+            "formats": res}
 
 
 def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
@@ -582,7 +581,10 @@ def read_traffic(name):
 
 
 def cpu_sim(mask, bb, planes, mode=None):
-    """The CPU oracle (FP64, the reference's algorithm) on the C2 lattice."""
+    """The CPU oracle (FP64, the reference's algorithm) on the C2 lattice
+    with the GPU arm's boundary rules; mode None: physics semantics (the GPU
+    arm's: half-way bounce-back, stress of the same time level), else the
+    oracle's PARITY / PHYSICS constant."""
     from oracle import oracle as O
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import classify
@@ -592,7 +594,7 @@ def cpu_sim(mask, bb, planes, mode=None):
     surf_c = (0.5 * 255 + 0.213, 0.5 * 191 + 0.087)
     bcs = [dict(kind=O.BC_VELOCITY, face=4, plane=kin, value=1.0, profile=1, c1=surf_c[0], c2=surf_c[1], R=24.0),
            dict(kind=O.BC_PRESSURE, face=5, plane=kout, value=1.0)]
-    sim = O.Sim(19, O.PARITY if mode is None else mode, cls, (bb[0], bb[2], bb[4]), 1.0, TAU, bcs)
+    sim = O.Sim(19, O.PHYSICS if mode is None else mode, cls, (bb[0], bb[2], bb[4]), 1.0, TAU, bcs)
     sim.set_amplitude(waveform.sinusoid_table(U_MEAN, PERIOD))
     return sim
 
@@ -746,7 +748,7 @@ def run_ours(args):
     s.set_graph_steps(B)
     L = capi.load()
     P = lambda a: a.ctypes.data_as(C.c_void_p)
-    nb = max(2, min(5, args.steps // 10))
+    nb = E2E_BATCHES
 
     def e2e_batch(k):
         s0 = k * B + s_base
@@ -780,8 +782,9 @@ def run_ours(args):
                 cores = os.cpu_count() or 1
                 v, n, el, na = cpu_baseline(tri, mask, bb, planes, cores, seconds=args.cpu_seconds)
                 cpu = {"value": v, "unit": "MLUPS", "cores": cores, "kind": "port",
-                       "sample": f"{n} FP64 parity steps of the full 256x192x512 lattice ({na} active nodes), "
-                                 f"{el:.1f} s, OpenMP on {cores} host threads, normals not computed"}
+                       "sample": f"{n} FP64 steps of the full 256x192x512 lattice ({na} active nodes) in the "
+                                 f"GPU arm's semantics (physics mode, same boundary rules), {el:.1f} s, OpenMP on "
+                                 f"{cores} host threads, normals not computed"}
             except Exception as e:  # the baseline is reported, never required
                 cpu = {"value": None, "unit": "MLUPS", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
         out = {
@@ -837,28 +840,45 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     # one lattice; each of the W warm-up and K timed "steps" is a bounded
     # sample of full-lattice LBM steps, sized so that the K samples take
-    # about --cpu-seconds together
-    sim = cpu_sim(mask, bb, planes)
-    na = sim.nactive
+    # about --cpu-seconds together.  The timed semantics are the GPU arm's
+    # (physics mode: half-way bounce-back, stress of the same time level,
+    # the same Zou-He rules); the reference's own semantics (parity mode:
+    # push streaming, its wall rule, time-lagged stress) are timed after it
+    # as a second, labelled number.
     per_sample = max(0.05, args.cpu_seconds / args.steps)
-    for _ in range(args.warmup):
-        cpu_sample(sim, cores, per_sample, max_steps=1)
-    total_n, total_t = 0, 0.0
-    for _ in range(args.steps):
-        n, el = cpu_sample(sim, cores, per_sample)
-        total_n += n
-        total_t += el
+
+    def timed(mode, samples):
+        sim = cpu_sim(mask, bb, planes, mode)
+        for _ in range(args.warmup):
+            cpu_sample(sim, cores, per_sample, max_steps=1)
+        tn, tt = 0, 0.0
+        for _ in range(samples):
+            n, el = cpu_sample(sim, cores, per_sample)
+            tn += n
+            tt += el
+        return sim.nactive, tn, tt
+
+    na, total_n, total_t = timed(O.PHYSICS, args.steps)
     value = na * total_n / total_t / 1e6
+    _, pn, pt = timed(O.PARITY, max(1, args.steps // 4))
     out = {
         "impl": "reference", "metric": "MLUPS (D3Q19 BGK lattice updates per second, active nodes)",
         "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded Y-bifurcation STL generated in-process)",
         "config": {"workload": "Y-bifurcation 256x192x512, parent r=24, daughters r=17 at +/-30 deg, seed 0",
-                   "lattice": "D3Q19", "storage": "f64", "tau": TAU, "active_nodes": na,
-                   "implementation": "reference algorithm restated in C (oracle/lbm_oracle.c), parity semantics",
+                   "lattice": "D3Q19", "storage": "f64", "tau": TAU,
+                   "inlet": "z-min Zou-He velocity, parabolic, u=0.03(1+0.5sin(2pi t/4000)+0.2sin(4pi t/4000))",
+                   "outlet": "z-max Zou-He density 1", "walls": "half-way bounce-back",
+                   "active_nodes": na,
+                   "implementation": "reference algorithm restated in C (oracle/lbm_oracle.c), physics semantics "
+                                     "(the GPU arm's)",
                    "step": f"one bounded sample of full-lattice LBM steps (~{per_sample:.2f} s)",
                    "lbm_steps_timed": total_n, "ms_per_lbm_step": 1e3 * total_t / total_n},
+        "parity_semantics": {"value": na * pn / pt / 1e6, "unit": "MLUPS", "lbm_steps_timed": pn,
+                             "seconds": pt,
+                             "what": "the same lattice in the reference's own semantics (push streaming, its "
+                                     "in-place wall rule, time-lagged stress), FP64, same threads"},
         "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port",
                          "sample": f"{total_n} full-lattice FP64 steps in {total_t:.1f} s on {cores} threads, "
                                    f"{args.steps} samples"},

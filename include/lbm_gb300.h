@@ -53,8 +53,8 @@ typedef int lbm_status;
  * LBM_PARITY reproduces the reference step exactly (Simulation.cpp:569-601):
  *   collision on every non-solid node; push streaming that keeps a
  *   destination's previous value when the link comes from solid or the
- *   post-collision value is exactly zero (Simulation.cpp:264-290); Zou-He
- *   formulas of Boundary.cpp:157-185 and Simulation.cpp:628-838; the in-place
+ *   post-collision value is exactly zero (Simulation.cpp:211-237); Zou-He
+ *   formulas of Boundary.cpp:129-157 and Simulation.cpp:628-838; the in-place
  *   wall rule of Simulation.cpp:843-863; wall shear stress from the
  *   post-boundary f and the same step's equilibrium, without the
  *   (1 - 1/2tau) factor (Simulation.cpp:880-898).
@@ -129,7 +129,7 @@ typedef struct {
     double wss_scale;  /* C of the wall shear stress (reference: 1060*dt^2/(s^2*1e-6)) */
     double tawss_div;  /* TAWSS = accumulated |tau| / tawss_div (reference: 0.9) */
     int device;        /* CUDA device ordinal */
-    /* Physics mode: LBM_COLLISION_BGK (the reference's, Simulation.cpp:96-261)
+    /* Physics mode: LBM_COLLISION_BGK (the reference's, Simulation.cpp:43-208)
      * or LBM_COLLISION_REGULARIZED (no reference counterpart: the
      * non-equilibrium part is projected on its second moment before
      * relaxing, which keeps flows stable at tau near 1/2 where BGK diverges).
@@ -208,7 +208,7 @@ lbm_status lbm_set_inlet_table(lbm_handle* h, const double* amp, int64_t n);
 lbm_status lbm_set_waveform(lbm_handle* h, int wave, const double* amp, int64_t n);
 
 /* f = w_i, accumulators cleared, step counter 0 (Node.cpp:30-37,
- * Simulation.cpp:85-91). */
+ * Simulation.cpp:32-38). */
 lbm_status lbm_init_equilibrium(lbm_handle* h);
 /* f = f_eq(rho, u) + regularised non-equilibrium part (regularized != 0) or
  * f_eq only; rho and u (3 per node) per active node, FP32. */
@@ -253,7 +253,7 @@ lbm_status lbm_get_classes(lbm_handle* h, uint8_t* cls);
 lbm_status lbm_get_distributions(lbm_handle* h, double* f);
 lbm_status lbm_set_distributions(lbm_handle* h, const double* f);
 /* rho and u of the post-boundary distributions per active node
- * (Collision's moment formulas, Simulation.cpp:105-158). */
+ * (Collision's moment formulas, Simulation.cpp:52-175). */
 lbm_status lbm_get_macro(lbm_handle* h, double* rho, double* u3);
 /* Next-to-wall nodes in increasing n (Simulation.cpp:880-905). Any pointer
  * may be NULL. */
@@ -308,7 +308,7 @@ lbm_status lbm_set_graph_steps(lbm_handle* h, int steps_per_graph);
  * Each barrier wait is bounded (~0.25 s): a wait that gives up ends the
  * launch and the next lbm_step / lbm_check_status returns LBM_ERR_CUDA.
  * New interface: the reference has one host loop iteration per step
- * (Simulation.cpp:560-597). */
+ * (Simulation.cpp:575-599). */
 lbm_status lbm_set_persistent(lbm_handle* h, int steps_per_launch);
 /* Testing the bounded barrier: extra arrivals every barrier of the next
  * persistent launches waits for (0 in normal use).  A count far above any

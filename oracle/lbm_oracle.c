@@ -15,9 +15,9 @@
  *   Subdomain.cpp:173-218              Connectivity, IdentifyNextToWallLattices
  *   Subdomain.cpp:224-370              calculateBoundaryNormals
  *   Node.cpp:30-37                     Initialize (f = w, fnew = 0)
- *   Simulation.cpp:96-261              Collision
- *   Simulation.cpp:264-290             Streaming (push, zero skip)
- *   Boundary.cpp:157-185               ApplyBc (Zou-He velocity, x-min)
+ *   Simulation.cpp:43-208              Collision
+ *   Simulation.cpp:211-237             Streaming (push, zero skip)
+ *   Boundary.cpp:129-157               ApplyBc (Zou-He velocity, x-min)
  *   Simulation.cpp:628-838             ApplyOutletBc (y-max, z-min)
  *   Simulation.cpp:843-863             ApplyWallBc
  *   Simulation.cpp:880-905             ComputeWallShearStress, ComputeOSIAndTAWSS
@@ -332,6 +332,7 @@ struct oracle_sim {
     uint8_t* cls;      /* active -> class */
     int32_t* nbr;      /* active*Q -> active index of x + c_q, or -1 */
     double *f, *fnew, *feq, *rho, *u;
+    double* pulled;    /* physics mode: the pull's output, swapped with f after each step */
     double* prof;      /* active -> inlet profile factor */
     int64_t *nw, *wall;  /* active indices */
     double *nw_n, *wall_n, *wss, *acc, *accm, *osi, *tawss;
@@ -446,7 +447,7 @@ void oracle_sim_destroy(oracle_sim* s) {
     free(s->pt); free(s->cls); free(s->nbr); free(s->f); free(s->fnew); free(s->feq);
     free(s->rho); free(s->u); free(s->prof); free(s->nw); free(s->wall); free(s->nw_n);
     free(s->wall_n); free(s->wss); free(s->acc); free(s->accm); free(s->osi); free(s->tawss);
-    free(s->amp); free(s->wq); free(s);
+    free(s->amp); free(s->wq); free(s->pulled); free(s);
 }
 
 void oracle_sim_set_amplitude(oracle_sim* s, const double* amp, int64_t n) {
@@ -507,7 +508,8 @@ void oracle_sim_compute_normals(oracle_sim* s, const double* tri, int64_t ntri, 
     }
 }
 
-/* Collision (Simulation.cpp:96-261) for one node; f, fnew, feq point at its Q values. */
+/* Collision (Simulation.cpp:43-208: moments :52-175, equilibrium :183-197,
+ * relaxation :201-205) for one node; f, fnew, feq point at its Q values. */
 static void collide_node(int Q, double tau, const double* f, double* fnew, double* feq, double* rho_out,
                          double* u_out) {
     double density = 0.0;
@@ -536,7 +538,7 @@ static void collide_node(int Q, double tau, const double* f, double* fnew, doubl
     u_out[0] = ux; u_out[1] = uy; u_out[2] = uz;
 }
 
-/* Boundary::ApplyBc, D3Q19 (Boundary.cpp:157-185). */
+/* Boundary::ApplyBc, D3Q19 (Boundary.cpp:129-157). */
 static void ref_inlet_q19(double* m, double vel) {
     double u0 = vel, u1 = 0.0, u2 = 0.0;
     double rhoN = (m[2] + m[3] + m[4] + m[5] + m[14] + m[15] + m[16] + m[17] + m[18] +
@@ -774,9 +776,9 @@ void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads) {
 #else
     (void)nthreads;
 #endif
-    double* g = NULL;
-    if (s->mode == ORC_PHYSICS) g = (double*)malloc(sizeof(double) * (size_t)(na * Q + 1));
+    if (s->mode == ORC_PHYSICS && !s->pulled) s->pulled = (double*)malloc(sizeof(double) * (size_t)(na * Q + 1));
     for (int it = 0; it < nsteps; ++it) {
+        double* g = s->pulled;
         double amp = s->amp[s->step % s->namp];
         /* collide */
 #pragma omp parallel for schedule(static)
@@ -788,7 +790,7 @@ void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads) {
         /* stream */
         if (s->mode == ORC_PARITY) {
             /* push; a destination keeps its value when the link is missing or
-             * the post-collision value is exactly zero (Simulation.cpp:273-277) */
+             * the post-collision value is exactly zero (Simulation.cpp:220-224) */
 #pragma omp parallel for schedule(static)
             for (int64_t b = 0; b < na; ++b)
                 for (int q = 0; q < Q; ++q) {
@@ -819,7 +821,8 @@ void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads) {
                     }
                     g[b * Q + q] = v;
                 }
-            memcpy(s->f, g, sizeof(double) * (size_t)(na * Q));
+            s->pulled = s->f;
+            s->f = g;
         }
         /* boundary conditions: inlet / outlets (list order irrelevant: each node is independent) */
 #pragma omp parallel for schedule(static)
@@ -853,7 +856,6 @@ void oracle_sim_step(oracle_sim* s, int nsteps, int nthreads) {
         }
         s->step++;
     }
-    free(g);
 }
 
 int64_t oracle_sim_nactive(const oracle_sim* s) { return s->nact; }

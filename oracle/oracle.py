@@ -223,8 +223,22 @@ def reference_available() -> bool:
     return os.path.exists(REF_HARNESS)
 
 
-def build_reference(ref_dir: str = "/root/reference") -> bool:
-    if not os.path.isdir(ref_dir):
+def reference_dir() -> str:
+    """Where the reference's sources are read from: $LBM_REFERENCE_DIR, else
+    the default the Makefile beside this file gives its REF variable."""
+    env = os.environ.get("LBM_REFERENCE_DIR")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as fh:
+        for line in fh:
+            if line.startswith("REF ?="):
+                return line.split("=", 1)[1].strip()
+    return ""
+
+
+def build_reference(ref_dir: str | None = None) -> bool:
+    ref_dir = ref_dir or reference_dir()
+    if not ref_dir or not os.path.isdir(ref_dir):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}", "-j8"], check=True)
     return os.path.exists(REF_HARNESS)

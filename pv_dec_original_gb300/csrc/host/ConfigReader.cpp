@@ -1,7 +1,6 @@
 #include "ConfigReader.h"
 
 #include <cstdlib>
-#include <cstring>
 #include <fstream>
 #include <iostream>
 
@@ -61,34 +60,52 @@ bool ConfigReader::readConfigStrings(std::map<std::string, std::string>& values)
     return true;
 }
 
+// Equation blocks.  Grammar (comment and blank lines are skipped):
+//   marker    := any line containing the word "Equation"
+//   condition := any other line containing "Conditions:"; the text after
+//                the tag is the block's condition (a later one replaces it)
+//   body      := every other line, appended with its newline
+// A marker closes the open block when it has both a condition and a body
+// (an incomplete block stays open and keeps collecting); the end of the
+// file closes it the same way.  Blocks come out as (condition, body).
+namespace {
+
+struct EquationBlock {
+    std::string condition, body;
+    bool complete() const { return !condition.empty() && !body.empty(); }
+};
+
+}  // namespace
+
 bool ConfigReader::readEquations(std::vector<std::pair<std::string, std::string>>& equations) {
-    std::ifstream file(configFile);
-    if (!file.is_open()) {
+    std::ifstream in(configFile);
+    if (!in) {
         error_ = "Error opening file: " + configFile;
         std::cerr << error_ << std::endl;
         return false;
     }
-    std::string line, equation, conditions;
-    while (std::getline(file, line)) {
-        if (line.empty() || line[0] == '#') continue;
-        size_t equationPos = line.find("Equation");
-        size_t conditionsPos = line.find("Conditions:");
-        if (equationPos != std::string::npos) {
-            if (!equation.empty() && !conditions.empty()) {
-                equations.emplace_back(conditions, equation);
-                equation.clear();
-                conditions.clear();
-            }
-        } else if (conditionsPos != std::string::npos) {
-            conditions = line.substr(conditionsPos + std::strlen("Conditions:"));
-        } else {
-            equation += line + '\n';
+    static const char kTag[] = "Conditions:";
+    EquationBlock open;
+    auto close_if_complete = [&]() {
+        if (!open.complete()) return;
+        equations.emplace_back(std::move(open.condition), std::move(open.body));
+        open = EquationBlock{};
+    };
+    for (std::string text; std::getline(in, text);) {
+        if (text.empty() || text.front() == '#') continue;
+        if (text.find("Equation") != std::string::npos) {
+            close_if_complete();
+            continue;
         }
+        const size_t tag = text.find(kTag);
+        if (tag != std::string::npos) open.condition = text.substr(tag + sizeof(kTag) - 1);
+        else open.body.append(text).push_back('\n');
     }
-    if (!equation.empty() && !conditions.empty()) equations.emplace_back(conditions, equation);
+    close_if_complete();
     return true;
 }
 
 void ConfigReader::printEquations(const std::vector<std::pair<std::string, std::string>>& equations) const {
-    for (const auto& eq : equations) std::cout << "Equation Section: " << eq.first << "\n" << eq.second << "\n\n";
+    for (size_t k = 0; k < equations.size(); ++k)
+        std::cout << "Equation Section: " << equations[k].first << '\n' << equations[k].second << "\n\n";
 }

@@ -74,7 +74,7 @@ int64_t Simulation::steps() {
 
 void Simulation::InitializeShearStressAccumulators() {
     // accumulators live on the device; a fresh state starts from f = w with
-    // cleared accumulators (Simulation.cpp:85-91)
+    // cleared accumulators (Simulation.cpp:32-38)
     if (h_) check(lbm_init_equilibrium(h_), "lbm_init_equilibrium");
 }
 

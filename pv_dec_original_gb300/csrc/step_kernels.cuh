@@ -12,10 +12,10 @@
 // active nodes whose 18 neighbour offsets in active-index space agree (in
 // practice an x-run of a row), so loads of a warp are contiguous and stores
 // are exactly contiguous.  Launch k:
-//   1. pulls f*_q(x - c_q) from the input planes        (Streaming, Simulation.cpp:264-290)
+//   1. pulls f*_q(x - c_q) from the input planes        (Streaming, Simulation.cpp:211-237)
 //   2. applies Zou-He / the wall rule on boundary nodes (Simulation.cpp:614-863)
 //   3. accumulates wall shear stress on next-to-wall nodes (Simulation.cpp:880-898)
-//   4. collides and writes f* to the output planes      (Collision, Simulation.cpp:96-261)
+//   4. collides and writes f* to the output planes      (Collision, Simulation.cpp:43-208)
 // so the step order of Iterate() (Simulation.cpp:577-586) is kept with the
 // step boundary moved between 3 and 4; a prologue launch collides the initial
 // state and a read-out launch stops after 2.
@@ -31,7 +31,7 @@
 // Parity semantics for links whose source is missing: the reference's push
 // leaves the destination's previous value in place; the boundary list keeps
 // that previous post-boundary value in `stale`.  A pulled value that is
-// exactly 0.0 is treated the same way (Simulation.cpp:275); on interior
+// exactly 0.0 is treated the same way (Simulation.cpp:220-224); on interior
 // nodes, which keep no previous value, the event is flagged instead
 // (FLAG_EXACT_ZERO) -- it needs a post-collision population of exactly zero.
 #pragma once
@@ -45,7 +45,7 @@ constexpr int MODE_PARITY = LBM_PARITY;
 constexpr int MODE_PHYSICS = LBM_PHYSICS;
 constexpr int KIND_STEP = 0, KIND_PROLOGUE = 1, KIND_READOUT = 2;
 
-// Momentum sums with the reference's explicit index lists (Simulation.cpp:122-228);
+// Momentum sums with the reference's explicit index lists (Simulation.cpp:66-175);
 // the same lists apply to offsets because sum_q w_q c_q = 0.
 template <int Q, typename R>
 __device__ __forceinline__ void momentum(const R (&f)[Q], R& px, R& py, R& pz) {
@@ -64,7 +64,7 @@ __device__ __forceinline__ void momentum(const R (&f)[Q], R& px, R& py, R& pz) {
 }
 
 // Moments.  Full f (FP64): rho = sum f and u = j / rho with three divisions,
-// as the reference rounds them (Simulation.cpp:105-158).  Offsets (FP32):
+// as the reference rounds them (Simulation.cpp:52-175).  Offsets (FP32):
 // r = rho - 1 = sum d, u = j / (1 + r).  `r` returns rho (full) or rho - 1.
 template <int Q, typename R, bool OFF>
 __device__ __forceinline__ void moments(const R (&f)[Q], R& r, R& ux, R& uy, R& uz) {
@@ -83,7 +83,7 @@ __device__ __forceinline__ void moments(const R (&f)[Q], R& r, R& ux, R& uy, R& 
 }
 
 // Equilibrium of direction q.  Full: w rho (1 + 3cu + 4.5(cu)^2 - 1.5u^2) in the
-// reference's operation order (Simulation.cpp:239-249).  Offset:
+// reference's operation order (Simulation.cpp:183-197).  Offset:
 // feq - w = w (r + rho (3cu + 4.5(cu)^2 - 1.5u^2)) with r = rho - 1.
 template <int Q, int q, typename R, bool OFF>
 __device__ __forceinline__ R feq_q(R r, R ux, R uy, R uz, R usqr) {
@@ -340,7 +340,7 @@ __device__ __forceinline__ void relax_pairs_units(float (&g)[Q], float A, float 
 // ---------------------------------------------------------------------------
 // Boundary formulas.
 
-// Boundary::ApplyBc, D3Q19 x-min velocity inlet (Boundary.cpp:157-185), full f.
+// Boundary::ApplyBc, D3Q19 x-min velocity inlet (Boundary.cpp:129-157), full f.
 __device__ __forceinline__ void ref_inlet_q19(double (&m)[19], double vel) {
     const double u0 = vel, u1 = 0.0, u2 = 0.0;
     double rhoN = (m[2] + m[3] + m[4] + m[5] + m[14] + m[15] + m[16] + m[17] + m[18] +
@@ -388,7 +388,7 @@ __device__ __forceinline__ void ref_outlet_zmin_q19(double (&m)[19]) {
 //   N_t = (sum_{c_a=0} f c_t - 2/3 rho u_t) / M      (M = 2 for D3Q19, 6 for D3Q27)
 //   f_i = f_opp(i) + 6 w_i rho (c_i . u) - sum_t c_it N_t
 // which reduces to the reference's formulas on its faces for both lattices
-// (Boundary.cpp:115-185).  On offsets d = f - w the same lines hold with
+// (Boundary.cpp:87-157).  On offsets d = f - w the same lines hold with
 // S_0 + 2 S_{-sigma} gaining +1 (the weights of those populations sum to 1)
 // and everything else unchanged (w_i = w_opp(i), sum_{c_a=0} w c_t = 0).
 template <int Q, int FACE, typename R, bool OFF>

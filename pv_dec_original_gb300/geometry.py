@@ -34,7 +34,7 @@ import numpy as np
 __all__ = [
     "Surface", "write_stl_ascii", "read_stl_ascii", "capped_cylinder", "y_bifurcation",
     "stenosed_tube", "elbow", "add_bbox_anchors", "marching_tetrahedra", "reference_lattice_dims",
-    "config_c1_cylinder", "config_c2_bifurcation", "config_c4_ensemble",
+    "config_c1_cylinder", "config_c1_cylinder_x", "config_c2_bifurcation", "config_c4_ensemble",
 ]
 
 
@@ -409,6 +409,19 @@ def config_c1_cylinder(lattice=(24, 24, 104)) -> Surface:
     s = add_bbox_anchors(s, (0.0, 0.0, 0.0), (nx - 1.0, ny - 1.0, float(nz)))
     s.meta.update({"kind": "cylinder", "radius": 10.0, "center": (cx, cy), "z0": z0, "length": 100.0})
     return s
+
+
+def config_c1_cylinder_x() -> Surface:
+    """The C1 cylinder turned to lie along +x (coordinates cycled (x, y, z)
+    -> (z, x, y), a rotation), so its inflow face is the x-min face on which
+    the reference's velocity inlet formula acts (Boundary.cpp:129-157)."""
+    s = config_c1_cylinder()
+    v = s.v[:, :, [2, 0, 1]].copy()
+    n = s.n[:, [2, 0, 1]].copy()
+    cx, cy = s.meta["center"]
+    meta = dict(s.meta)
+    meta.update({"kind": "cylinder_x", "center": (cx, cy), "axis": "x"})
+    return Surface(v, n, meta)
 
 
 def config_c2_bifurcation(lattice=(256, 192, 512), seed: int = 0, h: float = 3.0) -> Surface:

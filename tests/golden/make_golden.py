@@ -1,8 +1,9 @@
 """Generate the golden fixtures from the reference's own C++ (compiled unchanged).
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run in a checkout that has the reference sources (the directory given by
+--ref, else $LBM_REFERENCE_DIR, else the REF default of oracle/Makefile):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref DIR]
 
 It builds ``oracle/_ref/ref_harness`` (see oracle/Makefile), generates the
 input geometries with the package's generators, runs the reference's
@@ -37,6 +38,7 @@ def geometries():
     """name -> (tri12, spacing)"""
     g = {}
     g["c1_cylinder"] = (G.config_c1_cylinder().tri12(), 1.0)
+    g["c1x_cylinder"] = (G.config_c1_cylinder_x().tri12(), 1.0)
     g["elbow_z"] = (G.elbow(radius=5.0, leg=22.0, h=1.6, seed=1, exit="z-").tri12(), 1.0)
     g["elbow_y"] = (G.elbow(radius=5.0, leg=22.0, h=1.6, seed=2, exit="y+").tri12(), 1.0)
     bif = G.y_bifurcation(6.0, 4.25, 30.0, z_in=1.3, z_out=60.6, z_split=38.0, center=(16.2, 10.1), seed=0, h=1.5)
@@ -88,6 +90,12 @@ SIMS = {
     # x-min inlet with a parabolic profile and y-max outlet (outlet 1)
     "elbow_y": dict(rules=[("inlet", 0, None, "min"), ("outlet1", 1, None, "max")], profile="auto",
                     tau=0.7, dt=8e-6, nsteps=80, amp=lambda s: 0.04),
+    # the C1 cylinder along x: parabolic x-min inlet (u_max 0.05), tau 0.8;
+    # the reference has no x-max outlet formula, so the far end is wall
+    # (the run covers the inflow transient: 200 steps, before the pressure
+    # wave returns from the closed end)
+    "c1x_cylinder": dict(rules=[("inlet", 0, None, "min")], profile="auto", tau=0.8, dt=1e-4, nsteps=200,
+                         amp=lambda s: 0.05),
 }
 
 
@@ -164,17 +172,23 @@ def pulse_fixture(tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=O.reference_dir())
+    ap.add_argument("--only", nargs="*", default=None,
+                    help="fixture names to (re)generate, e.g. sim_c1x_cylinder vox_c1_cylinder pulse")
     a = ap.parse_args()
     if not O.build_reference(a.ref):
         sys.exit(f"reference sources not found at {a.ref}")
+    want = (lambda name: True) if a.only is None else (lambda name: name in a.only)
     with tempfile.TemporaryDirectory() as tmp:
         geos = geometries()
         for name, (tri, sp) in geos.items():
-            vox_fixture(name, tri, sp, tmp)
+            if want("vox_" + name) and name != "c1x_cylinder":
+                vox_fixture(name, tri, sp, tmp)
         for name in SIMS:
-            sim_fixture(name, geos[name][0], geos[name][1], tmp)
-        pulse_fixture(tmp)
+            if want("sim_" + name):
+                sim_fixture(name, geos[name][0], geos[name][1], tmp)
+        if want("pulse"):
+            pulse_fixture(tmp)
 
 
 if __name__ == "__main__":

@@ -61,9 +61,13 @@ def test_gpu_parity_graph_and_split_calls_identical(gpu_lib, path):
     assert np.array_equal(a.wss()["acc"], b.wss()["acc"])
 
 
-@pytest.mark.parametrize("prec,tol", [("f32", 2e-5), ("f16", 5e-3), ("bf16", 3e-2)])
-def test_gpu_low_precision_parity_vs_fp64(gpu_lib, prec, tol):
-    d = load(fixtures("sim")[0])
+@pytest.mark.parametrize("path", fixtures("sim"), ids=lambda p: p.split("/")[-1])
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-5), ("f16", 5e-3), ("bf16", 3e-2)])
+def test_gpu_low_precision_parity_vs_fp64(gpu_lib, path, prec, tol):
+    """Parity semantics in each storage format against the FP64 run of the
+    same golden case: velocity L2 relative error within the stated
+    tolerance (1e-5 for FP32)."""
+    d = load(path)
     ref, _ = _gpu_parity_run(gpu_lib, d, gpu_lib.LBM_F64)
     got, _ = _gpu_parity_run(gpu_lib, d, prec)
     r_rho, r_u = ref.macro()

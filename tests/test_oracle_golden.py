@@ -61,6 +61,57 @@ def test_oracle_step_bit_exact_vs_reference(oracle_lib, path):
         assert np.array_equal(nw[k], d["nw_" + k]), k
 
 
+def _pv_fixture():
+    from helpers import GOLDEN
+    d = load(GOLDEN + "/pv_stl.npz")
+    tri = np.concatenate([d["verts"][d["faces"]].reshape(-1, 9), d["normals"]], axis=1)
+    return d, np.ascontiguousarray(tri)
+
+
+def test_oracle_pv_mask_pin(oracle_lib):
+    """PV.stl at spacing 0.05: the binned oracle's mask is the pinned one,
+    and the brute-force oracle (every triangle for every point, the
+    reference's loop) agrees with it on 12x12 columns of the pinned block."""
+    O = oracle_lib
+    d, tri = _pv_fixture()
+    sp = float(d["spacing"])
+    bb, dims = O.bbox_dims(tri, sp)
+    assert tuple(dims) == tuple(int(v) for v in d["dims"]) and np.array_equal(bb, d["bbox"])
+    mask, _, _ = O.voxelize(tri, sp)
+    assert int(mask.sum()) == int(d["nfluid"])
+    assert sha(mask.reshape(-1)) == str(d["mask_sha"])
+    i0, j0, n = (int(v) for v in d["brute_block"])
+    i0, j0 = i0 + n // 2 - 6, j0 + n // 2 - 6
+    org = (bb[0] + i0 * sp, bb[2] + j0 * sp, bb[4])
+    sub, _, _ = O.voxelize(tri, sp, bbox=bb, origin=org, dims=(12, 12, dims[2]), culled=False)
+    assert sub.any() and np.array_equal(sub, mask[:, j0:j0 + 12, i0:i0 + 12])
+
+
+def test_pv_windows_pin_from_reference_rule(oracle_lib):
+    """The reference's PV windows (ComplexGeometry.cpp:1369-1429, long
+    double) on the pinned mask's boundary points give the pinned lists."""
+    import importlib.util
+    from helpers import GOLDEN
+    spec = importlib.util.spec_from_file_location("make_pv_fixture", GOLDEN + "/make_pv_fixture.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    O = oracle_lib
+    d, tri = _pv_fixture()
+    sp = float(d["spacing"])
+    nx, ny, nz = (int(v) for v in d["dims"])
+    bb = d["bbox"]
+    mask, _, _ = O.voxelize(tri, sp)
+    bidx = np.flatnonzero(O.find_boundary(mask, 19).reshape(-1))
+    assert len(bidx) == int(d["nboundary"])
+    coords = np.stack([bb[0] + (bidx % nx) * sp, bb[2] + ((bidx // nx) % ny) * sp, bb[4] + (bidx // (nx * ny)) * sp],
+                      axis=1)
+    win = mk.classify_windows(coords)
+    for w in range(4):
+        assert int((win == w).sum()) == int(d["window_count"][w])
+        assert sha(bidx[win == w].astype(np.int64)) == str(d["window_sha"][w])
+    assert int((win < 0).sum()) == int(d["nwall"])
+
+
 def test_waveform_matches_reference():
     from helpers import GOLDEN
     from pv_dec_original_gb300 import waveform
