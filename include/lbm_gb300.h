@@ -323,13 +323,16 @@ lbm_status lbm_preset_barrier(lbm_handle* h, unsigned extra_arrivals);
  * (block size, minimum resident blocks per SM) = (128,12) (128,10) (128,8)
  * (256,3) (256,1); variant 5, the tiled kernel (bulk copies stage each
  * 256-node tile's sources in shared memory; physics mode, FP32 / FP16 /
- * BF16; elsewhere it runs variant 0, or 4 for FP64).  A new handle starts
- * on variant 0, FP64 on variant 4.  lbm_autotune times each variant for trial_steps steps on a
- * snapshot of the current state, restores the state, keeps the fastest and
- * reports it (and, if ms_per_step is not NULL, the time of every variant:
- * LBM_NUM_VARIANTS floats).  No reference counterpart (the reference has a
- * single serial loop). */
-#define LBM_NUM_VARIANTS 6
+ * BF16; elsewhere it runs variant 0, or 4 for FP64); variants 6 (128,10)
+ * and 7 (128,12), the compact kernel (32 bytes of node metadata per warp of
+ * 32 nodes instead of 12 bytes a node; physics mode, FP32 / FP16 / BF16,
+ * half-way bounce-back; elsewhere variant 0).  A new handle starts on
+ * variant 0, FP64 on variant 4.  lbm_autotune times each variant for
+ * trial_steps steps on a snapshot of the current state, restores the
+ * state, keeps the fastest and reports it (and, if ms_per_step is not NULL,
+ * the time of every variant: LBM_NUM_VARIANTS floats).  No reference
+ * counterpart (the reference has a single serial loop). */
+#define LBM_NUM_VARIANTS 8
 lbm_status lbm_autotune(lbm_handle* h, int trial_steps, int* best, float* ms_per_step);
 lbm_status lbm_set_variant(lbm_handle* h, int variant);
 

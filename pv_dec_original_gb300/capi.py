@@ -72,7 +72,7 @@ EXPORTS = [
     "lbm_init_from_macro_device", "lbm_nearest_next_to_wall", "lbm_set_wall_distances", "lbm_get_wall_distances",
     "lbm_get_macro_async", "lbm_get_wss_async", "lbm_wait_outputs",
 ]
-NUM_VARIANTS = 6
+NUM_VARIANTS = 8  # LBM_NUM_VARIANTS: lbm_autotune writes this many floats
 
 
 def lib_path() -> str:

@@ -45,6 +45,8 @@ struct lbm_handle {
     int64_t npts = 0, stride = 0;
     int32_t* seg_delta = nullptr;  // per pull segment: Q offsets in active-index space
     int64_t nseg = 0;
+    int32_t* seg_abs = nullptr;      // compact step kernel: rows of q * stride + delta_q
+    uint32_t* warp_block = nullptr;  // compact step kernel: a block of words per warp of 32 active nodes
     GeometryLists g;
     bool has_geo = false;
     bool has_state = false;
@@ -238,7 +240,7 @@ void free_geometry(lbm_handle* h) {
                     g.act_idx, g.act_pt,
                     h->buf[0], h->buf[1], h->stale, h->nw_prev, h->nw_n, h->nw_wss, h->nw_acc, h->nw_accm,
                     h->partials, h->sums, h->out_f, h->macro, h->seg_delta, h->nw_nf, h->nw_wssf, h->nw_accf, h->tile_plan,
-                    h->nw_ring, h->nw_out, h->sp_q, h->nw_fields};
+                    h->nw_ring, h->nw_out, h->sp_q, h->nw_fields, h->seg_abs, h->warp_block};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     g = GeometryLists();
@@ -246,6 +248,8 @@ void free_geometry(lbm_handle* h) {
     h->nw_n = h->nw_wss = h->nw_acc = h->nw_accm = h->partials = h->sums = h->out_f = h->macro = nullptr;
     h->seg_delta = nullptr;
     h->nseg = 0;
+    h->seg_abs = nullptr;
+    h->warp_block = nullptr;
     h->bct = nullptr;
     h->sp_flux = nullptr;
     h->nw_nf = h->nw_wssf = nullptr;
@@ -276,6 +280,8 @@ StepParams make_params(lbm_handle* h, int kind) {
     }
     p.stride = h->stride;
     p.seg_delta = h->seg_delta;
+    p.seg_abs = h->seg_abs;
+    p.warp_block = h->warp_block;
     p.nact = h->g.nact;
     p.act_word = h->g.act_word;
     p.sp_of_act = h->g.sp_of_act;
@@ -918,6 +924,7 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
         h->bc[b].c2 = bc[b].c2;
         h->bc[b].R = bc[b].R;
         h->bc[b].wave = bc[b].wave;
+        h->bc[b].value_m1 = (float)(bc[b].value - 1.0);
     }
     CK(h, dalloc(h, &h->bct, sizeof(BCDev) * (nbc + 1)));
     if (nbc) CK(h, cudaMemcpyAsync(h->bct, h->bc.data(), sizeof(BCDev) * nbc, cudaMemcpyHostToDevice, h->st));
@@ -943,6 +950,14 @@ lbm_status lbm_set_geometry(lbm_handle* h, const uint8_t* mask, const int dims[3
     CK(h, dalloc(h, &h->nw_wssf, sizeof(float) * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_accf, sizeof(float2) * 4 * (h->g.nnw + 1)));
     CK(h, dalloc(h, &h->nw_ring, sizeof(float) * kRingSlots * 4 * (h->g.nnw + 1)));
+    if (h->d.mode == LBM_PHYSICS && h->d.precision != LBM_F64 && (int64_t)Q * h->stride < ((int64_t)1 << 31)) {
+        // compact step kernel: absolute pull rows and per-warp blocks
+        const int64_t rows = h->nseg * (Q == 19 ? kDeltaRow<19> : kDeltaRow<27>);
+        CK(h, dalloc(h, &h->warp_block, sizeof(uint32_t) * kWarpBlockWords * block_warps(h->g.nact)));
+        CK(h, dalloc(h, &h->seg_abs, sizeof(int32_t) * (rows + 4)));
+        CK(h, build_compact_meta(Q, h->g.act_word, h->g.sp_of_act, h->g.nact, h->g.nnw, h->seg_delta, h->nseg,
+                                 h->stride, h->warp_block, h->seg_abs, h->st));
+    }
     h->nblocks = ceil_div(h->g.nact, kStepThreads);
     CK(h, dalloc(h, &h->partials, sizeof(double) * kPartialStride * (h->nblocks + 1)));
     CK(h, dalloc(h, &h->sums, sizeof(double) * kPartialStride));

@@ -44,7 +44,8 @@ struct BCDev {
     double value;
     int profile;
     double c1, c2, R;
-    int wave;  // inlet waveform of a velocity rule
+    int wave;        // inlet waveform of a velocity rule
+    float value_m1;  // pressure rules: value - 1 (density offset) for the FP32-arithmetic formats
 };
 
 // Everything one stream-collide launch needs (passed by value).
@@ -53,6 +54,13 @@ struct StepParams {
     void* fout;
     int64_t stride;            // elements per population plane (active nodes, padded)
     const int32_t* seg_delta;  // per pull segment, Q source offsets in active-index space (rows of kDeltaRow<Q>)
+    // compact step kernel (physics, FP32-arithmetic formats, 32-bit offsets):
+    // per pull segment the Q offsets q * stride + delta_q from the node's own
+    // entry of plane 0 (rows of kDeltaRow<Q>), and per warp of 32
+    // consecutive active nodes kWarpBlockWords words of lane masks and first
+    // boundary-list entries (step_kernels.cuh); null where not built
+    const int32_t* seg_abs;
+    const uint32_t* warp_block;
     // one thread per active node; packed word layout in step_kernels.cuh
     int64_t nact;
     const uint64_t* act_word;
@@ -127,7 +135,7 @@ constexpr int kStepThreads = 256;
 // (collide the initial state), 2 materialize (post-boundary f + sums).
 constexpr int kRingSlots = 32;  // FP32 stress ring: two halves of kFoldEvery steps
 constexpr int kFoldEvery = 16;  // steps between folds of the FP32 stress ring
-constexpr int kNumVariants = 6;  // launch-shape variants of the step kernel (step_kernels.cuh)
+constexpr int kNumVariants = LBM_NUM_VARIANTS;  // launch-shape variants of the step kernel (step_kernels.cuh)
 cudaError_t launch_step_f64(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 cudaError_t launch_step_f32(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
 cudaError_t launch_step_f16(int Q, int mode, int kind, int variant, const StepParams& p, cudaStream_t s);
@@ -143,6 +151,16 @@ cudaError_t launch_multi_f16(int Q, int mode, const StepParams& even, const Step
                              unsigned* bar, cudaStream_t s);
 cudaError_t launch_multi_bf16(int Q, int mode, const StepParams& even, const StepParams& odd, int nsteps,
                               unsigned* bar, cudaStream_t s);
+
+// Warp blocks of the compact step kernel (built by step_fast.cu): words of
+// lane masks and first entries per warp of 32 active nodes, and the number
+// of warps covered (whole blocks of 256 nodes plus one, zero past the last
+// node).
+constexpr int kWarpBlockWords = 8;
+inline int64_t block_warps(int64_t nact) { return (nact + 255) / 256 * 8 + 8; }
+cudaError_t build_compact_meta(int Q, const uint64_t* act_word, const int32_t* sp_of_act, int64_t nact, int64_t nnw,
+                               const int32_t* seg_delta, int64_t nseg, int64_t stride, uint32_t* warp_block,
+                               int32_t* seg_abs, cudaStream_t s);
 
 // State initialisation: what = 0 fills f = w on every active node, what = 1
 // stores fa[a*Q + q] (FP64, per active node) into the planes.

@@ -15,6 +15,43 @@ cudaError_t init_state_fast(int precision, int Q, int what, void* f, int64_t str
 
 namespace {
 
+// Warp blocks of the compact step kernel (layout in step_kernels.cuh), one
+// warp of this kernel per warp of 32 active nodes: lane masks by ballot,
+// first entries by shuffle from the lowest lane of each mask.
+__global__ void k_warp_block(const uint64_t* __restrict__ act_word, const int32_t* __restrict__ sp_of_act,
+                             int64_t nact, int64_t nnw, uint32_t* __restrict__ out) {
+    constexpr int WB = kWarpBlockWords;
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool in = a < nact;
+    const uint64_t w = in ? act_word[a] : 0ull;
+    const int32_t e = in ? sp_of_act[a] : -1;
+    const uint32_t seg = (uint32_t)word_segment(w);
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, seg, 1);
+    const uint32_t segmask = __ballot_sync(0xffffffffu, in && lane > 0 && seg != prev);
+    const uint32_t nwm = __ballot_sync(0xffffffffu, in && word_nw(w));
+    const uint32_t otm = __ballot_sync(0xffffffffu, in && e >= nnw);
+    const uint32_t bcm = __ballot_sync(0xffffffffu, in && word_class(w) >= CLS_BC0);
+    const uint32_t nw0 = __shfl_sync(0xffffffffu, (uint32_t)e, nwm ? __ffs(nwm) - 1 : 0);
+    const uint32_t ot0 = __shfl_sync(0xffffffffu, (uint32_t)(e - (int32_t)nnw), otm ? __ffs(otm) - 1 : 0);
+    const uint32_t seg0 = __shfl_sync(0xffffffffu, seg, 0);
+    if (lane == 0 && in) {
+        uint32_t* b = out + (size_t)WB * (a >> 5);
+        b[0] = seg0; b[1] = segmask; b[2] = nwm; b[3] = otm;
+        b[4] = bcm; b[5] = nwm ? nw0 : 0u; b[6] = otm ? ot0 : 0u; b[7] = 0u;
+    }
+}
+
+// Rows of q * stride + delta_q (padding entries 0).
+template <int Q>
+__global__ void k_seg_abs(const int32_t* __restrict__ delta, int64_t nseg, int64_t stride, int32_t* __restrict__ out) {
+    constexpr int DR = kDeltaRow<Q>;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nseg * DR) return;
+    const int q = (int)(k % DR);
+    out[k] = q < Q ? (int32_t)(q * stride + delta[k]) : 0;
+}
+
 // Next-to-wall read-out of the FP32 formats, as doubles: out[0] = |tau| of
 // the last step, out[1..3] = sum tau, out[4] = sum |tau| (each [nnw]); the
 // sums are the folded accumulators plus the pending ring slots first ..
@@ -38,6 +75,26 @@ __global__ void k_nw_readout(const float2* __restrict__ accf, const float4* __re
 }
 
 }  // namespace
+
+cudaError_t build_compact_meta(int Q, const uint64_t* act_word, const int32_t* sp_of_act, int64_t nact, int64_t nnw,
+                               const int32_t* seg_delta, int64_t nseg, int64_t stride, uint32_t* warp_block,
+                               int32_t* seg_abs, cudaStream_t st) {
+    if ((int64_t)Q * stride >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(warp_block, 0, sizeof(uint32_t) * kWarpBlockWords * block_warps(nact), st);
+    if (e != cudaSuccess) return e;
+    const int64_t n = nseg * (Q == 19 ? kDeltaRow<19> : kDeltaRow<27>);
+    if (n > 0) {
+        if (Q == 19) k_seg_abs<19><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(seg_delta, nseg, stride, seg_abs);
+        else k_seg_abs<27><<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(seg_delta, nseg, stride, seg_abs);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (nact > 0) {
+        k_warp_block<<<(unsigned)ceil_div(nact, 256), 256, 0, st>>>(act_word, sp_of_act, nact, nnw, warp_block);
+        e = cudaGetLastError();
+    }
+    return e;
+}
 
 cudaError_t nw_readout_f32(const float2* accf, const float* ring, int64_t nnw, int first, int pending, int last,
                            const float* wss_ckpt, double* out, cudaStream_t st) {

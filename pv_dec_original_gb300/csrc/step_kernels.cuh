@@ -141,18 +141,24 @@ __device__ __forceinline__ R cdot(R x, R y, R z) {
     }
 }
 
+// Sums of a pair relaxation: the even parts (one per pair) and, per axis,
+// sum c_a x the odd parts, for the closure of the collision invariants.
+template <typename R>
+struct PairSums {
+    R sym = R(0), ax = R(0), ay = R(0), az = R(0);
+};
+
 // BGK relaxation of offsets d = f - w, direction pairs (q, opp q) sharing
 // the even part of the equilibrium.  With A = 1 + r, B = r - 1.5 A u^2 and
 // du = c_q . u:  feq_{q|opp} - w_q = w_q (B + 4.5 A du^2 +|- 3 A du), and
-// d* = (1 - omega) d + omega (feq - w).
+// d* = (1 - omega) d + omega (feq - w).  The rest population is left to
+// the caller (close_invariants).
 template <int Q, int q = 0>
 __device__ __forceinline__ void relax_pairs(float (&f)[Q], float A, float B, float ux, float uy, float uz, float om,
-                                            float om1) {
+                                            float om1, PairSums<float>& ps) {
     if constexpr (q < Q) {
         constexpr int o = Lat<Q>::opp(q);
-        if constexpr (q == Lat<Q>::REST) {
-            f[q] = om1 * f[q] + (om * (float)Lat<Q>::w(q)) * B;
-        } else if constexpr (q < o) {
+        if constexpr (q != Lat<Q>::REST && q < o) {
             const float du = cdot<Q, q, float>(ux, uy, uz);
             const float ow = om * (float)Lat<Q>::w(q);
             const float t = A * du;
@@ -160,9 +166,46 @@ __device__ __forceinline__ void relax_pairs(float (&f)[Q], float A, float B, flo
             const float anti = (3.0f * ow) * t;
             f[q] = om1 * f[q] + (sym + anti);
             f[o] = om1 * f[o] + (sym - anti);
+            ps.sym += sym;
+            ps.ax = cadd<Lat<Q>::cx(q)>(ps.ax, anti);
+            ps.ay = cadd<Lat<Q>::cy(q)>(ps.ay, anti);
+            ps.az = cadd<Lat<Q>::cz(q)>(ps.az, anti);
         }
-        relax_pairs<Q, q + 1>(f, A, B, ux, uy, uz, om, om1);
+        relax_pairs<Q, q + 1>(f, A, B, ux, uy, uz, om, om1, ps);
     }
+}
+
+// Closure of the collision invariants in FP32 arithmetic.  The collision
+// conserves mass and momentum only through identities of the lattice
+// weights (sum w = 1, sum w c c = I/3); products with the FP32-rounded
+// weights break them by the same relative amount at every node and step, a
+// coherent bias that accumulates (an FP32 bifurcation run drifted in mass
+// against FP64 by ~5e-7 in 1000 steps, its velocity by 7e-6 -- 2.8e-5 on
+// D3Q27 -- and by 1.7e-4 over 12,000 steps).  Instead of its own
+// equilibrium the rest population takes the mass the pairs leave, and each
+// axis pair (+a, -a) takes half the momentum defect.  With every pair
+// member post-collision = keep pre + (sym +- anti):
+//   sum post   = keep r + 2 sum sym + rest part        := r
+//   sum c post = keep j + 2 sum c anti + 2 h (per axis) := j
+// hold exactly in real arithmetic on the computed terms, so only the
+// rounding of the individual results, random from node to node, remains.
+// keep (the coefficient of the pre-collision values: 1 - omega for BGK, 0
+// for the regularized collision) and 1 - keep must both be exact floats:
+// 1 - omega is exact for 1/2 <= omega <= 2 (Sterbenz), i.e. 1/2 <= tau <= 2.
+// Axis pairs: D3Q19 (0, 1) (2, 3) (4, 5); D3Q27 (1, 2) (3, 4) (5, 6).
+template <int Q>
+__device__ __forceinline__ void close_invariants(float (&f)[Q], const PairSums<float>& ps, float keep, float r,
+                                                 float jx, float jy, float jz) {
+    constexpr int XP = Q == 19 ? 0 : 1, YP = Q == 19 ? 2 : 3, ZP = Q == 19 ? 4 : 5;
+    constexpr int RS = Lat<Q>::REST;
+    const float give = 1.0f - keep;  // exact
+    f[RS] = keep * f[RS] + (give * r - 2.0f * ps.sym);
+    const float hx = fmaf(0.5f * give, jx, -ps.ax);
+    const float hy = fmaf(0.5f * give, jy, -ps.ay);
+    const float hz = fmaf(0.5f * give, jz, -ps.az);
+    f[XP] += hx; f[Lat<Q>::opp(XP)] -= hx;
+    f[YP] += hy; f[Lat<Q>::opp(YP)] -= hy;
+    f[ZP] += hz; f[Lat<Q>::opp(ZP)] -= hz;
 }
 
 // Second moments sum_q d_q c_qa c_qb (xx, yy, zz, xy, xz, yz) from the
@@ -196,7 +239,7 @@ __device__ __forceinline__ void second_moments(const R (&d)[Q], R (&m)[6]) {
 // 1/2 where BGK diverges.  kreg = 4.5 (1 - omega).
 template <int Q, typename R, int q = 0>
 __device__ __forceinline__ void relax_reg_pairs(R (&f)[Q], const R (&P)[6], R T3, R A, R B, R ux, R uy, R uz,
-                                                R kreg) {
+                                                R kreg, PairSums<R>& ps) {
     if constexpr (q < Q) {
         constexpr int o = Lat<Q>::opp(q);
         constexpr int cx = Lat<Q>::cx(q), cy = Lat<Q>::cy(q), cz = Lat<Q>::cz(q);
@@ -218,13 +261,17 @@ __device__ __forceinline__ void relax_reg_pairs(R (&f)[Q], const R (&P)[6], R T3
             const R anti = (R(3.0) * w) * t;
             f[q] = e + anti;
             f[o] = e - anti;
+            ps.sym += e;
+            ps.ax = cadd<cx>(ps.ax, anti);
+            ps.ay = cadd<cy>(ps.ay, anti);
+            ps.az = cadd<cz>(ps.az, anti);
         }
-        relax_reg_pairs<Q, R, q + 1>(f, P, T3, A, B, ux, uy, uz, kreg);
+        relax_reg_pairs<Q, R, q + 1>(f, P, T3, A, B, ux, uy, uz, kreg, ps);
     }
 }
 
 template <int Q, typename R>
-__device__ __forceinline__ void relax_regularized(R (&f)[Q], R r, R A, R ux, R uy, R uz, R om) {
+__device__ __forceinline__ void relax_regularized(R (&f)[Q], R r, R A, R ux, R uy, R uz, R om, PairSums<R>& ps) {
     R m[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
     second_moments<Q, 0, R>(f, m);
     const R r3 = r * (R(1) / R(3));
@@ -232,7 +279,7 @@ __device__ __forceinline__ void relax_regularized(R (&f)[Q], R r, R A, R ux, R u
                     m[3] - A * ux * uy,        m[4] - A * ux * uz,        m[5] - A * uy * uz};
     const R T3 = (P[0] + P[1] + P[2]) * (R(1) / R(3));
     const R B = r - R(1.5) * A * (ux * ux + uy * uy + uz * uz);
-    relax_reg_pairs<Q, R>(f, P, T3, A, B, ux, uy, uz, R(4.5) * (R(1) - om));
+    relax_reg_pairs<Q, R>(f, P, T3, A, B, ux, uy, uz, R(4.5) * (R(1) - om), ps);
 }
 
 // Wall shear stress from the non-equilibrium stress tensor
@@ -391,6 +438,14 @@ __device__ __forceinline__ void ref_outlet_zmin_q19(double (&m)[19]) {
 // (Boundary.cpp:87-157).  On offsets d = f - w the same lines hold with
 // S_0 + 2 S_{-sigma} gaining +1 (the weights of those populations sum to 1)
 // and everything else unchanged (w_i = w_opp(i), sum_{c_a=0} w c_t = 0).
+// The offset form keeps rho - 1 instead of rho (a pressure rule's `value`
+// is then rho - 1): S - 1 = S_0 + 2 S_{-sigma} is small, and forming S or
+// rho near 1 in FP32 would round the boundary's mass flux by the same few
+// 1e-8 at a node every step (an outlet's u_a = 1 - S / rho cancels down to
+// the velocity), a coherent bias like the one close_invariants removes:
+//   pressure:  u_a = sigma ((rho - 1) - (S - 1)) / rho
+//   velocity:  rho - 1 = ((S - 1) + sigma u_a) / (1 - sigma u_a)
+// with rho x formed as x + (rho - 1) x.
 template <int Q, int FACE, typename R, bool OFF>
 __device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
     constexpr int a = FACE / 2;
@@ -402,15 +457,26 @@ __device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
         if (ca == 0) S0 += m[q];
         else if (ca == -sg) Sm += m[q];
     }
-    const R S = (OFF ? R(1) : R(0)) + S0 + R(2.0) * Sm;
     R u[3] = {R(0), R(0), R(0)};
-    R rho;
-    if (pressure) {
-        rho = value;
-        u[a] = R(sg) * (R(1.0) - S / rho);
+    R rho = R(0), rm1 = R(0);  // rho (full f) or rho - 1 (offsets)
+    if constexpr (OFF) {
+        const R Sp = S0 + R(2.0) * Sm;
+        if (pressure) {
+            rm1 = value;
+            u[a] = R(sg) * (rm1 - Sp) / (R(1.0) + rm1);
+        } else {
+            u[a] = R(sg) * value;
+            rm1 = (Sp + R(sg) * u[a]) / (R(1.0) - R(sg) * u[a]);
+        }
     } else {
-        u[a] = R(sg) * value;
-        rho = S / (R(1.0) - R(sg) * u[a]);
+        const R S = S0 + R(2.0) * Sm;
+        if (pressure) {
+            rho = value;
+            u[a] = R(sg) * (R(1.0) - S / rho);
+        } else {
+            u[a] = R(sg) * value;
+            rho = S / (R(1.0) - R(sg) * u[a]);
+        }
     }
     R N[3] = {R(0), R(0), R(0)};
 #pragma unroll
@@ -420,7 +486,8 @@ __device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
 #pragma unroll
         for (int q = 0; q < Q; ++q)
             if (lat_c<Q>(q, a) == 0) st += m[q] * (R)lat_c<Q>(q, t);
-        N[t] = (st - (R(2.0) / R(3.0)) * rho * u[t]) / (R)Lat<Q>::ZH_M;
+        if constexpr (OFF) N[t] = (st - (R(2.0) / R(3.0)) * (u[t] + rm1 * u[t])) / (R)Lat<Q>::ZH_M;
+        else N[t] = (st - (R(2.0) / R(3.0)) * rho * u[t]) / (R)Lat<Q>::ZH_M;
     }
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -430,7 +497,8 @@ __device__ __forceinline__ void zou_he_face(R (&m)[Q], bool pressure, R value) {
 #pragma unroll
         for (int t = 0; t < 3; ++t)
             if (t != a) corr += (R)lat_c<Q>(q, t) * N[t];
-        m[q] = m[Lat<Q>::opp(q)] + R(6.0) * (R)Lat<Q>::w(q) * rho * cu - corr;
+        if constexpr (OFF) m[q] = m[Lat<Q>::opp(q)] + R(6.0) * (R)Lat<Q>::w(q) * (cu + rm1 * cu) - corr;
+        else m[q] = m[Lat<Q>::opp(q)] + R(6.0) * (R)Lat<Q>::w(q) * rho * cu - corr;
     }
 }
 
@@ -454,17 +522,19 @@ __device__ __forceinline__ void apply_bc(R (&m)[Q], const BCDev& b, double amp, 
     R vel;
     if constexpr (OFF) vel = (R)amp * (R)prof * (R)b.value;
     else vel = amp * prof * b.value;
+    // the reference outlets' density as zou_he_face takes it: rho, or rho - 1 on offsets
+    const R unit_rho = OFF ? R(0.0) : R(1.0);
     if constexpr (Q == 19 && !OFF) {
         if (b.kind == LBM_BC_REF_INLET) { ref_inlet_q19(m, vel); return; }
         if (b.kind == LBM_BC_REF_OUTLET_YMAX) { ref_outlet_ymax_q19(m); return; }
         if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { ref_outlet_zmin_q19(m); return; }
     } else {
         if (b.kind == LBM_BC_REF_INLET) { zou_he<Q, R, OFF>(m, LBM_FACE_XMIN, false, vel); return; }
-        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { zou_he<Q, R, OFF>(m, LBM_FACE_YMAX, true, R(1.0)); return; }
-        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { zou_he<Q, R, OFF>(m, LBM_FACE_ZMIN, true, R(1.0)); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_YMAX) { zou_he<Q, R, OFF>(m, LBM_FACE_YMAX, true, unit_rho); return; }
+        if (b.kind == LBM_BC_REF_OUTLET_ZMIN) { zou_he<Q, R, OFF>(m, LBM_FACE_ZMIN, true, unit_rho); return; }
     }
     if (b.kind == LBM_BC_VELOCITY) zou_he<Q, R, OFF>(m, b.face, false, vel);
-    else if (b.kind == LBM_BC_PRESSURE) zou_he<Q, R, OFF>(m, b.face, true, (R)b.value);
+    else if (b.kind == LBM_BC_PRESSURE) zou_he<Q, R, OFF>(m, b.face, true, OFF ? (R)b.value_m1 : (R)b.value);
 }
 
 __device__ __forceinline__ int bc_axis(const BCDev& b) {
@@ -725,6 +795,8 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
         // (parity) and the collision
         R r, ux, uy, uz;
         mom(g, r, ux, uy, uz);
+        float jx = 0.f, jy = 0.f, jz = 0.f;  // momentum of g (FP32 offsets: the collision invariants)
+        if constexpr (OFF && !SC) momentum<Q, float>(g, jx, jy, jz);
         R* __restrict__ prev = static_cast<R*>(P.nw_prev);
         if (KIND == KIND_STEP && nw >= 0) {
             if constexpr (!OFF) {
@@ -758,7 +830,11 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
                 } else {
                     wss_from_moments(m, r, ux, uy, uz, nr, P.wss_phys_f, t);
                 }
-                t[3] = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                // |tau| through the reciprocal square root (a few ulp; the
+                // IEEE square root takes its special-case path for every
+                // zero stress, as at rest)
+                const float t2 = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+                t[3] = t2 > 0.f ? t2 * rsqrtf(t2) : 0.f;
                 // this step's slot of the ring (folded kFoldEvery steps later)
                 reinterpret_cast<float4*>(P.nw_ring)[(int64_t)slot * P.nnw + nw] = make_float4(t[0], t[1], t[2], t[3]);
             }
@@ -777,13 +853,18 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
         // ---- collide and store (every lane)
         if (MODE == MODE_PHYSICS && P.collision == LBM_COLLISION_REGULARIZED) {
             if constexpr (SC) {
+                PairSums<float> ps;
                 units_to_offsets<Q, S>(g);
-                relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f);
+                relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f, ps);
                 offsets_to_units<Q, S>(g);
             } else if constexpr (OFF) {
-                relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f);
+                // FP32: the invariants closed (the regularized values replace f: keep = 0)
+                PairSums<float> ps;
+                relax_regularized<Q, float>(g, r, 1.0f + r, ux, uy, uz, P.inv_tau_f, ps);
+                close_invariants<Q>(g, ps, 0.0f, r, jx, jy, jz);
             } else {
-                relax_regularized<Q, R>(g, r, r, ux, uy, uz, (R)P.inv_tau);
+                PairSums<R> ps;
+                relax_regularized<Q, R>(g, r, r, ux, uy, uz, (R)P.inv_tau, ps);
             }
         } else if constexpr (SC) {
             const float om = P.inv_tau_f;
@@ -792,10 +873,14 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
             const float K = om * Store<S>::geq;
             relax_pairs_units<Q>(g, A, B, ux, uy, uz, K, 3.0f * K, 1.0f - om);
         } else if constexpr (OFF) {
+            // FP32: BGK pairs, then the invariants closed (keep = 1 - omega)
             const float om = P.inv_tau_f;
+            const float om1 = 1.0f - om;
             const float A = 1.0f + r;
             const float B = r - 1.5f * A * (ux * ux + uy * uy + uz * uz);
-            relax_pairs<Q>(g, A, B, ux, uy, uz, om, 1.0f - om);
+            PairSums<float> ps;
+            relax_pairs<Q>(g, A, B, ux, uy, uz, om, om1, ps);
+            close_invariants<Q>(g, ps, om1, r, jx, jy, jz);
         } else {
             relax_all<Q, R, OFF>(g, r, ux, uy, uz, ux * ux + uy * uy + uz * uz, (R)P.inv_tau);
         }
@@ -1005,6 +1090,110 @@ __global__ void __launch_bounds__(BT, MINB) step_kernel(const StepParams P) {
         if (!P.pdl_early) pdl_trigger();
     }
     if constexpr (KIND == KIND_READOUT) block_partials<BT>(part, P.partials);
+}
+
+// ---------------------------------------------------------------------------
+// Compact step kernel: physics mode, FP32-arithmetic formats (FP32, FP16,
+// BF16), 32-bit offsets, half-way bounce-back.  The same update as
+// step_kernel (node_finish is shared, results are bit-identical), with the
+// per-node 64-bit word and boundary-list entry (12 bytes a node) replaced
+// by a block of words per warp of 32 consecutive active nodes: every lane
+// derives its pull segment and its boundary-list entry from the warp's lane
+// masks with a population count.  Pull offsets come from rows that already
+// hold q * stride + delta_q, so a population's source index is one add (or,
+// for a missing link, the node's own opposite population).
+//
+// Warp block (kWarpBlockWords words; warp w covers nodes 32 w .. 32 w + 31):
+//   0 pull segment of lane 0's node
+//   1 lane bit l (l >= 1): node l starts a new segment (segments are
+//     numbered consecutively in active order)
+//   2 next-to-wall lanes     3 wall and boundary-condition lanes
+//   4 boundary-condition lanes
+//   5 boundary-list entry of the first next-to-wall lane (next-to-wall
+//     entries come first, in active order: lane l's entry is word 5 + the
+//     next-to-wall lanes below l)
+//   6 the same for the first wall / boundary-condition lane, counted from
+//     the first entry after the next-to-wall ones
+//   7 zero
+// A lane's pull row (per-segment table) and a wall lane's missing-link mask
+// (boundary list) wait on these words: lane masks -> row -> populations,
+// the same three dependent loads as step_kernel's word -> row ->
+// populations.  Measured on the 256x192x512 bifurcation: loading the warp's
+// rows and masks beside the lane masks (prefetched to L1, or both rows in
+// registers) did not shorten the step (FP32 30.7 / 37.1 us against 30.3 us,
+// FP16 28.7 / 33.8 against 26.5 us), so the chain is not what bounds it.
+template <int Q, typename S, int BT, int MINB>
+__global__ void __launch_bounds__(BT, MINB) step_compact_kernel(const StepParams P) {
+    using R = typename Store<S>::real;
+    constexpr int DR = kDeltaRow<Q>, WB = kWarpBlockWords;
+    double part[kPartialStride];
+    uint32_t blk = blockIdx.x;
+    if (P.pdl_early) pdl_trigger();
+    if (blk < (uint32_t)P.fold_blocks) {
+        // leading blocks: the stress ring's fold
+        pdl_wait();
+        if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
+        fold_blocks_work(P, blk, BT);
+        if (!P.pdl_early) pdl_trigger();
+        return;
+    }
+    blk -= (uint32_t)P.fold_blocks;
+    {
+        // blocks from both ends of the active-node order first (step_kernel)
+        const uint32_t nm = (uint32_t)((P.nact + BT - 1) / BT);
+        blk = (blk & 1) ? nm - 1 - (blk >> 1) : (blk >> 1);
+    }
+    const uint32_t a = blk * BT + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31, bit = 1u << lane, below = bit - 1u;
+    // read-only metadata before the dependency wait; the blocks cover whole
+    // thread blocks (zero past the last node)
+    const uint32_t* wb = P.warp_block + (size_t)WB * (a >> 5);
+    const uint4 m0 = __ldg(reinterpret_cast<const uint4*>(wb));
+    const uint4 m1 = __ldg(reinterpret_cast<const uint4*>(wb) + 1);
+    const uint32_t kseg = __popc(m0.y & (below | bit));  // this lane's segment within the warp
+    const bool nw = (m0.z & bit) != 0, ot = (m0.w & bit) != 0, bc = (m1.x & bit) != 0;
+    int32_t s = 0;
+    uint32_t miss = 0;
+    float nr[3] = {0.f, 0.f, 0.f};
+    if (nw) {
+        s = (int32_t)(m1.y + __popc(m0.z & below));
+        const int32_t ns = (int32_t)P.nw_stride;
+        nr[0] = __ldg(P.nw_nf + s);
+        nr[1] = __ldg(P.nw_nf + ns + s);
+        nr[2] = __ldg(P.nw_nf + 2 * ns + s);
+    }
+    if (ot) {
+        s = (int32_t)P.nnw + (int32_t)(m1.z + __popc(m0.w & below));
+        miss = __ldg(P.sp_miss + s);
+    }
+    int32_t row[DR];
+    {
+        const int4* r4 = reinterpret_cast<const int4*>(P.seg_abs + (m0.x + kseg) * DR);
+#pragma unroll
+        for (int k = 0; k < DR / 4; ++k) {
+            const int4 v = __ldg(r4 + k);
+            row[4 * k] = v.x; row[4 * k + 1] = v.y; row[4 * k + 2] = v.z; row[4 * k + 3] = v.w;
+        }
+    }
+    pdl_wait();
+    // block 0 is a node block when there are no fold blocks
+    if (blockIdx.x == 0 && threadIdx.x == 0) *P.step_next = *P.step_base + 1;
+    if (a < (uint32_t)P.nact) {
+        const S* __restrict__ fin = static_cast<const S*>(P.fin);
+        const uint32_t st = (uint32_t)P.stride;
+        R g[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            uint32_t idx = a + (uint32_t)row[q];
+            if (q != Lat<Q>::REST && (miss & (1u << Lat<Q>::opp(q)))) idx = a + (uint32_t)Lat<Q>::opp(q) * st;
+            g[q] = Store<S>::template load<Q>(fin + idx, q);  // w_opp(q) == w_q: the same decode
+        }
+        const int slot = nw ? (int)(*P.step_base & (kRingSlots - 1)) : 0;
+        node_finish<Q, S, MODE_PHYSICS, KIND_STEP, false>(P, a, 0, s, nw || bc,
+                                                           bc ? CLS_BC0 : (ot ? CLS_WALL : CLS_FLUID), miss, g, nr,
+                                                           slot, part);
+    }
+    if (!P.pdl_early) pdl_trigger();
 }
 
 // Launch-shape variants of the step kernel, picked by the autotuner
@@ -1456,6 +1645,23 @@ cudaError_t launch_tile(const StepParams& p, cudaStream_t st) {
     return e;
 }
 
+// The compact kernel where its warp blocks exist (physics, FP32-arithmetic
+// formats, 32-bit offsets, half-way bounce-back); the flat kernel's default
+// shape elsewhere.
+template <int Q, typename S, int MODE, int BT, int MB>
+cudaError_t launch_compact(const StepParams& p, cudaStream_t st) {
+    if constexpr (Store<S>::offset && MODE == MODE_PHYSICS) {
+        if (p.warp_block && p.seg_abs && !p.sp_q && (int64_t)Q * p.stride < ((int64_t)1 << 31)) {
+            StepParams q = p;
+            q.fold_blocks = ceil_div(p.nnw, BT);
+            const int64_t nb = ceil_div(p.nact, BT);
+            if (nb <= 0) return cudaSuccess;
+            return launch_dependent(step_compact_kernel<Q, S, BT, MB>, q.fold_blocks + nb, BT, MB, q, st);
+        }
+    }
+    return launch_step_variant<Q, S, MODE, 0>(p, st);
+}
+
 template <int Q, typename S, int MODE>
 cudaError_t launch_family(int kind, int variant, const StepParams& p, cudaStream_t st) {
     if (kind == KIND_STEP) {
@@ -1464,6 +1670,8 @@ cudaError_t launch_family(int kind, int variant, const StepParams& p, cudaStream
             case 2: return launch_step_variant<Q, S, MODE, 2>(p, st);
             case 3: return launch_step_variant<Q, S, MODE, 3>(p, st);
             case 4: return launch_step_variant<Q, S, MODE, 4>(p, st);
+            case 6: return launch_compact<Q, S, MODE, 128, 10>(p, st);
+            case 7: return launch_compact<Q, S, MODE, 128, 12>(p, st);
             case 5:
                 // the tiled kernel where a plan exists (physics, FP32-arithmetic
                 // formats, 32-bit offsets, half-way bounce-back); the default
