@@ -24,10 +24,13 @@ bounded sample of full-lattice steps.
 
 At N = 1 the line's "extra" object adds secondary measurements (skipped by
 --quick or their --no-* flags): FP16 storage, D3Q27, the voxelizer's ray
-tests per second, the 384x288x768 precision comparison against an FP64 run,
-three inlet periods of the bifurcation, the 64-vessel packed ensemble, the
-learned warm start, and (with --small-ensembles) launch-bound lattices
-stepped one launch per step vs persistent launches.
+tests per second, the reference's own PV.stl case (752x583x472, its
+inlet / outlet windows and polynomial pulse), the 384x288x768 precision
+comparison against an FP64 run, three inlet periods of the bifurcation
+(with an FP64 run from a one-ulp-perturbed start as the yardstick), the
+64-vessel packed ensemble, the learned warm start, and (with
+--small-ensembles) launch-bound lattices stepped one launch per step vs
+persistent launches.
 """
 from __future__ import annotations
 
@@ -320,6 +323,53 @@ def periods_extra(capi, mask, surf, tri, origin, device, periods=3):
             "collision": "regularized", "reference": "FP64 run of the same case on the GPU",
             "f64_1ulp": "FP64 started from the initial state moved by one ulp per value (random sign)",
             "formats": res}
+
+
+def pv_extra(capi, cr, device, flush, steps=20):
+    """The reference's own workload: PV.stl (11,670 triangles; the surface
+    stored in tests/golden/pv_stl.npz) at spacing 0.05 -> a 752x583x472
+    lattice, the reference's PV inlet / outlet windows (ComplexGeometry.cpp:
+    1378-1408) with its formulas' faces, tau = 1.5 (LBM.cpp:62), the
+    polynomial pulse of Pulsatile at dt = 8e-6 (pulsatile.h:14-28,
+    Simulation.cpp:548-563), half-way bounce-back walls, D3Q19 physics mode.
+    Voxelizer time, then per-step CUDA events with the L2 flushed between
+    steps (as the headline) for FP32 and FP16 storage."""
+    from pv_dec_original_gb300 import waveform
+    d = np.load(os.path.join(ROOT, "tests", "golden", "pv_stl.npz"))
+    tri = np.ascontiguousarray(np.concatenate([d["verts"][d["faces"]].reshape(-1, 9), d["normals"]], axis=1))
+    sp = float(d["spacing"])
+    t0 = time.perf_counter()
+    mask, desc = capi.voxelize(tri, sp)
+    vox_s = time.perf_counter() - t0
+    bb = np.array(desc.bbox[:])
+    org = (bb[0], bb[2], bb[4])
+    windows = [(capi.LBM_BC_REF_INLET, "x-", -16.9538, (-191.0, -187.0), (-118.0, -114.0)),
+               (capi.LBM_BC_REF_OUTLET_YMAX, "y+", -170.016, (2.0, 5.0), (-109.0, -106.0)),
+               (capi.LBM_BC_REF_OUTLET_ZMIN, "z-", -110.0, (-27.0, -25.0), (-198.0, -195.0)),
+               (capi.LBM_BC_REF_OUTLET_ZMIN, "z-", -123.0, (-33.0, -30.0), (-189.0, -186.0))]
+    rules = [capi.bc_spec(k, f, -1, 1.0, region=(c, 1e-2, t1, t2)) for k, f, c, t1, t2 in windows]
+    table = waveform.reference_table(8e-6, 20000)
+    out = {"lattice": [int(v) for v in d["dims"]], "triangles": int(len(tri)), "voxelize_s": vox_s,
+           "fluid_points": int(mask.sum())}
+    for prec in ("f32", "f16"):
+        t0 = time.perf_counter()
+        s = capi.Solver(19, prec, capi.LBM_PHYSICS, 1.5, sp, org, 1.0, 0.9, device)
+        s.set_geometry(mask, rules)
+        s.set_normals(tri)
+        s.set_inlet_table(table)
+        setup_s = time.perf_counter() - t0
+        s.step(5)
+        best, _ = s.autotune(5)
+        ms = time_steps(cr, s, steps, flush, s.stream())
+        m = sum(ms) / len(ms)
+        act = s.counts()["active"]
+        gbs = act * BYTES_PER_LU[(19, prec)] / (m * 1e-3) / 1e9
+        out[prec] = {"active_nodes": act, "mlups": act / (m * 1e-3) / 1e6, "ms_per_step": m, "hbm_gbs": gbs,
+                     "frac_of_measured_hbm": gbs / read_peaks()[0], "variant": best, "setup_s": setup_s,
+                     "bc_nodes": s.counts()["bc"]}
+        s.close()
+    out["f16"]["speedup_vs_f32"] = out["f16"]["mlups"] / out["f32"]["mlups"]
+    return out
 
 
 def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
@@ -720,6 +770,11 @@ def run_ours(args):
             extra["voxelizer"] = {"error": str(e)}
     if extras and args.Q == 19:
         extra["d3q27"] = d3q27_extra(capi, cr, mask, surf, tri, origin, local, flush, args.steps)
+    if extras:
+        try:
+            extra["pv_case"] = pv_extra(capi, cr, local, flush)
+        except Exception as e:  # a measurement, not the benchmark: record why it is missing
+            extra["pv_case"] = {"error": str(e)}
     if extras and not args.no_precision:
         extra["precision_c3"] = precision_extra(capi, cr, local)
         extra["c2_three_periods"] = periods_extra(capi, mask, surf, tri, origin, local)

@@ -318,6 +318,17 @@ lbm_status lbm_set_persistent(lbm_handle* h, int steps_per_launch);
  * LBM_ERR_CUDA and clears the barrier; the state is then undefined until the
  * next lbm_init_*. */
 lbm_status lbm_preset_barrier(lbm_handle* h, unsigned extra_arrivals);
+/* Testing the error path of the step kernels' flags: sets the handle's flag
+ * word as a kernel would raise it, so that the next lbm_step /
+ * lbm_check_status reports it (and clears LBM_FLAG_BOUNDS).
+ * LBM_FLAG_BOUNDS is raised for real only by the bounds-checked build
+ * (pv_dec_original_gb300.build with checked=True, compiled with
+ * -DLBM_CHECK), whose step kernels test every population, pull-row and
+ * boundary-list index against its array and skip an access outside it.  No
+ * reference counterpart (the reference has no error checks). */
+#define LBM_FLAG_NONFINITE 1
+#define LBM_FLAG_BOUNDS 4
+lbm_status lbm_preset_flags(lbm_handle* h, unsigned flags);
 
 /* Launch-shape variants of the step kernel: one node per thread with
  * (block size, minimum resident blocks per SM) = (128,12) (128,10) (128,8)
@@ -348,8 +359,11 @@ lbm_status lbm_set_variant(lbm_handle* h, int variant);
  * inside the library (held by every GPU that loads it until exit), so nact
  * is limited to 4,194,304; larger inputs get LBM_ERR_ARG.  The first call on
  * a device looks the array up with that device current: make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race; serialise them.  Errors: lbm_last_global_error(). */
+ * stream capture; a device reset between calls is not supported (the
+ * looked-up address is kept for the process).  All calls share the array:
+ * calls that overlap on the GPU race; serialise them.  A CUDA error left
+ * pending by earlier work is returned as LBM_ERR_CUDA, named as earlier,
+ * with nothing launched.  Errors: lbm_last_global_error(). */
 lbm_status lbm_moment_sums_noalloc(const double* d_f, int64_t nact, int Q, double* d_out, void* stream);
 
 #ifdef __cplusplus

@@ -70,11 +70,12 @@ def _stale(obj: str, deps) -> bool:
     return any(os.path.exists(x) and os.path.getmtime(x) > t for x in deps)
 
 
-def _compile(src: str, fmad: bool, verbose: bool):
-    obj = os.path.join(OUT, os.path.basename(src).replace(".cu", ".o"))
+def _compile(src: str, fmad: bool, verbose: bool, out: str = OUT, defines=()):
+    obj = os.path.join(out, os.path.basename(src).replace(".cu", ".o"))
     if not _stale(obj, _deps(src)):
         return obj, None
     cmd = [nvcc(), "-std=c++17", "-O3", *ARCH, "-lineinfo", f"--fmad={'true' if fmad else 'false'}",
+           *[f"-D{d}" for d in defines],
            "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3",
            "-I", os.path.join(HERE, "..", "include"), "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -135,5 +136,38 @@ def build(verbose: bool = False, jobs: int = 0) -> str:
     return LIB
 
 
+CHECK_OUT = os.path.join(HERE, "_build_check")
+CHECK_LIB = os.path.join(CHECK_OUT, "liblbm_gb300.so")
+# units whose kernels carry the bounds checks (in_bounds, lbm_internal.cuh)
+CHECK_UNITS = ("step_f64.cu", "step_f32.cu", "step_f16.cu", "step_bf16.cu", "step_fast.cu", "capi.cu")
+
+
+def build_checked(jobs: int = 0) -> str:
+    """The bounds-checked library (-DLBM_CHECK): the step kernels test every
+    population, pull-row and boundary-list index before the access, skip an
+    access outside its array and raise a flag the host reports; the other
+    units are the normal build's.  Slower; for debugging and its test.
+    Bind it with LBM_LIBRARY=<path> (capi.lib_path)."""
+    build(jobs=jobs)
+    os.makedirs(CHECK_OUT, exist_ok=True)
+    jobs = jobs or min(8, os.cpu_count() or 4)
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        futs = [ex.submit(_compile, s, fm, False, CHECK_OUT, ("LBM_CHECK",)) for s, fm in UNITS if s in CHECK_UNITS]
+        res = [f.result() for f in futs]
+    errs = [e for _, e in res if e]
+    if errs:
+        raise RuntimeError("checked build failed:\n" + "\n".join(errs))
+    objs = [o for o, _ in res] + [os.path.join(OUT, s.replace(".cu", ".o")) for s, _ in UNITS if s not in CHECK_UNITS]
+    if _stale(CHECK_LIB, objs):
+        r = subprocess.run([nvcc(), "-shared", *ARCH, "-o", CHECK_LIB, *objs, "-lcudart"], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError("checked link failed:\n" + r.stderr)
+    return CHECK_LIB
+
+
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    if "--checked" in sys.argv:
+        print(build_checked())
+    else:
+        print(build(verbose="-v" in sys.argv))

@@ -22,6 +22,7 @@ MAX_BC = 256
 LBM_COLLISION_BGK = 0
 LBM_COLLISION_REGULARIZED = 1
 MAX_WAVES = 256
+LBM_FLAG_NONFINITE, LBM_FLAG_BOUNDS = 1, 4
 
 ERRORS = {-1: "LBM_ERR_ARG", -2: "LBM_ERR_CUDA", -3: "LBM_ERR_STATE", -4: "LBM_ERR_NONFINITE",
           -5: "LBM_ERR_ALLOC", -6: "LBM_ERR_IO", -7: "LBM_ERR_UNSUPPORTED"}
@@ -65,7 +66,8 @@ EXPORTS = [
     "lbm_set_waveform", "lbm_init_equilibrium",
     "lbm_init_from_macro", "lbm_step", "lbm_step_async", "lbm_check_status", "lbm_sync", "lbm_get_counts", "lbm_get_classes", "lbm_get_distributions",
     "lbm_set_distributions", "lbm_get_macro", "lbm_get_wss", "lbm_get_conservation", "lbm_save", "lbm_load",
-    "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_set_persistent", "lbm_preset_barrier", "lbm_autotune", "lbm_set_variant",
+    "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_set_persistent", "lbm_preset_barrier",
+    "lbm_preset_flags", "lbm_autotune", "lbm_set_variant",
     "lbm_moment_sums_noalloc",
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
     "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
@@ -76,7 +78,9 @@ NUM_VARIANTS = 8  # LBM_NUM_VARIANTS: lbm_autotune writes this many floats
 
 
 def lib_path() -> str:
-    return _build.LIB
+    """The library this process binds: $LBM_LIBRARY when set (e.g. the
+    bounds-checked build), else the in-tree build."""
+    return os.environ.get("LBM_LIBRARY") or _build.LIB
 
 
 def load(build_if_missing: bool = True):
@@ -130,6 +134,7 @@ def load(build_if_missing: bool = True):
     L.lbm_set_graph_steps.argtypes = [P, C.c_int]
     L.lbm_set_persistent.argtypes = [P, C.c_int]
     L.lbm_preset_barrier.argtypes = [P, C.c_uint]
+    L.lbm_preset_flags.argtypes = [P, C.c_uint]
     L.lbm_autotune.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     L.lbm_set_variant.argtypes = [P, C.c_int]
     L.lbm_moment_sums_noalloc.argtypes = [P, C.c_int64, C.c_int, P, P]
@@ -305,6 +310,10 @@ class Solver:
     def preset_barrier(self, extra_arrivals):
         """Testing: extra arrivals the persistent barrier waits for (see lbm_preset_barrier)."""
         self._c(load().lbm_preset_barrier(self.h, int(extra_arrivals)))
+
+    def preset_flags(self, flags):
+        """Testing: the kernel error flags the next step reports (see lbm_preset_flags)."""
+        self._c(load().lbm_preset_flags(self.h, int(flags)))
 
     def autotune(self, trial_steps=10):
         """Time every launch variant on a snapshot of the state; keep the fastest."""

@@ -282,6 +282,7 @@ StepParams make_params(lbm_handle* h, int kind) {
     p.seg_delta = h->seg_delta;
     p.seg_abs = h->seg_abs;
     p.warp_block = h->warp_block;
+    p.nseg = h->nseg;
     p.nact = h->g.nact;
     p.act_word = h->g.act_word;
     p.sp_of_act = h->g.sp_of_act;
@@ -364,6 +365,9 @@ int start_state(lbm_handle* h, bool reset) {
     return LBM_OK;
 }
 
+static_assert(LBM_FLAG_NONFINITE == FLAG_NONFINITE && LBM_FLAG_BOUNDS == FLAG_BOUNDS, "flag values");
+static_assert(LBM_NUM_VARIANTS == kNumVariants, "variant count");
+
 int check_flags(lbm_handle* h) {
     unsigned f = 0;
     CK(h, cudaMemcpyAsync(&f, h->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
@@ -376,6 +380,12 @@ int check_flags(lbm_handle* h) {
         return fail(h, LBM_ERR_CUDA,
                     "a step kernel's bounded wait gave up (a tiled step's bulk copy or a persistent launch's grid "
                     "barrier)");
+    }
+    if (f & FLAG_BOUNDS) {
+        CK(h, cudaMemsetAsync(h->flags, 0, sizeof(unsigned), h->st));
+        CK(h, cudaStreamSynchronize(h->st));
+        return fail(h, LBM_ERR_CUDA,
+                    "a step kernel's index fell outside its array (bounds-checked build; the access was skipped)");
     }
     if (f & FLAG_NONFINITE)
         return fail(h, LBM_ERR_NONFINITE, "a density became NaN/Inf: the run diverged (check tau and the inlet)");
@@ -1305,6 +1315,17 @@ lbm_status lbm_preset_barrier(lbm_handle* h, unsigned extra_arrivals) {
     REQUIRE(h, h->bar, LBM_ERR_STATE, "no persistent barrier: call lbm_set_persistent first");
     CK(h, cudaSetDevice(h->d.device));
     CK(h, cudaMemcpyAsync(h->bar + 1, &extra_arrivals, sizeof(unsigned), cudaMemcpyHostToDevice, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return LBM_OK;
+}
+
+lbm_status lbm_preset_flags(lbm_handle* h, unsigned flags) {
+    if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+    REQUIRE(h, h->has_geo, LBM_ERR_STATE, "set the geometry first");
+    REQUIRE(h, (flags & ~(unsigned)(FLAG_NONFINITE | FLAG_BOUNDS)) == 0, LBM_ERR_ARG,
+            "only LBM_FLAG_NONFINITE and LBM_FLAG_BOUNDS can be preset");
+    CK(h, cudaSetDevice(h->d.device));
+    CK(h, cudaMemcpyAsync(h->flags, &flags, sizeof(unsigned), cudaMemcpyHostToDevice, h->st));
     CK(h, cudaStreamSynchronize(h->st));
     return LBM_OK;
 }

@@ -13,7 +13,28 @@ namespace lbm {
 enum : uint8_t { CLS_SOLID = 0, CLS_FLUID = 1, CLS_WALL = 2, CLS_BC0 = 3, CLS_NW_BIT = 0x80, CLS_MASK = 0x7f };
 
 // Error flags raised by kernels (polled by the host after each batch).
+// FLAG_BOUNDS is raised only by the bounds-checked build (LBM_CHECK), whose
+// step kernels test every index against its array before the access and
+// skip the access when it falls outside.
 enum : unsigned { FLAG_NONFINITE = 1u, FLAG_EXACT_ZERO = 2u, FLAG_BOUNDS = 4u, FLAG_TIMEOUT = 8u };
+
+#ifdef LBM_CHECK
+constexpr bool kChecked = true;
+#else
+constexpr bool kChecked = false;
+#endif
+
+// Bounds-checked build: true when 0 <= i < n; otherwise raises FLAG_BOUNDS
+// and the caller skips the access.  Compiles to `true` elsewhere.
+__device__ __forceinline__ bool in_bounds(int64_t i, int64_t n, unsigned* flags) {
+    if constexpr (!kChecked) {
+        return true;
+    } else {
+        if (i >= 0 && i < n) return true;
+        atomicOr(flags, FLAG_BOUNDS);
+        return false;
+    }
+}
 
 // Tiled step: tiles of kTileNodes consecutive active nodes whose sources
 // are staged in shared memory by bulk copies.  Per-tile plan (int32):
@@ -61,6 +82,7 @@ struct StepParams {
     // boundary-list entries (step_kernels.cuh); null where not built
     const int32_t* seg_abs;
     const uint32_t* warp_block;
+    int64_t nseg;              // pull segments (rows of seg_delta / seg_abs)
     // one thread per active node; packed word layout in step_kernels.cuh
     int64_t nact;
     const uint64_t* act_word;

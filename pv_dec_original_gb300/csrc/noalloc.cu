@@ -21,6 +21,12 @@
 //     partials before the final sum reads them, so nothing has to start at
 //     zero, but calls that overlap on the GPU (different streams, or graphs
 //     replayed concurrently) race on it: serialise them.
+//   - The scratch address is kept per device ordinal for the life of the
+//     process; a device reset (cudaDeviceReset) between calls is not
+//     supported.
+//   - A CUDA error left pending by earlier, unrelated work is not reported
+//     as this call's: the call takes it from the runtime first, returns
+//     LBM_ERR_CUDA naming it as earlier, and launches nothing.
 //   - No cudaMalloc, cudaFree or allocating library routine is called.
 #include <cstdio>
 #include <mutex>
@@ -124,6 +130,16 @@ lbm_status lbm_moment_sums_noalloc(const double* d_f, int64_t nact, int Q, doubl
     if (nact < 0 || (nact > 0 && !d_f) || !d_out) return report(LBM_ERR_ARG, "null buffer or negative size");
     if (nact > kNoAllocMaxNodes)
         return report(LBM_ERR_ARG, "more than 4194304 nodes: exceeds the fixed scratch array of this entry point");
+    {
+        // an error of earlier work must not be read below as a failure of these launches
+        const cudaError_t earlier = cudaGetLastError();
+        if (earlier != cudaSuccess) {
+            char msg[200];
+            std::snprintf(msg, sizeof(msg), "a CUDA error from earlier work was pending (%s); nothing launched",
+                          cudaGetErrorName(earlier));
+            return report(LBM_ERR_CUDA, msg);
+        }
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return report(LBM_ERR_CUDA, "cudaGetDevice failed");
     if (dev < 0 || dev >= kMaxDevices) return report(LBM_ERR_ARG, "device ordinal beyond 63");

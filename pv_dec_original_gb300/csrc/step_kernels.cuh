@@ -35,6 +35,7 @@
 // nodes, which keep no previous value, the event is flagged instead
 // (FLAG_EXACT_ZERO) -- it needs a post-collision population of exactly zero.
 #pragma once
+#include <atomic>
 #include <type_traits>
 
 #include "lbm_internal.cuh"
@@ -620,13 +621,15 @@ __device__ __forceinline__ void fold_half(const StepParams& P, int64_t nw, int h
 // The fold blocks of a step launch (the first P.fold_blocks blocks, BT
 // threads each): at a step whose index is a multiple of kFoldEvery, fold
 // the half of the ring this step does not write.
+// Each fold thread folds next-to-wall nodes a fold-grid apart (a step
+// launch carries one fold block per kFoldNodes x block size nodes).
+constexpr int kFoldNodes = 4;
 __device__ __forceinline__ void fold_blocks_work(const StepParams& P, int64_t block, int bt) {
     const int64_t step = *P.step_base;
     if (step % kFoldEvery != 0) return;
-    const int64_t nw = block * bt + threadIdx.x;
-    if (nw >= P.nnw) return;
     const int writing = (int)((step % kRingSlots) / kFoldEvery);
-    fold_half(P, nw, 1 - writing);
+    const int64_t stride = (int64_t)(P.fold_blocks > 0 ? P.fold_blocks : gridDim.x) * bt;
+    for (int64_t nw = block * bt + threadIdx.x; nw < P.nnw; nw += stride) fold_half(P, nw, 1 - writing);
 }
 
 // The same as a kernel of its own, after a step launch without fold blocks.
@@ -726,7 +729,9 @@ __device__ __forceinline__ void node_finish(const StepParams& P, const int64_t a
         }
         if (!direct && !parity_readout) {
             if (c >= CLS_BC0) {
-                const BCDev& B = P.bct[__ldg(P.sp_bc + s)];
+                int32_t rule = __ldg(P.sp_bc + s);
+                if (!in_bounds(rule, P.nbc, P.flags)) rule = 0;
+                const BCDev& B = P.bct[rule];
                 double amp = 0.0;
                 const int64_t len = __ldg(P.wave_len + B.wave);
                 if (len > 0) {
@@ -952,7 +957,8 @@ __device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, 
     // boundary-condition and next-to-wall nodes (bounce-back is folded
     // into the loads).  The list entry is fetched before the loads.
     const bool lng = MODE == MODE_PARITY ? word_special(word) : (c >= CLS_BC0 || word_nw(word));
-    const int64_t s = lng ? (int64_t)sp_entry : 0;
+    int64_t s = lng ? (int64_t)sp_entry : 0;
+    if (lng && !in_bounds(s, P.nsp, P.flags)) s = 0;
     // FP32 formats: a next-to-wall node loads its normal now, beside the
     // populations, so the stress below waits on nothing
     float nr[3] = {0.f, 0.f, 0.f};
@@ -978,7 +984,8 @@ __device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, 
         for (int q = 0; q < Q; ++q) g[q] = Store<S>::template load<Q, CG>(fin_a + q * st, q);
     } else {
         int32_t dl[DR];
-        const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + word_segment(word) * DR);
+        const int64_t seg = in_bounds(word_segment(word), P.nseg, P.flags) ? word_segment(word) : 0;
+        const int4* __restrict__ drow = reinterpret_cast<const int4*>(P.seg_delta + seg * DR);
 #pragma unroll
         for (int k = 0; k < DR / 4; ++k) {
             const int4 v = __ldg(drow + k);
@@ -995,7 +1002,10 @@ __device__ __forceinline__ void pull_node(const StepParams& P, const int64_t a, 
             } else {
                 off = q * st + (src_missing ? 0 : dl[q]);
             }
-            g[q] = Store<S>::template load<Q, CG>(fin_a + off, q);  // w_opp(q) == w_q: same decode
+            if (in_bounds((int64_t)ai + (int64_t)off, (int64_t)Q * P.stride, P.flags))
+                g[q] = Store<S>::template load<Q, CG>(fin_a + off, q);  // w_opp(q) == w_q: same decode
+            else
+                g[q] = R(0);
         }
         if constexpr (MODE == MODE_PHYSICS && WALLS) {
             // interpolated bounce-back (the launcher picks this kernel when wall distances are set)
@@ -1157,6 +1167,7 @@ __global__ void __launch_bounds__(BT, MINB) step_compact_kernel(const StepParams
     float nr[3] = {0.f, 0.f, 0.f};
     if (nw) {
         s = (int32_t)(m1.y + __popc(m0.z & below));
+        if (!in_bounds(s, P.nnw, P.flags)) s = 0;
         const int32_t ns = (int32_t)P.nw_stride;
         nr[0] = __ldg(P.nw_nf + s);
         nr[1] = __ldg(P.nw_nf + ns + s);
@@ -1164,11 +1175,13 @@ __global__ void __launch_bounds__(BT, MINB) step_compact_kernel(const StepParams
     }
     if (ot) {
         s = (int32_t)P.nnw + (int32_t)(m1.z + __popc(m0.w & below));
+        if (!in_bounds(s, P.nsp, P.flags)) s = 0;
         miss = __ldg(P.sp_miss + s);
     }
     int32_t row[DR];
     {
-        const int4* r4 = reinterpret_cast<const int4*>(P.seg_abs + (m0.x + kseg) * DR);
+        const uint32_t seg = in_bounds((int64_t)m0.x + kseg, P.nseg, P.flags) ? m0.x + kseg : 0u;
+        const int4* r4 = reinterpret_cast<const int4*>(P.seg_abs + seg * DR);
 #pragma unroll
         for (int k = 0; k < DR / 4; ++k) {
             const int4 v = __ldg(r4 + k);
@@ -1186,7 +1199,10 @@ __global__ void __launch_bounds__(BT, MINB) step_compact_kernel(const StepParams
         for (int q = 0; q < Q; ++q) {
             uint32_t idx = a + (uint32_t)row[q];
             if (q != Lat<Q>::REST && (miss & (1u << Lat<Q>::opp(q)))) idx = a + (uint32_t)Lat<Q>::opp(q) * st;
-            g[q] = Store<S>::template load<Q>(fin + idx, q);  // w_opp(q) == w_q: the same decode
+            if (in_bounds(idx, (int64_t)Q * st, P.flags))
+                g[q] = Store<S>::template load<Q>(fin + idx, q);  // w_opp(q) == w_q: the same decode
+            else
+                g[q] = R(0);
         }
         const int slot = nw ? (int)(*P.step_base & (kRingSlots - 1)) : 0;
         node_finish<Q, S, MODE_PHYSICS, KIND_STEP, false>(P, a, 0, s, nw || bc,
@@ -1211,12 +1227,19 @@ constexpr Variant kVariants[kFlatVariants] = {{128, 12}, {128, 10}, {128, 8}, {2
 // pdl_trigger / pdl_wait); minb: the kernel's minimum resident blocks per SM.
 inline cudaError_t launch_dependent(void (*kern)(const StepParams), int64_t nblocks, int bt, int minb,
                                     const StepParams& p0, cudaStream_t st) {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // SM count per device ordinal (handles on different devices may step
+    // from different threads)
+    constexpr int kDevs = 64;
+    static std::atomic<int> sms_of[kDevs];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kDevs) return cudaErrorInvalidDevice;
+    int sms = sms_of[dev].load(std::memory_order_acquire);
+    if (sms <= 0) {
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
+        sms_of[dev].store(sms, std::memory_order_release);
     }
     StepParams p = p0;
     p.pdl_early = nblocks > (int64_t)minb * sms ? 1 : 0;
@@ -1242,7 +1265,7 @@ cudaError_t launch_step_variant(const StepParams& p, cudaStream_t st) {
     const bool walls = PHYS && p.sp_q != nullptr;  // interpolated bounce-back: one shape, (128, 8)
     const int bw = walls && narrow ? 128 : bt;
     StepParams q = p;
-    q.fold_blocks = Store<S>::offset ? ceil_div(p.nnw, bw) : 0;
+    q.fold_blocks = Store<S>::offset ? ceil_div(p.nnw, (int64_t)bw * kFoldNodes) : 0;
     const int64_t nblocks = q.fold_blocks + ceil_div(p.nact, bw);
     if (ceil_div(p.nact, bw) <= 0) return cudaSuccess;
     if (nblocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
@@ -1364,17 +1387,27 @@ __global__ void __launch_bounds__(kMultiThreads, multi_min_blocks<Q, S>())
 template <int Q, typename S, int MODE, bool WALLS>
 cudaError_t launch_multi_t(const StepPair& pp, int nsteps, unsigned* bar, cudaStream_t st) {
     auto kern = step_kernel_multi<Q, S, MODE, WALLS>;
-    static int per_sm = 0;  // resident blocks per SM of this instantiation
-    static int sms = 0;
-    if (per_sm == 0) {
-        int dev = 0, v = 0, n = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    // resident blocks per SM of this instantiation and SM count, per device
+    // ordinal (handles on different devices may step from different threads)
+    constexpr int kDevs = 64;
+    static std::atomic<int> per_sm_of[kDevs];
+    static std::atomic<int> sms_of[kDevs];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kDevs) return cudaErrorInvalidDevice;
+    int per_sm = per_sm_of[dev].load(std::memory_order_acquire);
+    int sms = sms_of[dev].load(std::memory_order_acquire);
+    if (per_sm <= 0 || sms <= 0) {
+        int v = 0, n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kMultiThreads, 0);
         if (e != cudaSuccess) return e;
         if (v <= 0 || n <= 0) return cudaErrorInvalidConfiguration;
         sms = n;
         per_sm = v;
+        sms_of[dev].store(n, std::memory_order_release);
+        per_sm_of[dev].store(v, std::memory_order_release);
     }
     if (nsteps == 0) return cudaSuccess;  // the occupancy query alone (before a stream capture)
     const StepParams& p = pp.p[0];
@@ -1617,17 +1650,20 @@ __global__ void __launch_bounds__(kTileNodes, 1) tile_step_kernel(const StepPara
 
 template <int Q, typename S, int NS>
 cudaError_t launch_tile_ns(const StepParams& p, cudaStream_t st) {
-    static int attr_bytes = 0;  // per instantiation: opt-in shared memory set so far
-    if (p.tile.smem_bytes > attr_bytes) {
-        cudaError_t e = cudaFuncSetAttribute(tile_step_kernel<Q, S, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             p.tile.smem_bytes);
-        if (e != cudaSuccess) return e;
-        attr_bytes = p.tile.smem_bytes;
-    }
+    // per instantiation and device ordinal: opt-in shared memory set so far
+    constexpr int kDevs = 64;
+    static std::atomic<int> attr_bytes[kDevs];
     int dev = 0, nsm = 1;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
-                                                   cudaSuccess || nsm <= 0)
-        nsm = 1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kDevs) return cudaErrorInvalidDevice;
+    if (p.tile.smem_bytes > attr_bytes[dev].load(std::memory_order_acquire)) {
+        e = cudaFuncSetAttribute(tile_step_kernel<Q, S, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 p.tile.smem_bytes);
+        if (e != cudaSuccess) return e;
+        attr_bytes[dev].store(p.tile.smem_bytes, std::memory_order_release);
+    }
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
     int64_t grid = (int64_t)nsm * p.tile.ctas_per_sm;
     if (grid > p.tile.ntiles) grid = p.tile.ntiles;
     tile_step_kernel<Q, S, NS><<<(unsigned)grid, kTileNodes, p.tile.smem_bytes, st>>>(p);
@@ -1653,7 +1689,7 @@ cudaError_t launch_compact(const StepParams& p, cudaStream_t st) {
     if constexpr (Store<S>::offset && MODE == MODE_PHYSICS) {
         if (p.warp_block && p.seg_abs && !p.sp_q && (int64_t)Q * p.stride < ((int64_t)1 << 31)) {
             StepParams q = p;
-            q.fold_blocks = ceil_div(p.nnw, BT);
+            q.fold_blocks = ceil_div(p.nnw, (int64_t)BT * kFoldNodes);
             const int64_t nb = ceil_div(p.nact, BT);
             if (nb <= 0) return cudaSuccess;
             return launch_dependent(step_compact_kernel<Q, S, BT, MB>, q.fold_blocks + nb, BT, MB, q, st);

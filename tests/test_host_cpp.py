@@ -98,6 +98,60 @@ def test_lbm_run_end_to_end_vs_oracle(tmp_path, gpu_lib, oracle_lib):
     near = np.argmin(((ijk[None] - g[:, None]) ** 2).sum(-1), 1)
     np.testing.assert_array_equal(vx[:, 3], csv[near, 3])
     np.testing.assert_array_equal(vx[:, 5], csv[near, 5])
+    _check_vtu(str(tmp_path / "Fluid_Variables" / "30.vtu"), mask, o)
+
+
+def _vtu_arrays(path):
+    """DataArray name -> (values, components) of an ASCII .vtu file."""
+    import re
+    txt = open(path).read()
+    out = {}
+    for m in re.finditer(r'<DataArray type="(\w+)"([^>]*)>(.*?)</DataArray>', txt, re.S):
+        typ, attrs, body = m.groups()
+        name = re.search(r'Name="(\w+)"', attrs)
+        comp = re.search(r'NumberOfComponents="(\d+)"', attrs)
+        key = name.group(1) if name else "Points"
+        dt = np.float64 if typ.startswith("Float") else np.int64
+        out[key] = (np.array(body.split(), dtype=dt), int(comp.group(1)) if comp else 1)
+    piece = re.search(r'NumberOfPoints="(\d+)" NumberOfCells="(\d+)"', txt)
+    return out, int(piece.group(1)), int(piece.group(2))
+
+
+def _check_vtu(path, mask, oracle_sim):
+    """The .vtu against the layout of WriteVTK_Collective
+    (OutputFile.cpp:259-429): every active node in point order (x fastest)
+    at its integer lattice coordinates; a hexahedron (type 12) for every
+    lattice cube whose eight corners are active, cubes in z, y, x loop order,
+    corners (x,y,z) (x+1,y,z) (x+1,y+1,z) (x,y+1,z) then the same at z+1;
+    point fields Velocity, Density and VelocityMagnitude -- here of the
+    post-boundary distributions (the oracle's f after the same steps)."""
+    arr, npts, ncell = _vtu_arrays(path)
+    nz, ny, nx = mask.shape
+    act = np.flatnonzero(mask.reshape(-1) > 0)
+    assert npts == len(act)
+    pts = arr["Points"][0].reshape(-1, 3)
+    ijk = np.stack([act % nx, (act // nx) % ny, act // (nx * ny)], 1)
+    np.testing.assert_array_equal(pts, ijk)
+    pid = np.full(mask.size, -1, np.int64)
+    pid[act] = np.arange(len(act))
+    pid = pid.reshape(nz, ny, nx)
+    corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    ids = np.stack([pid[dz:nz - 1 + dz, dy:ny - 1 + dy, dx:nx - 1 + dx] for dx, dy, dz in corners], -1)
+    cells = ids[(ids >= 0).all(-1)]  # z, y, x order of the cube loop
+    assert ncell == len(cells)
+    np.testing.assert_array_equal(arr["connectivity"][0].reshape(-1, 8), cells)
+    np.testing.assert_array_equal(arr["offsets"][0], 8 * np.arange(1, ncell + 1))
+    assert np.all(arr["types"][0] == 12)
+    f, _, _ = oracle_sim.f()
+    from oracle import oracle as O
+    c, _, _ = O.lattice(19)
+    rho = f.sum(axis=1)
+    u = (f @ c) / rho[:, None]
+    vel, ncomp = arr["Velocity"]
+    assert ncomp == 3
+    np.testing.assert_allclose(arr["Density"][0], rho, rtol=1e-13)
+    np.testing.assert_allclose(vel.reshape(-1, 3), u, rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(arr["VelocityMagnitude"][0], np.linalg.norm(u, axis=1), rtol=1e-10, atol=1e-14)
 
 
 @pytest.mark.gpu
