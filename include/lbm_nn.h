@@ -24,6 +24,19 @@ extern "C" {
 lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const void* w, const float* bias, int co,
                              int ksize, int stride, int relu, void* y, float* y_f32, void* stream);
 
+/* Convolution engine.  LBM_NN_ENGINE_AUTO (default): 3x3x3 stride-1
+ * convolutions whose grid has D % 4 == 0, H % 16 == 0 and W % 8 == 0 --
+ * the forward pass and the input gradient -- run on the tcgen05 tensor
+ * cores with tensor-memory accumulators (conv_tc.cu); the others, and the
+ * weight gradients, on mma.sync.  LBM_NN_ENGINE_MMA_SYNC: mma.sync
+ * everywhere (the comparison path).  Process-wide. */
+#define LBM_NN_ENGINE_AUTO 0
+#define LBM_NN_ENGINE_MMA_SYNC 1
+lbm_status lbm_nn_set_conv_engine(int engine);
+/* Waits for the device, then reports (LBM_ERR_CUDA) and clears a bounded
+ * wait of a tensor-core convolution that gave up since the last call. */
+lbm_status lbm_nn_conv_status(void);
+
 /* Gradients of the convolution above (before its activation): dx = dL/dx
  * (BF16, written; needs w_t, scratch of the weight's size), dw += dL/dw and
  * db += dL/db (FP32, accumulated); any of dx / dw / db may be NULL. */

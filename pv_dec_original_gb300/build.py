@@ -36,6 +36,7 @@ UNITS = [
     ("capi.cu", False),
     ("noalloc.cu", False),
     ("nn.cu", True),
+    ("conv_tc.cu", True),
 ]
 HOST_UNITS = ["host/LatticeModel.cpp", "host/GeometryReader.cpp", "host/ComplexGeometry.cpp",
               "host/Subdomain.cpp", "host/Simulation.cpp", "host/Boundary.cpp", "host/ConfigReader.cpp",

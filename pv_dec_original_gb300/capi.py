@@ -69,7 +69,8 @@ EXPORTS = [
     "lbm_get_stream", "lbm_get_launch_count", "lbm_set_graph_steps", "lbm_set_persistent", "lbm_preset_barrier",
     "lbm_preset_flags", "lbm_autotune", "lbm_set_variant",
     "lbm_moment_sums_noalloc",
-    "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
+    "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_set_conv_engine", "lbm_nn_conv_status",
+    "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
     "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
     "lbm_init_from_macro_device", "lbm_nearest_next_to_wall", "lbm_set_wall_distances", "lbm_get_wall_distances",
     "lbm_get_macro_async", "lbm_get_wss_async", "lbm_wait_outputs",
@@ -141,6 +142,8 @@ def load(build_if_missing: bool = True):
     I3 = C.POINTER(C.c_int)
     L.lbm_nn_conv3d_fwd.argtypes = [P, I3, C.c_int, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P]
     L.lbm_nn_conv3d_bwd.argtypes = [P, I3, C.c_int, P, P, C.c_int, C.c_int, C.c_int, P, P, P, P, P]
+    L.lbm_nn_set_conv_engine.argtypes = [C.c_int]
+    L.lbm_nn_conv_status.argtypes = []
     L.lbm_nn_relu_bwd.argtypes = [P, P, C.c_int64, P]
     L.lbm_nn_upsample2.argtypes = [P, I3, C.c_int, P, C.c_int, P]
     L.lbm_nn_add.argtypes = [P, P, P, C.c_int64, P]

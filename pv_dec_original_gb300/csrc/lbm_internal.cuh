@@ -233,6 +233,17 @@ constexpr int kDeltaRow = (Q + 3) / 4 * 4;
 cudaError_t nw_readout_f32(const float2* accf, const float* ring, int64_t nnw, int first, int pending, int last,
                            const float* wss_ckpt, double* out, cudaStream_t st);
 
+// 3x3x3 stride-1 convolutions of the warm-start network on tcgen05 tensor
+// cores (conv_tc.cu): shapes they take (channels 16 / 32 / 64, D % 4, H %
+// 16, W % 8 == 0), the forward convolution, the flipped-transposed weights
+// that turn the input gradient into a forward convolution, and the flag of
+// a bounded wait that gave up (read and cleared).
+bool conv3_tc_applies(int D, int H, int W, int ci, int co);
+cudaError_t conv3_tc(const void* x, int D, int H, int W, int ci, const void* w, const float* bias, int co, int relu,
+                     void* y, float* y32, cudaStream_t st);
+cudaError_t conv3_flip_transpose(const void* w, void* wt, int co, int ci, cudaStream_t st);
+cudaError_t conv_tc_status(unsigned* flags);
+
 // Message returned by lbm_last_global_error() (capi.cu).
 void set_last_global_error(const char* msg);
 

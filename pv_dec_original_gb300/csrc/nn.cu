@@ -15,6 +15,7 @@
 // Kernel size 3 (padding 1, stride 1 or 2) or 1 (stride 1).
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 
@@ -474,6 +475,16 @@ int report(const char* what, cudaError_t e) {
 
 bool padded16(int c) { return c == 16 || c == 32 || c == 64; }  // the channel counts the kernels are built for
 
+// Convolution engine (lbm_nn_set_conv_engine): tcgen05 where its shapes
+// apply, or mma.sync everywhere.
+std::atomic<int> g_engine{LBM_NN_ENGINE_AUTO};
+
+// 3x3x3, stride 1, on shapes the tensor-core kernel tiles (conv_tc.cu).
+bool use_tc(const Conv& g) {
+    return g_engine.load() == LBM_NN_ENGINE_AUTO && g.ks == 3 && g.stride == 1 &&
+           lbm::conv3_tc_applies(g.D, g.H, g.W, g.ci, g.co);
+}
+
 Conv make_conv(const int dims_in[3], int ci, int co, int ks, int stride) {
     Conv g{};
     g.D = dims_in[0]; g.H = dims_in[1]; g.W = dims_in[2];
@@ -540,9 +551,32 @@ lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const 
         return report("lbm_nn_conv3d_fwd", cudaSuccess);
     const Conv g = make_conv(dims_in, ci, co, ksize, stride);
     const int64_t rows = (int64_t)g.Do * g.Ho * g.Wo;
-    cudaError_t e = launch_gemm<0>(co, static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias,
-                                   static_cast<bf16*>(y), y_f32, g, rows, ci, relu, static_cast<cudaStream_t>(stream));
+    cudaError_t e;
+    if (use_tc(g))
+        e = lbm::conv3_tc(x, g.D, g.H, g.W, ci, w, bias, co, relu, y, y_f32, static_cast<cudaStream_t>(stream));
+    else
+        e = launch_gemm<0>(co, static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias, static_cast<bf16*>(y),
+                           y_f32, g, rows, ci, relu, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? LBM_OK : report("lbm_nn_conv3d_fwd", e);
+}
+
+lbm_status lbm_nn_set_conv_engine(int engine) {
+    if (engine != LBM_NN_ENGINE_AUTO && engine != LBM_NN_ENGINE_MMA_SYNC)
+        return report("lbm_nn_set_conv_engine", cudaSuccess);
+    g_engine.store(engine);
+    return LBM_OK;
+}
+
+lbm_status lbm_nn_conv_status(void) {
+    unsigned f = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = lbm::conv_tc_status(&f);
+    if (e != cudaSuccess) return report("lbm_nn_conv_status", e);
+    if (f) {
+        lbm::set_last_global_error("lbm_nn_conv_status: a tensor-core convolution's bounded wait gave up");
+        return LBM_ERR_CUDA;
+    }
+    return LBM_OK;
 }
 
 lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const void* w, void* w_t, int co,
@@ -555,7 +589,11 @@ lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const 
     const int taps = ksize * ksize * ksize;
     const int64_t rows_out = (int64_t)g.Do * g.Ho * g.Wo, rows_in = (int64_t)g.D * g.H * g.W;
     cudaError_t e = cudaSuccess;
-    if (dx) {
+    if (dx && use_tc(g)) {
+        // stride 1: dx is the forward convolution of dy with the flipped, transposed weights
+        e = lbm::conv3_flip_transpose(w, w_t, co, ci, st);
+        if (e == cudaSuccess) e = lbm::conv3_tc(dy, g.Do, g.Ho, g.Wo, co, w_t, nullptr, ci, 0, dx, nullptr, st);
+    } else if (dx) {
         const int64_t nw = (int64_t)co * taps * ci;
         k_transpose_w<<<grid1(nw), 256, 0, st>>>(static_cast<const bf16*>(w), static_cast<bf16*>(w_t), co, taps, ci);
         e = cudaGetLastError();
