@@ -492,120 +492,142 @@ def small_ensembles_extra(cr, device, sizes=(1, 4, 16, 64), steps=3000):
     return {"rows": rows, "timing": f"CUDA events around {steps} steps; L2 not flushed (lattices fit in L2)"}
 
 
-def warmstart_extra(device, n_train=32, n_test=6, tau=0.55, box=(64, 64, 128)):
-    """Learned warm start (scaled-down C5: 128x64x64 grids instead of
-    128x128x256, 32 training vessels of radius 8-18): train on the device, then on held-out
-    vessels the steps and wall time until the wall shear stress of an FP32
-    lattice stays within 1% of the converged WSS (an FP64 lattice from rest
-    run to the residual 1e-6), for a start from rest, from the Poiseuille
-    prior alone and from the network's prediction (prior + learned
-    correction), every lattice with the regularized collision (BGK diverges
-    at tau = 0.55 on these vessels); wall time = prediction time (all on the device) + steps x
-    the lattice's measured time per step.  Beside it: the FP64 steps to the
-    residual 1e-6 from the network's start (capped at 2x the cold count),
-    the prediction errors of the network and of the prior, and the
-    tensor-core convolution throughput of one forward pass at the full C5
-    grid."""
+def warmstart_extra(device, box=(64, 64, 128), n_train=32, n_test=6, tau=0.55, radius=(2.0, 5.0),
+                    train_iters=2000, conv=True):
+    """Learned warm start under pulsatile inlets: seeded stenosed tubes and
+    bifurcations in a D x H x W box (defaults: 128 x 64 x 64, tube radii
+    4-10 lattice units, 32 training and 6 held-out vessels; the full C5 case
+    is --warmstart-c5: 256 x 128 x 128, radii 8-20, 200 and 32), each with
+    its own waveform u(s) = mean (1 + 0.5 sin(2 pi s/T) + 0.2 sin(4 pi s/T)),
+    mean 0.01-0.04, T 2000-6000 steps.  Training targets: each training
+    vessel's converged periodic state at phase 0 (its own lattice run from
+    rest, period by period, until the cycle-to-cycle WSS change is below
+    1e-3).  On every held-out vessel, three FP32 lattices (regularized
+    collision: BGK diverges at tau = 0.55 here) start from rest (cold, as
+    the reference does), from the Poiseuille prior alone and from the
+    network's prediction, each run to its converged periodic state; the
+    figure is the first step from which the WSS stays within 1% of the cold
+    run's converged cycle at the same phase, and wall time = prediction time
+    (all on the device) + steps x the lattice's measured time per step."""
     import torch
     from pv_dec_original_gb300 import capi
     from pv_dec_original_gb300 import warmstart as WS
     rlb = capi.LBM_COLLISION_REGULARIZED
     t0 = time.perf_counter()
-    train_m = WS.vessel_members(n_train, seed=1, box=box)
-    test_m = WS.vessel_members(n_test, seed=99, box=box)
-    sols = WS.steady_ensemble(train_m, tau=tau, steps=100000, device=device, collision=rlb)
-    samples = [WS.make_sample(mask, m, rho, u, tau=tau, device=device) for (mask, rho, u), m in zip(sols, train_m)]
+    train_m = WS.vessel_members(n_train, seed=1, box=box, radius=radius)
+    test_m = WS.vessel_members(n_test, seed=99, box=box, radius=radius)
+    sols = WS.periodic_solutions(train_m, tau=tau, device=device, collision=rlb)
+    samples = [WS.make_sample(mask, dict(m, period=T), rho, u, tau=tau, device=device)
+               for (mask, rho, u, T, _, _), m in zip(sols, train_m)]
+    periods = [k for (_, _, _, _, k, _) in sols]
     data_s = time.perf_counter() - t0
     net = WS.WarmStartNet(sols[0][0].shape, device=device, seed=0)
     t0 = time.perf_counter()
-    hist = WS.train(net, samples, iters=2000, lr=2e-3, batch=4)
+    hist = WS.train(net, samples, iters=train_iters, lr=2e-3, batch=4)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     # the network's forward pass is captured once for the grid size and
     # replayed for every vessel (capture outside the timed regions)
-    x0, _ = WS.features(sols[0][0], train_m[0]["inlet_mean"], train_m[0]["period"], tau=tau, device=device)
-    net.forward_graphed(x0)
+    net.forward_graphed(samples[0][0])
     torch.cuda.synchronize()
-    rows = []
-    dev = torch.device("cuda", device)
-    for m in test_m:
-        # the converged answer: an FP64 lattice from rest to the residual 1e-6
-        sr, mask = WS.single_lattice(m, tau=tau, precision="f64", device=device, collision=rlb)
-        sr.set_graph_steps(100)
-        n64, r64 = WS.steps_to_converge(sr, tol=1e-6, max_steps=150000)
-        _, uc = sr.macro()
-        wc = sr.wss()["wss"]
-        sr.close()
-        # timed arms on FP32 lattices (the production storage)
-        sc, _ = WS.single_lattice(m, tau=tau, precision="f32", device=device, collision=rlb)
-        sc.set_graph_steps(100)
-        c1 = WS.steps_to_wss(sc, wc, 0.01, max_steps=150000)
-        t0 = time.perf_counter()
-        sc.step(2000)
-        t_step = (time.perf_counter() - t0) / 2000
-        sc.close()
-        arms = {}
-        for arm in ("prior", "net"):
-            sw, _ = WS.single_lattice(m, tau=tau, precision="f32", device=device, collision=rlb)
-            sw.set_graph_steps(100)
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            x, prior = WS.features(mask, m["inlet_mean"], m["period"], tau=tau, device=device)
-            y = net.forward_graphed(x) if arm == "net" else WS.zero_output(prior)
-            rho, u = WS.prediction_to_device(y, prior)
-            sw.init_from_macro_device(rho.data_ptr(), u.data_ptr(), True, torch.cuda.current_stream(dev).cuda_stream)
-            t_pred = time.perf_counter() - t0
-            w1 = WS.steps_to_wss(sw, wc, 0.01, max_steps=max(4 * (c1 or 0), 20000))
-            sw.close()
-            ua = u.cpu().numpy().reshape(-1, 3)
-            arms[arm] = {"steps_1pct_wss": w1, "s_1pct_wss": None if w1 is None else t_pred + w1 * t_step,
-                         "predict_s": t_pred, "err_u": float(np.linalg.norm(ua - uc) / np.linalg.norm(uc))}
-        # the residual criterion from the network's start, FP64 (capped at 2x the cold count)
-        s64, _ = WS.single_lattice(m, tau=tau, precision="f64", device=device, collision=rlb)
-        s64.set_graph_steps(100)
-        x, prior = WS.features(mask, m["inlet_mean"], m["period"], tau=tau, device=device)
-        rho, u = WS.prediction_to_device(net.forward(x), prior)
-        s64.init_from_macro_device(rho.data_ptr(), u.data_ptr(), True, torch.cuda.current_stream(dev).cuda_stream)
-        nres, rres = WS.steps_to_converge(s64, tol=1e-6, max_steps=2 * n64)
-        arms["net"]["f64_steps_residual_1e-6"] = nres if rres < 1e-6 else None
-        arms["net"]["f64_final_residual"] = rres
-        arms["net"]["f64_wss_diff_at_end"] = WS.wss_error(s64.wss()["wss"], wc)
-        s64.close()
-        rows.append({"kind": m["kind"], "active": int(mask.sum()), "f32_us_per_step": t_step * 1e6,
-                     "cold": {"steps_1pct_wss": c1, "s_1pct_wss": None if c1 is None else c1 * t_step,
-                              "f64_steps_residual_1e-6": n64, "f64_final_residual": r64},
-                     **arms})
-    # convolution throughput at the C5 grid (128x128x256), forward pass
-    big = WS.WarmStartNet((256, 128, 128), device=device, seed=0)
-    xb = torch.zeros(256 * 128 * 128 * WS.C_IN, dtype=torch.bfloat16, device=torch.device("cuda", device))
-    big.forward(xb)
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    ev[0].record(big.stream)
-    for _ in range(3):
-        big.forward(xb)
-    ev[1].record(big.stream)
-    torch.cuda.synchronize()
-    fwd_ms = ev[0].elapsed_time(ev[1]) / 3
-    flops = sum(2.0 * big.nvox(mm["lvl_out"]) * mm["co"] * mm["taps"] * mm["ci"] for mm in big.meta.values())
+    del samples
+    rows = [WS.periodic_arms(net, m, tau=tau, device=device, collision=rlb) for m in test_m]
     ok = [r for r in rows if all(r[k]["steps_1pct_wss"] is not None for k in ("cold", "prior", "net"))]
     tot = lambda arm, k: sum(r[arm][k] for r in ok)
-    return {"grid": list(sols[0][0].shape), "train_vessels": n_train, "test_vessels": n_test, "tau": tau,
-            "data_s": data_s, "train_s": train_s, "train_iters": 2000, "loss_first_last": [hist[0], hist[-1]],
-            "criterion": "FP32 lattice WSS within 1% of the converged (residual 1e-6, FP64, from rest) WSS at 3 "
-                         "checks 100 steps apart; time = prediction (features, network forward replayed from a CUDA "
-                         "graph captured once for the grid size, prior, smoothing, state build) + steps x measured "
-                         "FP32 time per step",
-            "vessels_reaching_1pct": {k: sum(r[k]["steps_1pct_wss"] is not None for r in rows)
-                                      for k in ("cold", "prior", "net")},
-            "net_over_cold_time": tot("net", "s_1pct_wss") / tot("cold", "s_1pct_wss"),
-            "prior_over_cold_time": tot("prior", "s_1pct_wss") / tot("cold", "s_1pct_wss"),
-            "net_over_cold_steps": tot("net", "steps_1pct_wss") / tot("cold", "steps_1pct_wss"),
-            "prior_over_cold_steps": tot("prior", "steps_1pct_wss") / tot("cold", "steps_1pct_wss"),
-            "per_vessel": rows,
-            "conv_forward_c5_grid": {"grid": [256, 128, 128], "ms": fwd_ms, "gflop": flops / 1e9,
-                                     "tflops": flops / (fwd_ms * 1e-3) / 1e12,
-                                     "kernel": "mma.sync m16n8k16 BF16 implicit GEMM, FP32 accumulate"}}
+    ratio = lambda a, b, k: (tot(a, k) / tot(b, k)) if ok and tot(b, k) > 0 else None
+    out = {"grid": list(sols[0][0].shape), "train_vessels": n_train, "test_vessels": n_test, "tau": tau,
+           "tube_radius_lu": [radius[0] * box[0] / 32.0, radius[1] * box[0] / 32.0],
+           "inlet": "per vessel u(s) = mean (1 + 0.5 sin(2 pi s/T) + 0.2 sin(4 pi s/T)), mean 0.01-0.04, "
+                    "T 2000-6000 steps",
+           "training_targets": "converged periodic state at phase 0 (cycle-to-cycle WSS change < 1e-3)",
+           "training_periods_run": [min(periods), max(periods)],
+           "data_s": data_s, "train_s": train_s, "train_iters": train_iters, "loss_first_last": [hist[0], hist[-1]],
+           "criterion": "FP32 lattice WSS within 1% of the cold run's converged periodic WSS at the same phase "
+                        "(checked every 100 steps) from that step on; time = prediction (features, network "
+                        "forward replayed from a CUDA graph captured once for the grid size, prior, smoothing, "
+                        "state build) + steps x measured FP32 time per step",
+           "vessels_reaching_1pct": {k: sum(r[k]["steps_1pct_wss"] is not None for r in rows)
+                                     for k in ("cold", "prior", "net")},
+           "net_over_cold_time": ratio("net", "cold", "s_1pct_wss"),
+           "prior_over_cold_time": ratio("prior", "cold", "s_1pct_wss"),
+           "net_over_cold_steps": ratio("net", "cold", "steps_1pct_wss"),
+           "prior_over_cold_steps": ratio("prior", "cold", "steps_1pct_wss"),
+           "per_vessel": rows}
+    if conv:
+        out["conv_forward_c5_grid"] = conv_forward_c5(device)
+    return out
+
+
+def conv_forward_c5(device, dims=(256, 128, 128), reps=5):
+    """One forward pass of the warm-start network at the C5 grid (128 x 128
+    x 256 voxels, random BF16 input), CUDA events around `reps` passes after
+    a warm-up pass, on each convolution engine: tcgen05 (3x3x3 stride-1
+    layers on the fifth-generation tensor cores, the others on mma.sync) and
+    mma.sync everywhere; per layer, the tcgen05 engine's time of one
+    convolution launch (10 launches timed)."""
+    import ctypes as C
+    import torch
+    from pv_dec_original_gb300 import capi
+    from pv_dec_original_gb300 import warmstart as WS
+    L = capi.load()
+    dev = torch.device("cuda", device)
+    big = WS.WarmStartNet(dims, device=device, seed=0)
+    nvox = dims[0] * dims[1] * dims[2]
+    g = torch.Generator(device=dev).manual_seed(0)
+    xb = (torch.rand(nvox * WS.C_IN, device=dev, generator=g) - 0.5).to(torch.bfloat16)
+    flops = sum(2.0 * big.nvox(mm["lvl_out"]) * mm["co"] * mm["taps"] * mm["ci"] for mm in big.meta.values())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    out = {"grid": list(dims), "gflop": flops / 1e9}
+    outputs = {}
+    try:
+        for name, engine in (("mma_sync", 1), ("tcgen05", 0)):
+            capi._check(L.lbm_nn_set_conv_engine(engine))
+            big.forward(xb)
+            torch.cuda.synchronize(dev)
+            outputs[name] = big.y32.clone()
+            ev[0].record(big.stream)
+            for _ in range(reps):
+                big.forward(xb)
+            ev[1].record(big.stream)
+            torch.cuda.synchronize(dev)
+            ms = ev[0].elapsed_time(ev[1]) / reps
+            out[name] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12}
+        layers = {}
+        y = torch.empty(nvox * 64, dtype=torch.bfloat16, device=dev)
+        for name, m in big.meta.items():
+            src = m["src"]
+            xin = big.up[name] if src.startswith("up:") else (xb if src == "x" else big.act[src])
+            w = big.wb[m["w_off"]:m["w_off"] + m["w_n"]]
+            b = big.b[m["b_off"]:m["b_off"] + m["co"]]
+            gi = big.grid(m["lvl_in"])
+            args = (C.c_void_p(xin.data_ptr()), (C.c_int * 3)(*gi), m["ci"], C.c_void_p(w.data_ptr()),
+                    C.c_void_p(b.data_ptr()), m["co"], m["ks"], m["stride"], m["relu"], C.c_void_p(y.data_ptr()),
+                    None, big.st)
+            capi._check(L.lbm_nn_conv3d_fwd(*args))
+            ev[0].record(big.stream)
+            for _ in range(10):
+                L.lbm_nn_conv3d_fwd(*args)
+            ev[1].record(big.stream)
+            torch.cuda.synchronize(dev)
+            ms = ev[0].elapsed_time(ev[1]) / 10
+            fl = 2.0 * big.nvox(m["lvl_out"]) * m["co"] * m["taps"] * m["ci"]
+            go = [v // m["stride"] for v in gi]
+            tc = m["ks"] == 3 and all(v % d == 0 for v, d in zip(go, (4 if m["stride"] == 1 else 1, 16, 8)))
+            layers[name] = {"grid": list(gi), "ci": m["ci"], "co": m["co"], "k": m["ks"], "stride": m["stride"],
+                            "engine": "tcgen05" if tc else "mma.sync", "us": ms * 1e3,
+                            "tflops": fl / (ms * 1e-3) / 1e12}
+        out["layers_tcgen05_engine"] = layers
+    finally:
+        L.lbm_nn_set_conv_engine(0)
+    capi._check(L.lbm_nn_conv_status())
+    a, b = outputs["tcgen05"], outputs["mma_sync"]
+    out["engines_output_max_rel_diff"] = float((a - b).abs().max() / b.abs().max().clamp_min(1e-30))
+    out["ms"] = out["tcgen05"]["ms"]
+    out["tflops"] = out["tcgen05"]["tflops"]
+    out["speedup_vs_mma_sync"] = out["mma_sync"]["ms"] / out["tcgen05"]["ms"]
+    out["kernel"] = ("3x3x3 layers (stride 1 and 2): tcgen05.mma kind::f16 (BF16 x BF16 -> FP32 in tensor "
+                     "memory); the 1x1 output layer: mma.sync m16n8k16 BF16 implicit GEMM, FP32 accumulate")
+    return out
 
 
 def read_peaks():
@@ -781,7 +803,9 @@ def run_ours(args):
     if extras and not args.no_ensemble:
         extra["ensemble_c4"] = ensemble_extra(capi, cr, local, args.Q)
     if extras and not args.no_warmstart:
-        extra["warmstart_c5"] = warmstart_extra(local)
+        extra["warmstart_c5"] = dict(warmstart_extra(local),
+                                     scale="C5 scaled down (128x64x64 grids, 32 + 6 vessels); the full C5 case: "
+                                           "bench.py --warmstart-c5")
     if ws == 1 and args.small_ensembles:
         extra["small_ensembles"] = small_ensembles_extra(cr, local)
 
@@ -963,10 +987,24 @@ def main():
                     help="add the launch-bound small-ensemble measurement (flat vs persistent launches)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--variant", type=int, default=None, help="force a launch shape (skips the autotuner)")
+    ap.add_argument("--conv-only", nargs=3, type=int, default=None, metavar=("D", "H", "W"),
+                    help="only the warm-start network's forward pass on a D x H x W grid (both convolution "
+                         "engines, per-layer times); prints its JSON")
+    ap.add_argument("--warmstart-c5", action="store_true",
+                    help="only the learned warm start at the full C5 case (256x128x128 grids, 200 training and 32 "
+                         "held-out vessels, pulsatile inlets); prints its JSON (about 10-20 minutes)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.conv_only:
+        from pv_dec_original_gb300 import capi
+        capi.load(build_if_missing=True)
+        print(json.dumps(conv_forward_c5(0, tuple(args.conv_only))))
+    elif args.warmstart_c5:
+        from pv_dec_original_gb300 import capi
+        capi.load(build_if_missing=True)
+        print(json.dumps(warmstart_extra(0, box=(128, 128, 256), n_train=200, n_test=32, radius=(2.0, 5.0))))
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -24,12 +24,14 @@ extern "C" {
 lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const void* w, const float* bias, int co,
                              int ksize, int stride, int relu, void* y, float* y_f32, void* stream);
 
-/* Convolution engine.  LBM_NN_ENGINE_AUTO (default): 3x3x3 stride-1
- * convolutions whose grid has D % 4 == 0, H % 16 == 0 and W % 8 == 0 --
- * the forward pass and the input gradient -- run on the tcgen05 tensor
- * cores with tensor-memory accumulators (conv_tc.cu); the others, and the
- * weight gradients, on mma.sync.  LBM_NN_ENGINE_MMA_SYNC: mma.sync
- * everywhere (the comparison path).  Process-wide. */
+/* Convolution engine.  LBM_NN_ENGINE_AUTO (default): 3x3x3 convolutions
+ * run on the tcgen05 tensor cores with tensor-memory accumulators
+ * (conv_tc.cu) -- the forward pass at stride 1 on input grids with D % 4,
+ * H % 16 and W % 8 == 0 and at stride 2 on even grids whose output has
+ * H % 16 and W % 8 == 0, and the stride-1 input gradient on the same grids;
+ * the others, and the weight gradients, on mma.sync.
+ * LBM_NN_ENGINE_MMA_SYNC: mma.sync everywhere (the comparison path).
+ * Process-wide. */
 #define LBM_NN_ENGINE_AUTO 0
 #define LBM_NN_ENGINE_MMA_SYNC 1
 lbm_status lbm_nn_set_conv_engine(int engine);

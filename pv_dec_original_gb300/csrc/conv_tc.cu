@@ -1,29 +1,38 @@
-// 3x3x3 convolutions (stride 1, padding 1) of the warm-start network on the
-// fifth-generation tensor cores: tcgen05.mma with the accumulators in tensor
-// memory.  No reference counterpart (the reference always starts from rest).
+// 3x3x3 convolutions (padding 1, stride 1 or 2) of the warm-start network
+// on the fifth-generation tensor cores: tcgen05.mma with the accumulators in
+// tensor memory.  No reference counterpart (the reference always starts
+// from rest).
 //
-// One CTA (4 warps) computes an output block of 8 (x) x 16 (y) x 4 (z)
-// voxels and all co output channels.  Per 16-channel chunk of the input it
-// stages, with cp.async, the input block plus its one-voxel halo (10 x 18 x
-// 6 voxels) and the chunk of all 27 taps' weights in shared memory, in the
-// canonical no-swizzle K-major layout of the MMA operands: core matrices of
-// 8 rows x 16 bytes (8 channels), rows 16 bytes apart.
-//   input block: [channel half k (2)][z][y][x][8 channels]
-//   weights:     [tap][co / 8][channel half k][co % 8][8 channels]
+// One CTA (4 warps) computes an output block of 8 (x) x 16 (y) x TZ (z)
+// voxels (TZ = 4 at stride 1, 1 at stride 2) and all co output channels.
+// Per 16-channel chunk of the input it stages, with cp.async, the input
+// voxels the block reads (the block plus its one-voxel halo, 10 x 18 x 6 at
+// stride 1; 17 x 33 x 3 at stride 2) and the chunk of all 27 taps' weights
+// in shared memory, in the canonical no-swizzle K-major layout of the MMA
+// operands: core matrices of 8 rows x 16 bytes (8 channels), rows 16 bytes
+// apart.
+//   input:   [channel half k (2)][z][y][x parity p (S)][x / S][8 channels]
+//   weights: [tap][co / 8][channel half k][co % 8][8 channels]
 // The 128 output voxels of one z plane (8 x by 16 y) are the M = 128 rows
-// of one MMA: row m = 8 y + x, so rows m..m+7 are 8 consecutive x (one core
-// matrix) and the 16 groups of 8 rows are 16 y rows, one input row (10
-// voxels, 160 bytes) apart -- the stride-dimension offset.  The two channel
-// halves of the K = 16 slice are one block plane apart -- the leading-
-// dimension offset.  A tap (tx, ty, tz) is then just the descriptor's start
-// address moved by tx + 10 (ty + 18 tz) voxels: the 27 taps reuse the staged
-// block with no copies.  One elected thread issues the 4 planes x 27 taps
-// MMAs of a chunk (M = 128, N = co, K = 16, BF16 x BF16 -> FP32) into four
+// of one MMA: row m = 8 y + x.  Output x reads input x = S x + tx - 1, so
+// with the input's x split by parity (stride 2: even and odd columns in
+// separate runs) rows m..m+7 are 8 consecutive staged voxels -- one core
+// matrix -- and the 16 groups of 8 rows are 16 output rows, S input rows
+// apart: the stride-dimension offset.  The two channel halves of the K = 16
+// slice are one staged block apart: the leading-dimension offset.  A tap
+// (tx, ty, tz) is just the descriptor's start address (parity tx mod S,
+// column tx / S, row ty, plane S z + tz): the 27 taps reuse the staged block
+// with no copies.  One elected thread issues the TZ planes x 27 taps MMAs of
+// a chunk (M = 128, N = co, K = 16, BF16 x BF16 -> FP32) into TZ
 // accumulators of co tensor-memory columns each and commits them to an
-// mbarrier; every wait is bounded.  The epilogue reads the accumulators
-// with tcgen05.ld (warp w owns tensor-memory lanes 32 w .. 32 w + 31, i.e.
-// rows y = 4 w .. 4 w + 3), adds the bias, applies ReLU and stores BF16
-// (and FP32 when asked) channels-last.
+// mbarrier; every wait is bounded.  The epilogue reads the accumulators with
+// tcgen05.ld (warp w owns tensor-memory lanes 32 w .. 32 w + 31, i.e. rows
+// y = 4 w .. 4 w + 3), adds the bias, applies ReLU and stores BF16 (and
+// FP32 when asked) channels-last.
+//
+// Bound: the A operand (the staged input, 4 KB per MMA) is read from shared
+// memory by every MMA, 2 co FLOP a byte; at co = 16 that operand traffic,
+// not the tensor pipe, sets the rate (see the convolution profile).
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -34,13 +43,23 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-constexpr int TX = 8, TY = 16, TZ = 4;
-constexpr int XB = TX + 2, YB = TY + 2, ZB = TZ + 2;
-constexpr int BLOCK_VOX = XB * YB * ZB;          // 1080 staged voxels
-constexpr int HALF_BYTES = BLOCK_VOX * 16;        // one channel half (8 channels) of the block
-constexpr int TILE_BYTES = 2 * HALF_BYTES;        // 34,560
+constexpr int TX = 8, TY = 16;
 constexpr int kThreads = 128;
 constexpr long kWaitLimit = 1L << 20;  // mbarrier polls (each bounded by the hardware's own time limit)
+
+// Staged geometry per stride: output planes per CTA, staged planes, rows,
+// x parities and voxels per parity run.
+template <int S>
+struct Geo {
+    static constexpr int TZ = S == 1 ? 4 : 1;
+    static constexpr int ZB = S * (TZ - 1) + 3;
+    static constexpr int YB = S * (TY - 1) + 3;
+    static constexpr int PAR = S;
+    static constexpr int XH = S == 1 ? TX + 2 : TX + 1;  // stride 2: input x = 2 xh + p, rows 0..16
+    static constexpr int VOX = ZB * YB * PAR * XH;       // staged voxels (1080 / 1782)
+    static constexpr int HALF = VOX * 16;                // bytes of one channel half
+    static constexpr int TILE = 2 * HALF;
+};
 
 // Set when a bounded wait gave up (read and cleared by conv_tc_status).
 __device__ unsigned g_conv_tc_flags;
@@ -104,32 +123,34 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
-template <int CO>
+template <int S, int CO>
 __host__ __device__ constexpr int smem_bytes() {
-    return TILE_BYTES + 27 * CO * 32 + 16;  // block, weights, mbarrier + tensor-memory address
+    return Geo<S>::TILE + 27 * CO * 32 + 16;  // input, weights, mbarrier + tensor-memory address
 }
 
-template <int CO>
+template <int S, int CO>
 __host__ __device__ constexpr uint32_t tmem_cols() {
-    return TZ * CO < 32 ? 32u : (uint32_t)(TZ * CO);  // a power of two for CO in {16, 32, 64}
+    return Geo<S>::TZ * CO < 32 ? 32u : (uint32_t)(Geo<S>::TZ * CO);  // a power of two for CO in {16, 32, 64}
 }
 
-// x [D][H][W][ci], w [co][27][ci], y [D][H][W][co]; D % 4 == 0, H % 16 == 0, W % 8 == 0.
-template <int CO>
+// x [Di][Hi][Wi][ci], w [co][27][ci], y [Do][Ho][Wo][co] with Do = Di / S
+// etc.; Do % TZ == 0, Ho % 16 == 0, Wo % 8 == 0 (the launcher checks).
+template <int S, int CO>
 __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ x, const bf16* __restrict__ w,
                                                        const float* __restrict__ bias, bf16* __restrict__ y,
-                                                       float* __restrict__ y32, int D, int H, int W, int ci,
-                                                       int relu) {
+                                                       float* __restrict__ y32, int Di, int Hi, int Wi, int Do,
+                                                       int Ho, int Wo, int ci, int relu) {
+    using G = Geo<S>;
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char* tile = smem;
-    unsigned char* wsm = smem + TILE_BYTES;
+    unsigned char* wsm = smem + G::TILE;
     uint64_t* bar = reinterpret_cast<uint64_t*>(wsm + 27 * CO * 32);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nbx = W / TX, nby = H / TY;
+    const int nbx = Wo / TX, nby = Ho / TY;
     const int bx = blockIdx.x % nbx, by = (blockIdx.x / nbx) % nby, bz = blockIdx.x / (nbx * nby);
-    const int x0 = bx * TX, y0 = by * TY, z0 = bz * TZ;
-    constexpr uint32_t NCOL = tmem_cols<CO>();
+    const int x0 = bx * TX, y0 = by * TY, z0 = bz * G::TZ;
+    constexpr uint32_t NCOL = tmem_cols<S, CO>();
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(tslot)),
@@ -148,18 +169,20 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
 
     const uint32_t tile_a = saddr(tile), w_a = saddr(wsm);
     constexpr uint32_t IDESC = idesc_bf16(128, CO);
+    constexpr uint32_t SBO = S * G::PAR * G::XH * 16;  // S input rows per output row
     bool ok = true;
     const int chunks = ci / 16;
     int c = 0;
     for (; c < chunks && ok; ++c) {
-        // stage the input block (zero outside the grid: the padding) and the weights of this chunk
-        for (int i = tid; i < 2 * BLOCK_VOX; i += kThreads) {
+        // stage the input voxels (zero outside the grid: the padding) and the weights of this chunk
+        for (int i = tid; i < 2 * G::VOX; i += kThreads) {
             const int v = i >> 1, k = i & 1;
-            const int xx = v % XB, yy = (v / XB) % YB, zz = v / (XB * YB);
-            const int gx = x0 - 1 + xx, gy = y0 - 1 + yy, gz = z0 - 1 + zz;
-            const bool in = gx >= 0 && gy >= 0 && gz >= 0 && gx < W && gy < H && gz < D;
-            const bf16* src = in ? x + (((int64_t)gz * H + gy) * W + gx) * ci + c * 16 + k * 8 : x;
-            cp_async16(tile_a + k * HALF_BYTES + v * 16, src, in);
+            const int xh = v % G::XH, p = (v / G::XH) % G::PAR, yy = (v / (G::XH * G::PAR)) % G::YB,
+                      zz = v / (G::XH * G::PAR * G::YB);
+            const int gx = S * x0 - 1 + S * xh + p, gy = S * y0 - 1 + yy, gz = S * z0 - 1 + zz;
+            const bool in = gx >= 0 && gy >= 0 && gz >= 0 && gx < Wi && gy < Hi && gz < Di;
+            const bf16* src = in ? x + (((int64_t)gz * Hi + gy) * Wi + gx) * ci + c * 16 + k * 8 : x;
+            cp_async16(tile_a + k * G::HALF + v * 16, src, in);
         }
         for (int i = tid; i < 27 * CO * 2; i += kThreads) {
             const int k = i & 1, n = (i >> 1) % CO, t = (i >> 1) / CO;
@@ -171,11 +194,12 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int z = 0; z < TZ; ++z) {
+            for (int z = 0; z < G::TZ; ++z) {
                 for (int t = 0; t < 27; ++t) {
                     const int tz = t / 9, ty = (t / 3) % 3, tx = t % 3;
-                    const uint32_t a = tile_a + (((z + tz) * YB + ty) * XB + tx) * 16;
-                    const uint64_t ad = smem_desc(a, HALF_BYTES, XB * 16);
+                    const int zz = S * z + tz, p = tx % S, xo = tx / S;
+                    const uint32_t a = tile_a + (((zz * G::YB + ty) * G::PAR + p) * G::XH + xo) * 16;
+                    const uint64_t ad = smem_desc(a, G::HALF, SBO);
                     const uint64_t bd = smem_desc(w_a + t * (CO * 32), 128, 256);
                     mma_bf16(tmem + (uint32_t)(z * CO), ad, bd, IDESC, (c > 0 || t > 0) ? 1u : 0u);
                 }
@@ -193,8 +217,8 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
         // epilogue: warp w reads lanes 32 w .. 32 w + 31 = rows y = 4 w + lane / 8, x = lane % 8
         const int m = 32 * warp + lane;
         const int gx = x0 + (m & 7), gy = y0 + (m >> 3);
-        for (int z = 0; z < TZ; ++z) {
-            const int64_t vox = ((int64_t)(z0 + z) * H + gy) * W + gx;
+        for (int z = 0; z < G::TZ; ++z) {
+            const int64_t vox = ((int64_t)(z0 + z) * Ho + gy) * Wo + gx;
 #pragma unroll
             for (int c16 = 0; c16 < CO / 16; ++c16) {
                 float v[16];
@@ -239,45 +263,63 @@ __global__ void k_flip_transpose(const bf16* __restrict__ w, bf16* __restrict__ 
     wt[((int64_t)c * 27 + (26 - t)) * co + o] = w[e];
 }
 
-template <int CO>
-cudaError_t launch_co(const bf16* x, const bf16* w, const float* bias, bf16* y, float* y32, int D, int H, int W,
+template <int S, int CO>
+cudaError_t launch_co(const bf16* x, const bf16* w, const float* bias, bf16* y, float* y32, int Di, int Hi, int Wi,
                       int ci, int relu, cudaStream_t st) {
-    constexpr int bytes = smem_bytes<CO>();
+    constexpr int bytes = smem_bytes<S, CO>();
     static_assert(bytes <= 227 * 1024, "shared memory");
-    cudaError_t e = cudaFuncSetAttribute(k_conv3_tc<CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_conv3_tc<S, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    const int64_t blocks = (int64_t)(W / TX) * (H / TY) * (D / TZ);
-    k_conv3_tc<CO><<<(unsigned)blocks, kThreads, bytes, st>>>(x, w, bias, y, y32, D, H, W, ci, relu);
+    const int Do = Di / S, Ho = Hi / S, Wo = Wi / S;
+    const int64_t blocks = (int64_t)(Wo / TX) * (Ho / TY) * (Do / Geo<S>::TZ);
+    k_conv3_tc<S, CO><<<(unsigned)blocks, kThreads, bytes, st>>>(x, w, bias, y, y32, Di, Hi, Wi, Do, Ho, Wo, ci,
+                                                                 relu);
     return cudaGetLastError();
 }
 
 // Resident CTAs per SM times their tensor-memory columns must fit the 512
 // columns of an SM (an allocation that cannot be met waits for another
 // CTA's release): shared memory bounds the residency below that here --
-// (co = 16) 4 x 64, (32) 3 x 128, (64) 2 x 256 columns.
-static_assert((227 * 1024 / smem_bytes<16>()) * tmem_cols<16>() <= 512, "tensor memory (co 16)");
-static_assert((227 * 1024 / smem_bytes<32>()) * tmem_cols<32>() <= 512, "tensor memory (co 32)");
-static_assert((227 * 1024 / smem_bytes<64>()) * tmem_cols<64>() <= 512, "tensor memory (co 64)");
+// stride 1: (co = 16) 4 x 64, (32) 3 x 128, (64) 2 x 256 columns; stride 2:
+// at most 3 x 32, 2 x 32, 2 x 64.
+template <int S, int CO>
+constexpr bool tmem_fits() {
+    return (227 * 1024 / smem_bytes<S, CO>()) * tmem_cols<S, CO>() <= 512;
+}
+static_assert(tmem_fits<1, 16>() && tmem_fits<1, 32>() && tmem_fits<1, 64>(), "tensor memory (stride 1)");
+static_assert(tmem_fits<2, 16>() && tmem_fits<2, 32>() && tmem_fits<2, 64>(), "tensor memory (stride 2)");
+
+template <int S>
+cudaError_t launch_s(const void* x, int Di, int Hi, int Wi, int ci, const void* w, const float* bias, int co,
+                     int relu, void* y, float* y32, cudaStream_t st) {
+    const bf16* xb = static_cast<const bf16*>(x);
+    const bf16* wb = static_cast<const bf16*>(w);
+    bf16* yb = static_cast<bf16*>(y);
+    switch (co) {
+        case 16: return launch_co<S, 16>(xb, wb, bias, yb, y32, Di, Hi, Wi, ci, relu, st);
+        case 32: return launch_co<S, 32>(xb, wb, bias, yb, y32, Di, Hi, Wi, ci, relu, st);
+        default: return launch_co<S, 64>(xb, wb, bias, yb, y32, Di, Hi, Wi, ci, relu, st);
+    }
+}
 
 }  // namespace
 
 namespace lbm {
 
-bool conv3_tc_applies(int D, int H, int W, int ci, int co) {
+bool conv3_tc_applies(int D, int H, int W, int ci, int co, int stride) {
     const bool ch = (ci == 16 || ci == 32 || ci == 64) && (co == 16 || co == 32 || co == 64);
-    return ch && D > 0 && H > 0 && W > 0 && D % TZ == 0 && H % TY == 0 && W % TX == 0;
+    if (!ch || D <= 0 || H <= 0 || W <= 0) return false;
+    if (stride == 1) return D % Geo<1>::TZ == 0 && H % TY == 0 && W % TX == 0;
+    if (stride == 2)
+        return D % 2 == 0 && H % 2 == 0 && W % 2 == 0 && (D / 2) % Geo<2>::TZ == 0 && (H / 2) % TY == 0 &&
+               (W / 2) % TX == 0;
+    return false;
 }
 
 cudaError_t conv3_tc(const void* x, int D, int H, int W, int ci, const void* w, const float* bias, int co, int relu,
-                     void* y, float* y32, cudaStream_t st) {
-    const bf16* xb = static_cast<const bf16*>(x);
-    const bf16* wb = static_cast<const bf16*>(w);
-    bf16* yb = static_cast<bf16*>(y);
-    switch (co) {
-        case 16: return launch_co<16>(xb, wb, bias, yb, y32, D, H, W, ci, relu, st);
-        case 32: return launch_co<32>(xb, wb, bias, yb, y32, D, H, W, ci, relu, st);
-        default: return launch_co<64>(xb, wb, bias, yb, y32, D, H, W, ci, relu, st);
-    }
+                     void* y, float* y32, int stride, cudaStream_t st) {
+    return stride == 2 ? launch_s<2>(x, D, H, W, ci, w, bias, co, relu, y, y32, st)
+                       : launch_s<1>(x, D, H, W, ci, w, bias, co, relu, y, y32, st);
 }
 
 cudaError_t conv3_flip_transpose(const void* w, void* wt, int co, int ci, cudaStream_t st) {

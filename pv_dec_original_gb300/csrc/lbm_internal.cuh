@@ -233,14 +233,16 @@ constexpr int kDeltaRow = (Q + 3) / 4 * 4;
 cudaError_t nw_readout_f32(const float2* accf, const float* ring, int64_t nnw, int first, int pending, int last,
                            const float* wss_ckpt, double* out, cudaStream_t st);
 
-// 3x3x3 stride-1 convolutions of the warm-start network on tcgen05 tensor
-// cores (conv_tc.cu): shapes they take (channels 16 / 32 / 64, D % 4, H %
-// 16, W % 8 == 0), the forward convolution, the flipped-transposed weights
-// that turn the input gradient into a forward convolution, and the flag of
-// a bounded wait that gave up (read and cleared).
-bool conv3_tc_applies(int D, int H, int W, int ci, int co);
+// 3x3x3 convolutions of the warm-start network on tcgen05 tensor cores
+// (conv_tc.cu): the shapes they take (channels 16 / 32 / 64; input grid D x
+// H x W with, at stride 1, D % 4, H % 16, W % 8 == 0, at stride 2 even
+// dimensions and H / 2 % 16, W / 2 % 8 == 0), the forward convolution, the
+// flipped-transposed weights that turn a stride-1 input gradient into a
+// forward convolution, and the flag of a bounded wait that gave up (read
+// and cleared).
+bool conv3_tc_applies(int D, int H, int W, int ci, int co, int stride);
 cudaError_t conv3_tc(const void* x, int D, int H, int W, int ci, const void* w, const float* bias, int co, int relu,
-                     void* y, float* y32, cudaStream_t st);
+                     void* y, float* y32, int stride, cudaStream_t st);
 cudaError_t conv3_flip_transpose(const void* w, void* wt, int co, int ci, cudaStream_t st);
 cudaError_t conv_tc_status(unsigned* flags);
 

@@ -253,6 +253,78 @@ __global__ void k_up2_bwd(const bf16* __restrict__ dout, bf16* __restrict__ din,
     din[e] = __float2bfloat16(s);
 }
 
+// The same element-wise kernels on 8 BF16 values (16 bytes) a thread, for
+// 16-byte aligned tensors whose channel count (or length) is a multiple of
+// 8: one index computation and one load / store instruction per 8 values
+// (the one-value kernels spend their time on 64-bit index division).  The
+// arithmetic per value is the one-value kernels', so results are identical.
+union V8 {
+    uint4 u;
+    __nv_bfloat16 h[8];
+};
+
+__global__ void k_up2_v8(const uint4* __restrict__ in, uint4* __restrict__ out, int D, int H, int W, int c8) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)8 * D * H * W * c8;
+    if (e >= n) return;
+    const int ch = (int)(e % c8);
+    const int64_t v = e / c8;
+    const int x = (int)(v % (2 * W));
+    const int64_t r = v / (2 * W);
+    const int y = (int)(r % (2 * H)), z = (int)(r / (2 * H));
+    out[e] = in[(((int64_t)(z >> 1) * H + (y >> 1)) * W + (x >> 1)) * c8 + ch];
+}
+
+__global__ void k_up2_bwd_v8(const uint4* __restrict__ dout, uint4* __restrict__ din, int D, int H, int W, int c8) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)D * H * W * c8;
+    if (e >= n) return;
+    const int ch = (int)(e % c8);
+    const int64_t v = e / c8;
+    const int x = (int)(v % W);
+    const int64_t r = v / W;
+    const int y = (int)(r % H), z = (int)(r / H);
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int zz = 2 * z + (k >> 2), yy = 2 * y + ((k >> 1) & 1), xx = 2 * x + (k & 1);
+        V8 a;
+        a.u = dout[(((int64_t)zz * 2 * H + yy) * 2 * W + xx) * c8 + ch];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s[j] += __bfloat162float(a.h[j]);
+    }
+    V8 o;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) o.h[j] = __float2bfloat16(s[j]);
+    din[e] = o.u;
+}
+
+__global__ void k_add_v8(const uint4* __restrict__ a, const uint4* __restrict__ b, uint4* __restrict__ out,
+                         int64_t n8) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n8) return;
+    V8 x, y, o;
+    x.u = a[e];
+    y.u = b[e];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) o.h[j] = __float2bfloat16(__bfloat162float(x.h[j]) + __bfloat162float(y.h[j]));
+    out[e] = o.u;
+}
+
+__global__ void k_relu_bwd_v8(const uint4* __restrict__ y, uint4* __restrict__ dy, int64_t n8) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n8) return;
+    V8 a, g;
+    a.u = y[e];
+    g.u = dy[e];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (!(__bfloat162float(a.h[j]) > 0.f)) g.h[j] = __float2bfloat16(0.f);
+    dy[e] = g.u;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 // out = a + b (BF16, FP32 add)
 __global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf16* __restrict__ out, int64_t n) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -479,11 +551,13 @@ bool padded16(int c) { return c == 16 || c == 32 || c == 64; }  // the channel c
 // apply, or mma.sync everywhere.
 std::atomic<int> g_engine{LBM_NN_ENGINE_AUTO};
 
-// 3x3x3, stride 1, on shapes the tensor-core kernel tiles (conv_tc.cu).
+// 3x3x3 on shapes the tensor-core kernel tiles (conv_tc.cu): the forward
+// convolution at stride 1 or 2, the input gradient at stride 1.
 bool use_tc(const Conv& g) {
-    return g_engine.load() == LBM_NN_ENGINE_AUTO && g.ks == 3 && g.stride == 1 &&
-           lbm::conv3_tc_applies(g.D, g.H, g.W, g.ci, g.co);
+    return g_engine.load() == LBM_NN_ENGINE_AUTO && g.ks == 3 &&
+           lbm::conv3_tc_applies(g.D, g.H, g.W, g.ci, g.co, g.stride);
 }
+bool use_tc_dx(const Conv& g) { return g.stride == 1 && use_tc(g); }
 
 Conv make_conv(const int dims_in[3], int ci, int co, int ks, int stride) {
     Conv g{};
@@ -553,7 +627,8 @@ lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const 
     const int64_t rows = (int64_t)g.Do * g.Ho * g.Wo;
     cudaError_t e;
     if (use_tc(g))
-        e = lbm::conv3_tc(x, g.D, g.H, g.W, ci, w, bias, co, relu, y, y_f32, static_cast<cudaStream_t>(stream));
+        e = lbm::conv3_tc(x, g.D, g.H, g.W, ci, w, bias, co, relu, y, y_f32, g.stride,
+                          static_cast<cudaStream_t>(stream));
     else
         e = launch_gemm<0>(co, static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias, static_cast<bf16*>(y),
                            y_f32, g, rows, ci, relu, static_cast<cudaStream_t>(stream));
@@ -589,10 +664,10 @@ lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const 
     const int taps = ksize * ksize * ksize;
     const int64_t rows_out = (int64_t)g.Do * g.Ho * g.Wo, rows_in = (int64_t)g.D * g.H * g.W;
     cudaError_t e = cudaSuccess;
-    if (dx && use_tc(g)) {
+    if (dx && use_tc_dx(g)) {
         // stride 1: dx is the forward convolution of dy with the flipped, transposed weights
         e = lbm::conv3_flip_transpose(w, w_t, co, ci, st);
-        if (e == cudaSuccess) e = lbm::conv3_tc(dy, g.Do, g.Ho, g.Wo, co, w_t, nullptr, ci, 0, dx, nullptr, st);
+        if (e == cudaSuccess) e = lbm::conv3_tc(dy, g.Do, g.Ho, g.Wo, co, w_t, nullptr, ci, 0, dx, nullptr, 1, st);
     } else if (dx) {
         const int64_t nw = (int64_t)co * taps * ci;
         k_transpose_w<<<grid1(nw), 256, 0, st>>>(static_cast<const bf16*>(w), static_cast<bf16*>(w_t), co, taps, ci);
@@ -621,8 +696,11 @@ lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const 
 lbm_status lbm_nn_relu_bwd(const void* y, void* dy, int64_t n, void* stream) {
     if (!y || !dy || n < 0) return report("lbm_nn_relu_bwd", cudaSuccess);
     if (n == 0) return LBM_OK;
-    k_relu_bwd<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(y),
-                                                                        static_cast<bf16*>(dy), n);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n % 8 == 0 && aligned16(y) && aligned16(dy))
+        k_relu_bwd_v8<<<grid1(n / 8), 256, 0, st>>>(static_cast<const uint4*>(y), static_cast<uint4*>(dy), n / 8);
+    else
+        k_relu_bwd<<<grid1(n), 256, 0, st>>>(static_cast<const bf16*>(y), static_cast<bf16*>(dy), n);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? LBM_OK : report("lbm_nn_relu_bwd", e);
 }
@@ -631,7 +709,15 @@ lbm_status lbm_nn_upsample2(const void* x, const int dims_in[3], int c, void* y,
     if (!x || !dims_in || !y || c <= 0) return report("lbm_nn_upsample2", cudaSuccess);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t n = (int64_t)dims_in[0] * dims_in[1] * dims_in[2] * c;
-    if (!adjoint)
+    if (c % 8 == 0 && aligned16(x) && aligned16(y)) {
+        const int c8 = c / 8;
+        if (!adjoint)
+            k_up2_v8<<<grid1(n), 256, 0, st>>>(static_cast<const uint4*>(x), static_cast<uint4*>(y), dims_in[0],
+                                               dims_in[1], dims_in[2], c8);
+        else
+            k_up2_bwd_v8<<<grid1(n / 8), 256, 0, st>>>(static_cast<const uint4*>(x), static_cast<uint4*>(y),
+                                                       dims_in[0], dims_in[1], dims_in[2], c8);
+    } else if (!adjoint)
         k_up2<<<grid1(8 * n), 256, 0, st>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), dims_in[0],
                                             dims_in[1], dims_in[2], c);
     else  // x = gradient of the upsampled tensor, y = gradient of the coarse one (dims_in)
@@ -644,9 +730,13 @@ lbm_status lbm_nn_upsample2(const void* x, const int dims_in[3], int c, void* y,
 lbm_status lbm_nn_add(const void* a, const void* b, void* out, int64_t n, void* stream) {
     if (!a || !b || !out || n < 0) return report("lbm_nn_add", cudaSuccess);
     if (n == 0) return LBM_OK;
-    k_add<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(a),
-                                                                   static_cast<const bf16*>(b),
-                                                                   static_cast<bf16*>(out), n);
+    if (n % 8 == 0 && aligned16(a) && aligned16(b) && aligned16(out))
+        k_add_v8<<<grid1(n / 8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const uint4*>(a), static_cast<const uint4*>(b), static_cast<uint4*>(out), n / 8);
+    else
+        k_add<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(a),
+                                                                       static_cast<const bf16*>(b),
+                                                                       static_cast<bf16*>(out), n);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? LBM_OK : report("lbm_nn_add", e);
 }

@@ -374,11 +374,13 @@ def zero_output(prior):
     return torch.zeros(prior.n * C_OUT, dtype=torch.float32, device=prior.dev)
 
 
-def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4):
+def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4, radius=(4.0, 9.0), period=(2000.0, 6000.0)):
     """Seeded stenosed tubes (and every k-th a small Y-bifurcation) filling
-    a fixed box (x, y, z) between an inlet at z = 0 and an outlet at z = top;
-    radii scale with the box width (4-9 lattice units for tubes, 4-5.5 for
-    bifurcation parents at a width of 32)."""
+    a fixed box (x, y, z) between an inlet at z = 0 and an outlet at z = top,
+    each with its own inlet waveform (mean 0.01-0.04, period drawn from
+    `period` steps).  Tube radii are drawn from `radius` (lattice units at a
+    box width of 32, scaled with the width); bifurcation parents from its
+    lower end to 0.7 of the way up."""
     from . import geometry as G
     rng = np.random.default_rng(seed)
     nx, ny, nz = box
@@ -386,15 +388,15 @@ def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4):
     out = []
     for m in range(n):
         mean = float(rng.uniform(0.01, 0.04))
-        period = float(rng.uniform(2000.0, 6000.0))
+        per = float(rng.uniform(*period))
         cx, cy = 0.5 * (nx - 1) + 0.173, 0.5 * (ny - 1) + 0.061
         if bifurcation_every and m % bifurcation_every == bifurcation_every - 1:
-            r = float(rng.uniform(4.0, 5.5)) * sc
+            r = float(rng.uniform(radius[0], radius[0] + 0.3 * (radius[1] - radius[0]))) * sc
             s = G.y_bifurcation(r, 0.72 * r, float(rng.uniform(8.0, 14.0)), z_in=1.3, z_out=nz - 1.4,
                                 z_split=0.5 * nz, center=(cx, cy), seed=seed * 1000 + m, h=1.0)
             kind = "bifurcation"
         else:
-            r = float(rng.uniform(4.0, 9.0)) * sc
+            r = float(rng.uniform(*radius)) * sc
             s = G.stenosed_tube(r, nz - 2.7, float(rng.uniform(0.2, 0.7)), float(rng.uniform(0.0, 0.3)),
                                 center=(cx, cy), z0=1.3, seed=seed * 1000 + m, h=max(1.0, r / 8.0))
             kind = "stenosed_tube"
@@ -404,7 +406,7 @@ def vessel_members(n, seed, box=(32, 32, 64), bifurcation_every=4):
         meta = dict(s.meta)
         s = G.add_bbox_anchors(s, (0.0, 0.0, 0.0), (nx - 1.0, ny - 1.0, float(nz)))
         s.meta = meta
-        out.append({"surface": s, "radius": r, "center": (cx, cy), "inlet_mean": mean, "period": period,
+        out.append({"surface": s, "radius": r, "center": (cx, cy), "inlet_mean": mean, "period": per,
                     "kind": kind})
     return out
 
@@ -514,6 +516,129 @@ def single_lattice(member, tau=0.8, precision="f64", device=0, collision=0):
     s.set_normals(tri)
     s.set_inlet_table([member["inlet_mean"]])
     return s, mask
+
+
+def pulsatile_lattice(member, tau=0.55, precision="f32", device=0, collision=0, check=100):
+    """One member as its own lattice driven by its own waveform
+    u(s) = mean (1 + 0.5 sin(2 pi s / T) + 0.2 sin(4 pi s / T)), T = its
+    period rounded to a multiple of `check` steps; step 0 is phase 0, where
+    the inlet is at its mean (the Poiseuille prior's amplitude).  Returns
+    (solver, mask, T)."""
+    from . import waveform
+    T = int(check * max(1, round(member["period"] / check)))
+    s, mask = single_lattice(member, tau, precision, device, collision)
+    s.set_inlet_table(waveform.sinusoid_table(member["inlet_mean"], T))
+    return s, mask, T
+
+
+def run_periods(solver, T, check=100, tol=1e-3, max_periods=30, min_periods=2, keep=True):
+    """Steps a pulsatile lattice period by period, reading the wall shear
+    stress after every `check` steps, until the cycle-to-cycle change -- the
+    largest over the phases of |w_k(phase) - w_k-1(phase)| / |w_k-1(phase)|
+    -- is below `tol` (the converged periodic state) or max_periods have
+    run.  The lattice then stands at phase 0.  Returns (history [(step,
+    wss)] -- every check if `keep`, else the last two periods --, periods
+    run, last change)."""
+    nph = T // check
+    hist, change, k = [], float("inf"), 0
+    n0 = solver.counts()["steps"]
+    for k in range(1, max_periods + 1):
+        for _ in range(nph):
+            solver.step(check)
+            hist.append((solver.counts()["steps"] - n0, solver.wss()["wss"].astype(np.float32)))
+        if not keep and len(hist) > 2 * nph:
+            del hist[:len(hist) - 2 * nph]
+        if k >= 2:
+            change = max(wss_error(hist[-nph + j][1], hist[-2 * nph + j][1]) for j in range(nph))
+            if change < tol and k >= min_periods:
+                break
+    return hist, k, change
+
+
+def first_within_periodic(hist, ref_cycle, T, check=100, tol=0.01):
+    """First step of a (step, wss) history from which the WSS stays within
+    `tol` of the converged cycle's WSS at the same phase (ref_cycle: the
+    wss of one period, one entry per check, the first after `check` steps
+    of it); None if it never settles there."""
+    nph = T // check
+    ok = None
+    for n, w in hist:
+        if wss_error(w, ref_cycle[(n // check - 1) % nph]) < tol:
+            ok = n if ok is None else ok
+        else:
+            ok = None
+    return ok
+
+
+def periodic_solutions(members, tau=0.55, precision="f32", device=0, collision=0, check=100, tol=1e-3,
+                       max_periods=30):
+    """The converged periodic state at phase 0 of every member (each on its
+    own lattice from rest, run_periods): per member (mask, rho, u, period T
+    in steps, periods run, last cycle-to-cycle change)."""
+    out = []
+    for m in members:
+        s, mask, T = pulsatile_lattice(m, tau, precision, device, collision, check)
+        s.set_graph_steps(check)
+        _, k, ch = run_periods(s, T, check, tol, max_periods, keep=False)
+        rho, u = s.macro()
+        s.close()
+        out.append((mask, rho, u, T, k, ch))
+    return out
+
+
+def periodic_arms(net, member, tau=0.55, device=0, collision=0, check=100, tol=1e-3, max_periods=30,
+                  wss_tol=0.01):
+    """One held-out member's pulsatile lattice (FP32) started three ways --
+    from rest (cold, as the reference always starts), from the Poiseuille
+    prior alone, and from the network's prediction (prior + learned
+    correction) -- each run to its converged periodic state (run_periods).
+    The cold run's last period is the reference.  Per arm: the first step
+    from which the WSS stays within wss_tol of the reference at the same
+    phase, the periods run, the prediction time (features, network forward
+    replayed from its CUDA graph, prior, smoothing and state build, all on
+    the device; the caller captures the graph first) and the wall time =
+    prediction + steps x the lattice's measured time per step."""
+    import time
+    torch = _torch()
+    dev = torch.device("cuda", device)
+    sc, mask, T = pulsatile_lattice(member, tau, "f32", device, collision, check)
+    sc.set_graph_steps(check)
+    hist, kc, chc = run_periods(sc, T, check, tol, max_periods)
+    nph = T // check
+    ref = [w for _, w in hist[-nph:]]
+    c1 = first_within_periodic(hist, ref, T, check, wss_tol)
+    _, uc = sc.macro()
+    sc.step(check)
+    sc.sync()
+    t0 = time.perf_counter()
+    sc.step(10 * check)
+    sc.sync()
+    t_step = (time.perf_counter() - t0) / (10 * check)
+    sc.close()
+    row = {"kind": member["kind"], "radius": member["radius"], "period": T, "inlet_mean": member["inlet_mean"],
+           "active": int(mask.sum()), "f32_us_per_step": t_step * 1e6,
+           "cold": {"steps_1pct_wss": c1, "periods_run": kc, "last_cycle_change": chc,
+                    "s_1pct_wss": None if c1 is None else c1 * t_step}}
+    for arm in ("prior", "net"):
+        sw, _, _ = pulsatile_lattice(member, tau, "f32", device, collision, check)
+        sw.set_graph_steps(check)
+        sw.sync()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        x, prior = features(mask, member["inlet_mean"], T, tau=tau, device=device)
+        y = net.forward_graphed(x) if arm == "net" else zero_output(prior)
+        rho, u = prediction_to_device(y, prior)
+        sw.init_from_macro_device(rho.data_ptr(), u.data_ptr(), True, torch.cuda.current_stream(dev).cuda_stream)
+        sw.sync()
+        t_pred = time.perf_counter() - t0
+        ua = u.cpu().numpy().reshape(-1, 3)
+        hw, kw, chw = run_periods(sw, T, check, tol, kc + 1)
+        w1 = first_within_periodic(hw, ref, T, check, wss_tol)
+        sw.close()
+        row[arm] = {"steps_1pct_wss": w1, "periods_run": kw, "last_cycle_change": chw, "predict_s": t_pred,
+                    "s_1pct_wss": None if w1 is None else t_pred + w1 * t_step,
+                    "err_u_phase0": float(np.linalg.norm(ua - uc) / np.linalg.norm(uc))}
+    return row
 
 
 def make_sample(mask, member, rho, u, tau=0.8, device=0):

@@ -1,6 +1,7 @@
-"""3x3x3 stride-1 convolutions on the tcgen05 tensor cores (conv_tc.cu,
-selected by lbm_nn_conv3d_fwd / _bwd on grids with D % 4, H % 16 and W % 8
-== 0): forward and input gradient against PyTorch on the CPU in FP64 on
+"""3x3x3 convolutions on the tcgen05 tensor cores (conv_tc.cu, selected by
+lbm_nn_conv3d_fwd / _bwd: stride 1 on grids with D % 4, H % 16 and W % 8
+== 0, stride 2 on even grids whose output has H % 16 and W % 8 == 0):
+forward and input gradient against PyTorch on the CPU in FP64 on
 BF16-exact inputs and weights, and against the mma.sync engine on the same
 device buffers."""
 import ctypes as C
@@ -30,45 +31,48 @@ def _to_torch_w(w, co, ci):
     return w.reshape(co, 3, 3, 3, ci).permute(0, 4, 1, 2, 3).contiguous()
 
 
-def _fwd(L, gpu_lib, engine, xd, dims, ci, wd, bd, co, relu):
-    n = dims[0] * dims[1] * dims[2] * co
+def _fwd(L, gpu_lib, engine, xd, dims, ci, wd, bd, co, relu, s=1):
+    n = (dims[0] // s) * (dims[1] // s) * (dims[2] // s) * co
     yd = torch.empty(n, dtype=torch.bfloat16, device=xd.device)
     y32 = torch.empty(n, dtype=torch.float32, device=xd.device)
     gpu_lib._check(L.lbm_nn_set_conv_engine(engine))
     try:
         gpu_lib._check(L.lbm_nn_conv3d_fwd(_p(xd), _d(dims), ci, _p(wd), _p(bd) if bd is not None else None, co, 3,
-                                           1, relu, _p(yd), _p(y32), None))
+                                           s, relu, _p(yd), _p(y32), None))
     finally:
         L.lbm_nn_set_conv_engine(AUTO)
     return yd, y32
 
 
-def _bwd_dx(L, gpu_lib, engine, xd, dims, ci, wd, co, dyd):
+def _bwd_dx(L, gpu_lib, engine, xd, dims, ci, wd, co, dyd, s=1):
     dxd = torch.empty_like(xd)
     wtd = torch.empty_like(wd)
     gpu_lib._check(L.lbm_nn_set_conv_engine(engine))
     try:
-        gpu_lib._check(L.lbm_nn_conv3d_bwd(_p(xd), _d(dims), ci, _p(wd), _p(wtd), co, 3, 1, _p(dyd), _p(dxd), None,
+        gpu_lib._check(L.lbm_nn_conv3d_bwd(_p(xd), _d(dims), ci, _p(wd), _p(wtd), co, 3, s, _p(dyd), _p(dxd), None,
                                            None, None))
     finally:
         L.lbm_nn_set_conv_engine(AUTO)
     return dxd
 
 
-@pytest.mark.parametrize("ci,co,dims", [(16, 16, (4, 16, 8)), (16, 64, (8, 16, 16)), (32, 32, (4, 32, 8)),
-                                        (64, 64, (8, 16, 24)), (64, 16, (4, 16, 8)), (32, 64, (12, 32, 16)),
-                                        (64, 32, (4, 48, 8))])
-def test_gpu_conv_tc_matches_fp64_and_mma_sync(gpu_lib, ci, co, dims):
+@pytest.mark.parametrize("ci,co,dims,s", [(16, 16, (4, 16, 8), 1), (16, 64, (8, 16, 16), 1), (32, 32, (4, 32, 8), 1),
+                                          (64, 64, (8, 16, 24), 1), (64, 16, (4, 16, 8), 1), (32, 64, (12, 32, 16), 1),
+                                          (64, 32, (4, 48, 8), 1), (16, 32, (4, 32, 16), 2), (32, 64, (6, 64, 32), 2),
+                                          (64, 64, (2, 32, 48), 2), (64, 16, (4, 96, 16), 2)])
+def test_gpu_conv_tc_matches_fp64_and_mma_sync(gpu_lib, ci, co, dims, s):
     L = gpu_lib.load()
     dev = torch.device("cuda", 0)
-    rng = np.random.default_rng(ci * 3 + co + dims[0])
+    rng = np.random.default_rng(ci * 3 + co + dims[0] + s)
     D, H, W = dims
+    Do, Ho, Wo = D // s, H // s, W // s
     x = _bf(rng.normal(size=(D, H, W, ci)))
     w = _bf(rng.normal(size=(co, 27, ci)) * 0.2)
     b = torch.as_tensor(rng.normal(size=co) * 0.1)
     xt = x.permute(3, 0, 1, 2)[None].clone().requires_grad_(True)
-    yt = torch.nn.functional.conv3d(xt, _to_torch_w(w, co, ci), b, padding=1)
-    dy = _bf(rng.normal(size=(D, H, W, co)))
+    yt = torch.nn.functional.conv3d(xt, _to_torch_w(w, co, ci), b, stride=s, padding=1)
+    assert tuple(yt.shape[2:]) == (Do, Ho, Wo)
+    dy = _bf(rng.normal(size=(Do, Ho, Wo, co)))
     yt.backward(dy.permute(3, 0, 1, 2)[None])
     y_ref = yt.detach()[0].permute(1, 2, 3, 0)
     dx_ref = xt.grad[0].permute(1, 2, 3, 0)
@@ -77,19 +81,19 @@ def test_gpu_conv_tc_matches_fp64_and_mma_sync(gpu_lib, ci, co, dims):
     wd = w.to(torch.bfloat16).to(dev).reshape(-1)
     bd = b.to(torch.float32).to(dev)
     dyd = dy.to(torch.bfloat16).to(dev).reshape(-1)
-    y_tc, y32_tc = _fwd(L, gpu_lib, AUTO, xd, dims, ci, wd, bd, co, 0)
-    y_ms, y32_ms = _fwd(L, gpu_lib, MMA_SYNC, xd, dims, ci, wd, bd, co, 0)
-    dx_tc = _bwd_dx(L, gpu_lib, AUTO, xd, dims, ci, wd, co, dyd)
-    dx_ms = _bwd_dx(L, gpu_lib, MMA_SYNC, xd, dims, ci, wd, co, dyd)
+    y_tc, y32_tc = _fwd(L, gpu_lib, AUTO, xd, dims, ci, wd, bd, co, 0, s)
+    y_ms, y32_ms = _fwd(L, gpu_lib, MMA_SYNC, xd, dims, ci, wd, bd, co, 0, s)
+    dx_tc = _bwd_dx(L, gpu_lib, AUTO, xd, dims, ci, wd, co, dyd, s)
+    dx_ms = _bwd_dx(L, gpu_lib, MMA_SYNC, xd, dims, ci, wd, co, dyd, s)
     torch.cuda.synchronize()
     gpu_lib._check(L.lbm_nn_conv_status())
 
     # FP32 accumulation of BF16-exact products: relative 1e-5 of the output scale
     scale = float(y_ref.abs().max())
-    got = y32_tc.cpu().double().reshape(D, H, W, co)
+    got = y32_tc.cpu().double().reshape(Do, Ho, Wo, co)
     assert float((got - y_ref).abs().max()) <= 1e-5 * scale
     # the two engines differ only in summation order
-    assert float((got - y32_ms.cpu().double().reshape(D, H, W, co)).abs().max()) <= 1e-5 * scale
+    assert float((got - y32_ms.cpu().double().reshape(Do, Ho, Wo, co)).abs().max()) <= 1e-5 * scale
     # the BF16 output is the FP32 output rounded to nearest
     assert torch.equal(y_tc.cpu(), y32_tc.cpu().to(torch.bfloat16))
     # input gradient (BF16 output): within a BF16 rounding of the FP64 one
