@@ -638,13 +638,16 @@ def read_peaks():
     return 6800.0, "fallback"
 
 
-def read_traffic(name):
-    """dram bytes per launch from the committed ncu summary, if any."""
+def read_traffic(name, variant):
+    """DRAM bytes per launch (read + write, one ncu capture) of the step
+    kernel the launch variant runs -- the compact kernel for variants 6 and
+    7, the flat kernel otherwise -- from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
+    key = "traffic_bytes_per_launch[%s]" % ("compact" if variant in (6, 7) else "flat")
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch"):
+        if line.startswith(key):
             try:
                 return float(line.split("=", 1)[1].split()[0])
             except ValueError:
@@ -762,7 +765,7 @@ def run_ours(args):
     bpl = BYTES_PER_LU[(args.Q, args.precision)]
     peak, peak_kind = read_peaks()
     achieved = active * bpl / (mean_ms * 1e-3) / 1e9
-    traffic = read_traffic(f"step_kernel_c2_q{args.Q}_{args.precision}.txt")
+    traffic = read_traffic(f"step_kernel_c2_q{args.Q}_{args.precision}.txt", tuned[0])
 
     # secondary: FP16-offset storage on the same lattice (the precision config's storage)
     extra = {}
@@ -883,7 +886,9 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "bytes_per_lu": bpl, "peak_source": peak_kind,
-                         "kernel": f"lbm::step_kernel<{args.Q}, {args.precision}, physics, step>"},
+                         "kernel": (f"lbm::step_compact_kernel<{args.Q}, {args.precision}>" if tuned[0] in (6, 7)
+                                    else f"lbm::step_kernel<{args.Q}, {args.precision}, physics, step>"),
+                         "launch_variant": tuned[0]},
             "cpu_baseline": cpu,
             "e2e": {"value": aggregate_mlups(ws, active, B, e2e_t), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
