@@ -561,10 +561,12 @@ def warmstart_extra(device, box=(64, 64, 128), n_train=32, n_test=6, tau=0.55, r
 def conv_forward_c5(device, dims=(256, 128, 128), reps=5):
     """One forward pass of the warm-start network at the C5 grid (128 x 128
     x 256 voxels, random BF16 input), CUDA events around `reps` passes after
-    a warm-up pass, on each convolution engine: tcgen05 (3x3x3 stride-1
-    layers on the fifth-generation tensor cores, the others on mma.sync) and
-    mma.sync everywhere; per layer, the tcgen05 engine's time of one
-    convolution launch (10 launches timed)."""
+    a warm-up pass, on each convolution engine: tcgen05 (3x3x3 layers on the
+    fifth-generation tensor cores, the 1x1 layer on mma.sync) and mma.sync
+    everywhere; per layer, the tcgen05 engine's time of one convolution
+    launch (10 launches timed); and one training step of one sample
+    (forward, masked MSE, backward with the weight gradients, Adam) on each
+    engine."""
     import ctypes as C
     import torch
     from pv_dec_original_gb300 import capi
@@ -617,6 +619,27 @@ def conv_forward_c5(device, dims=(256, 128, 128), reps=5):
                             "engine": "tcgen05" if tc else "mma.sync", "us": ms * 1e3,
                             "tflops": fl / (ms * 1e-3) / 1e12}
         out["layers_tcgen05_engine"] = layers
+        # one training step (forward, masked MSE, backward, Adam) of one
+        # sample on each engine
+        tgt = torch.rand(nvox * 4, device=dev, generator=g)
+        msk = torch.ones(nvox, dtype=torch.uint8, device=dev)
+        for name, engine in (("mma_sync", 1), ("tcgen05", 0)):
+            capi._check(L.lbm_nn_set_conv_engine(engine))
+
+            def train_step():
+                big.zero_grad()
+                y32 = big.forward(xb)
+                big.backward(big.loss_and_grad(y32, tgt, msk, 1.0 / (4 * nvox)))
+                big.adam(1e-4)
+
+            train_step()
+            torch.cuda.synchronize(dev)
+            ev[0].record(big.stream)
+            for _ in range(reps):
+                train_step()
+            ev[1].record(big.stream)
+            torch.cuda.synchronize(dev)
+            out[name]["train_step_ms"] = ev[0].elapsed_time(ev[1]) / reps
     finally:
         L.lbm_nn_set_conv_engine(0)
     capi._check(L.lbm_nn_conv_status())

@@ -254,6 +254,179 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient dW[o][t][c] += sum over output voxels m of
+// dY[m][o] X[src(m, t)][c] (stride 1 or 2) on tcgen05.  GEMM rows are the
+// 27 ci (tap, input channel) pairs R = t ci + c in tiles of 128 (M), the
+// columns the co output channels (N), and K = 16 output voxels of one x-row
+// an MMA (Wo % 16 == 0).  Per 16-voxel slice the CTA stages, with cp.async,
+// the im2col rows of its tiles -- for every (tap, 8-channel group) the 16
+// voxels' source values, zero where the tap falls outside the grid -- and
+// dY of the 16 voxels, both MN-major: a core matrix is 8 voxels x 8
+// channels, 128 contiguous bytes; the next 8 rows (channels) lie 256 bytes
+// on, the next 8 voxels 128.  Two stages: the copies of slice k + 1 overlap
+// the MMAs of slice k (an mbarrier per stage, every wait bounded).  The
+// tiles of a CTA accumulate in tensor memory over its share of the slices
+// (CTAs along y take different tiles); the epilogue adds them to dW with
+// FP32 atomics.
+constexpr int kTileBytes = 128 * 32;  // one 128-row x 16-voxel BF16 tile
+
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int m, int n) {
+    return idesc_bf16(m, n) | (1u << 15) | (1u << 16);  // A and B MN-major
+}
+
+template <int CO>
+__global__ void __launch_bounds__(kThreads) k_conv3_wgrad_tc(const bf16* __restrict__ x, const bf16* __restrict__ dy,
+                                                             float* __restrict__ dw, int Di, int Hi, int Wi, int Do,
+                                                             int Ho, int Wo, int ci, int S, int tpg, int ncols,
+                                                             int slices_per_cta, int nslices) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int RT = (27 * ci + 127) / 128;
+    const int tile0 = blockIdx.y * tpg;
+    const int ntiles = min(tpg, RT - tile0);
+    const int stage_bytes = tpg * kTileBytes + CO * 32;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * stage_bytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int s_begin = blockIdx.x * slices_per_cta;
+    const int s_end = min(nslices, s_begin + slices_per_cta);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(tslot)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(saddr(bar), 1);
+        mbar_init(saddr(bar + 1), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t smem_a = saddr(smem);
+    const int xs = Wo / 16;  // slices per output row
+
+    // one slice's copies into stage b
+    auto stage = [&](int sl, int b) {
+        const uint32_t a_base = smem_a + b * stage_bytes, b_base = a_base + tpg * kTileBytes;
+        const int row = sl / xs, ox0 = (sl - row * xs) * 16;
+        const int oy = row % Ho, oz = row / Ho;
+        const int64_t m0 = ((int64_t)oz * Ho + oy) * Wo + ox0;
+        for (int i = tid; i < (CO / 8) * 16; i += kThreads) {
+            const int og = i >> 4, v = i & 15;
+            cp_async16(b_base + og * 256 + v * 16, dy + (m0 + v) * CO + og * 8, true);
+        }
+        for (int i = tid; i < ntiles * 256; i += kThreads) {
+            const int lg = i >> 4, v = i & 15;
+            const int R = (tile0 * 16 + lg) * 8;  // first row of this 8-row group
+            const int t = R / ci, cg = (R - t * ci) >> 3;
+            const int tz = t / 9, ty = (t / 3) % 3, tx = t % 3;
+            const int ix = S * (ox0 + v) + tx - 1, iy = S * oy + ty - 1, iz = S * oz + tz - 1;
+            const bool in = t < 27 && ix >= 0 && iy >= 0 && iz >= 0 && ix < Wi && iy < Hi && iz < Di;
+            const bf16* src = in ? x + (((int64_t)iz * Hi + iy) * Wi + ix) * ci + cg * 8 : x;
+            cp_async16(a_base + lg * 256 + v * 16, src, in);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+
+    constexpr uint32_t IDESC = idesc_bf16_mn(128, CO);
+    bool ok = true;
+    uint32_t uses[2] = {0u, 0u};
+    if (s_begin < s_end) stage(s_begin, 0);
+    int sl = s_begin;
+    for (; sl < s_end && ok; ++sl) {
+        const int b = (sl - s_begin) & 1;
+        if (sl + 1 < s_end) {
+            // the other stage is free once the MMAs of the previous slice are done
+            if (sl > s_begin) ok = mbar_wait(saddr(bar + (b ^ 1)), (uses[b ^ 1] - 1) & 1);
+            ok = __syncthreads_and(ok);
+            if (!ok) break;
+            stage(sl + 1, b ^ 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a_base = smem_a + b * stage_bytes, b_base = a_base + tpg * kTileBytes;
+            const uint64_t bd = smem_desc(b_base, 128, 256);
+            for (int j = 0; j < ntiles; ++j)
+                mma_bf16(tmem + (uint32_t)(j * CO), smem_desc(a_base + j * kTileBytes, 128, 256), bd, IDESC,
+                         sl > s_begin ? 1u : 0u);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             saddr(bar + b))
+                         : "memory");
+        }
+        ++uses[b];
+    }
+    // the MMAs of the last slice (each stage's last use) are done
+    if (ok && s_end > s_begin) {
+        const int bl = (s_end - 1 - s_begin) & 1;
+        ok = mbar_wait(saddr(bar + bl), (uses[bl] - 1) & 1);
+    }
+    ok = __syncthreads_and(ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && s_end > s_begin) {
+        for (int j = 0; j < ntiles; ++j) {
+            const int R = (tile0 + j) * 128 + 32 * warp + lane;
+            const int t = R / ci, c = R - t * ci;
+#pragma unroll
+            for (int c16 = 0; c16 < CO / 16; ++c16) {
+                float v[16];
+                tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(j * CO + c16 * 16), v);
+                if (t < 27) {
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) atomicAdd(dw + ((int64_t)(c16 * 16 + k) * 27 + t) * ci + c, v[k]);
+                }
+            }
+        }
+    } else if (!ok) {
+        // a wait gave up: record it, wait (bounded) for both stages' MMAs, release the tensor memory
+        if (tid == 0) atomicOr(&g_conv_tc_flags, 1u);
+        for (int b = 0; b < 2; ++b)
+            if (uses[b]) mbar_wait(saddr(bar + b), (uses[b] - 1) & 1);
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+}
+
+template <int CO>
+cudaError_t launch_wgrad_co(const bf16* x, const bf16* dy, float* dw, int Di, int Hi, int Wi, int ci, int S,
+                            cudaStream_t st) {
+    const int Do = (Di - 1) / S + 1, Ho = (Hi - 1) / S + 1, Wo = (Wi - 1) / S + 1;
+    const int RT = (27 * ci + 127) / 128;
+    const int tpg_max = 256 / CO;  // tensor-memory columns of a CTA <= 256
+    const int groups = (RT + tpg_max - 1) / tpg_max;
+    const int tpg = (RT + groups - 1) / groups;
+    int ncols = 32;
+    while (ncols < tpg * CO) ncols *= 2;
+    const int nslices = (int)((int64_t)Do * Ho * Wo / 16);
+    const int want = 4 * 152 / groups > 1 ? 4 * 152 / groups : 1;
+    const int spc = (nslices + want - 1) / want;
+    const int nx = (nslices + spc - 1) / spc;
+    // shared memory: two stages, two mbarriers and the tensor-memory slot,
+    // padded so that at most 512 / ncols CTAs reside on an SM (their
+    // tensor memory then always fits)
+    const int actual = 2 * (tpg * kTileBytes + CO * 32) + 32;
+    const int per_sm = 512 / ncols;
+    int bytes = 233472 / (per_sm + 1) + 1024;
+    if (bytes < actual) bytes = actual;
+    cudaError_t e =
+        cudaFuncSetAttribute(k_conv3_wgrad_tc<CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    k_conv3_wgrad_tc<CO><<<dim3((unsigned)nx, (unsigned)groups), kThreads, bytes, st>>>(
+        x, dy, dw, Di, Hi, Wi, Do, Ho, Wo, ci, S, tpg, ncols, spc, nslices);
+    return cudaGetLastError();
+}
+
 // Wt [ci][t][co] = W [co][26 - t][ci]: the input gradient of a stride-1
 // convolution is the forward convolution of dy with these weights.
 __global__ void k_flip_transpose(const bf16* __restrict__ w, bf16* __restrict__ wt, int co, int ci) {
@@ -320,6 +493,25 @@ cudaError_t conv3_tc(const void* x, int D, int H, int W, int ci, const void* w, 
                      void* y, float* y32, int stride, cudaStream_t st) {
     return stride == 2 ? launch_s<2>(x, D, H, W, ci, w, bias, co, relu, y, y32, st)
                        : launch_s<1>(x, D, H, W, ci, w, bias, co, relu, y, y32, st);
+}
+
+bool conv3_wgrad_tc_applies(int D, int H, int W, int ci, int co, int stride) {
+    const bool ch = (ci == 16 || ci == 32 || ci == 64) && (co == 16 || co == 32 || co == 64);
+    if (!ch || D <= 0 || H <= 0 || W <= 0 || (stride != 1 && stride != 2)) return false;
+    const int64_t Wo = (W - 1) / stride + 1;
+    const int64_t vox = (int64_t)((D - 1) / stride + 1) * ((H - 1) / stride + 1) * Wo;
+    return Wo % 16 == 0 && vox / 16 < ((int64_t)1 << 31);
+}
+
+cudaError_t conv3_wgrad_tc(const void* x, int D, int H, int W, int ci, const void* dy, int co, int stride, float* dw,
+                           cudaStream_t st) {
+    const bf16* xb = static_cast<const bf16*>(x);
+    const bf16* db = static_cast<const bf16*>(dy);
+    switch (co) {
+        case 16: return launch_wgrad_co<16>(xb, db, dw, D, H, W, ci, stride, st);
+        case 32: return launch_wgrad_co<32>(xb, db, dw, D, H, W, ci, stride, st);
+        default: return launch_wgrad_co<64>(xb, db, dw, D, H, W, ci, stride, st);
+    }
 }
 
 cudaError_t conv3_flip_transpose(const void* w, void* wt, int co, int ci, cudaStream_t st) {

@@ -244,6 +244,11 @@ bool conv3_tc_applies(int D, int H, int W, int ci, int co, int stride);
 cudaError_t conv3_tc(const void* x, int D, int H, int W, int ci, const void* w, const float* bias, int co, int relu,
                      void* y, float* y32, int stride, cudaStream_t st);
 cudaError_t conv3_flip_transpose(const void* w, void* wt, int co, int ci, cudaStream_t st);
+// Weight gradient dw += dL/dw of a 3x3x3 convolution (stride 1 or 2) on
+// tcgen05, for output grids whose x extent is a multiple of 16.
+bool conv3_wgrad_tc_applies(int D, int H, int W, int ci, int co, int stride);
+cudaError_t conv3_wgrad_tc(const void* x, int D, int H, int W, int ci, const void* dy, int co, int stride, float* dw,
+                           cudaStream_t st);
 cudaError_t conv_tc_status(unsigned* flags);
 
 // Message returned by lbm_last_global_error() (capi.cu).

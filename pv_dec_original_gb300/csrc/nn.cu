@@ -5,8 +5,11 @@
 //
 // Activations are BF16, channels-last (voxel-major, channel counts padded to
 // multiples of 16); weights are BF16 [co][tap][ci] with an FP32 master copy
-// for Adam; every product accumulates in FP32 on the tensor cores
-// (mma.sync m16n8k16 BF16).  A convolution is an implicit GEMM:
+// for Adam; every product accumulates in FP32 on the tensor cores.  The
+// 3x3x3 forward convolutions, stride-1 input gradients and weight
+// gradients run on tcgen05 where the grid tiles (conv_tc.cu); the kernels
+// here (mma.sync m16n8k16 BF16) take the rest and the comparison engine
+// (lbm_nn_set_conv_engine).  A convolution is an implicit GEMM:
 //   forward      rows = output voxels, cols = output channels, K = taps x ci
 //   input grad   rows = input voxels,  cols = input channels,  K = taps x co
 //                (the same kernel with the transposed weights [ci][tap][co])
@@ -419,6 +422,82 @@ __global__ void k_jfa_step(const int32_t* __restrict__ in, int32_t* __restrict__
     out[v] = best;
 }
 
+// The same flooding with every seed stored as its packed coordinates
+// x | y << 11 | z << 22 (grids up to 2048 x 2048 x 512: 31 bits, so an
+// empty voxel's -1 stays the only negative value) and one thread per
+// voxel on a (x blocks, y, z) grid: no 64-bit division per neighbour.  The
+// squared distances are integers below 2^24, exact in FP32 and in int32
+// alike, and neighbours are visited in the same order with the same strict
+// comparison, so the nearest seed and the distances are those of the
+// kernels above.
+constexpr int kPackBitsXY = 11, kPackBitsZ = 9;
+__host__ __device__ constexpr bool jfa_packs(int D, int H, int W) {
+    return W <= (1 << kPackBitsXY) && H <= (1 << kPackBitsXY) && D <= (1 << kPackBitsZ);
+}
+__device__ __forceinline__ int32_t jfa_pack(int x, int y, int z) {
+    return x | (y << kPackBitsXY) | (z << (2 * kPackBitsXY));
+}
+__device__ __forceinline__ int jfa_d2(int32_t s, int x, int y, int z) {
+    const int ex = x - (s & ((1 << kPackBitsXY) - 1)), ey = y - ((s >> kPackBitsXY) & ((1 << kPackBitsXY) - 1)),
+              ez = z - (s >> (2 * kPackBitsXY));
+    return ex * ex + ey * ey + ez * ez;
+}
+
+template <bool PLANAR>
+__global__ void k_jfa_seed_p(const uint8_t* __restrict__ mask, int D, int H, int W, int32_t* __restrict__ seed) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const int64_t v = ((int64_t)z * H + y) * W + x;
+    bool s = false;
+    if (mask[v]) {
+        const int d[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+        for (int k = 0; k < (PLANAR ? 4 : 6) && !s; ++k) {
+            const int xx = x + d[k][0], yy = y + d[k][1], zz = z + d[k][2];
+            s = xx < 0 || yy < 0 || zz < 0 || xx >= W || yy >= H || zz >= D ||
+                !mask[((int64_t)zz * H + yy) * W + xx];
+        }
+    }
+    seed[v] = s ? jfa_pack(x, y, z) : -1;
+}
+
+template <bool PLANAR>
+__global__ void k_jfa_step_p(const int32_t* __restrict__ in, int32_t* __restrict__ out, int D, int H, int W, int k) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const int64_t v = ((int64_t)z * H + y) * W + x;
+    int32_t best = in[v];
+    int bd = best >= 0 ? jfa_d2(best, x, y, z) : 0x7fffffff;
+    for (int dz = (PLANAR ? 0 : -1); dz <= (PLANAR ? 0 : 1); ++dz) {
+        const int zz = z + dz * k;
+        if (zz < 0 || zz >= D) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = y + dy * k;
+            if (yy < 0 || yy >= H) continue;
+            const int32_t* row = in + ((int64_t)zz * H + yy) * W;
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = x + dx * k;
+                if (xx < 0 || xx >= W) continue;
+                const int32_t s = __ldg(row + xx);
+                if (s < 0) continue;
+                const int d = jfa_d2(s, x, y, z);
+                if (d < bd) { bd = d; best = s; }
+            }
+        }
+    }
+    out[v] = best;
+}
+
+template <bool PLANAR>
+__global__ void k_jfa_finish_p(const int32_t* __restrict__ seed, const uint8_t* __restrict__ mask, int D, int H,
+                               int W, float* __restrict__ sdf) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const int64_t v = ((int64_t)z * H + y) * W + x;
+    const int32_t s = seed[v];
+    const float d = s >= 0 ? sqrtf((float)jfa_d2(s, x, y, z)) : 0.f;
+    sdf[v] = mask[v] ? d + 0.5f : (PLANAR ? 0.f : -(d + 0.5f));
+}
+
 template <bool PLANAR>
 __global__ void k_jfa_finish(const int32_t* __restrict__ seed, const uint8_t* __restrict__ mask, int D, int H,
                              int W, float* __restrict__ sdf) {
@@ -551,8 +630,9 @@ bool padded16(int c) { return c == 16 || c == 32 || c == 64; }  // the channel c
 // apply, or mma.sync everywhere.
 std::atomic<int> g_engine{LBM_NN_ENGINE_AUTO};
 
-// 3x3x3 on shapes the tensor-core kernel tiles (conv_tc.cu): the forward
-// convolution at stride 1 or 2, the input gradient at stride 1.
+// 3x3x3 on shapes the tensor-core kernels tile (conv_tc.cu): the forward
+// convolution at stride 1 or 2, the input gradient at stride 1 (the weight
+// gradient: conv3_wgrad_tc_applies).
 bool use_tc(const Conv& g) {
     return g_engine.load() == LBM_NN_ENGINE_AUTO && g.ks == 3 &&
            lbm::conv3_tc_applies(g.D, g.H, g.W, g.ci, g.co, g.stride);
@@ -602,10 +682,21 @@ void jfa(const uint8_t* mask, int D, int H, int W, int32_t* scratch, float* out,
     const int64_t n = (int64_t)D * H * W;
     int32_t* a = scratch;
     int32_t* b = a + n;
-    k_jfa_seed<PLANAR><<<grid1(n), 256, 0, st>>>(mask, D, H, W, a);
     const int big = PLANAR ? (H > W ? H : W) : (D > H ? (D > W ? D : W) : (H > W ? H : W));
     int k = 1;
     while (k * 2 < big) k *= 2;
+    if (jfa_packs(D, H, W) && H <= 65535 && D <= 65535) {
+        const dim3 grid((unsigned)lbm::ceil_div(W, 128), (unsigned)H, (unsigned)D);
+        k_jfa_seed_p<PLANAR><<<grid, 128, 0, st>>>(mask, D, H, W, a);
+        for (; k >= 1; k /= 2) {
+            k_jfa_step_p<PLANAR><<<grid, 128, 0, st>>>(a, b, D, H, W, k);
+            int32_t* t = a; a = b; b = t;
+        }
+        k_jfa_step_p<PLANAR><<<grid, 128, 0, st>>>(a, b, D, H, W, 1);
+        k_jfa_finish_p<PLANAR><<<grid, 128, 0, st>>>(b, mask, D, H, W, out);
+        return;
+    }
+    k_jfa_seed<PLANAR><<<grid1(n), 256, 0, st>>>(mask, D, H, W, a);
     for (; k >= 1; k /= 2) {
         k_jfa_step<PLANAR><<<grid1(n), 256, 0, st>>>(a, b, D, H, W, k);
         int32_t* t = a; a = b; b = t;
@@ -676,7 +767,10 @@ lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const 
             e = launch_gemm<1>(ci, static_cast<const bf16*>(dy), static_cast<const bf16*>(w_t), nullptr,
                                static_cast<bf16*>(dx), nullptr, g, rows_in, co, 0, st);
     }
-    if (e == cudaSuccess && dw) {
+    if (e == cudaSuccess && dw && g.ks == 3 && g_engine.load() == LBM_NN_ENGINE_AUTO &&
+        lbm::conv3_wgrad_tc_applies(g.D, g.H, g.W, ci, co, g.stride)) {
+        e = lbm::conv3_wgrad_tc(x, g.D, g.H, g.W, ci, dy, co, g.stride, dw, st);
+    } else if (e == cudaSuccess && dw) {
         const bf16* xb = static_cast<const bf16*>(x);
         const bf16* dyb = static_cast<const bf16*>(dy);
         switch (co) {

@@ -127,3 +127,43 @@ def test_gpu_conv_engine_argument(gpu_lib):
     L = gpu_lib.load()
     assert L.lbm_nn_set_conv_engine(7) == -1  # LBM_ERR_ARG
     assert L.lbm_nn_set_conv_engine(AUTO) == 0
+
+
+@pytest.mark.parametrize("ci,co,dims,s", [(16, 16, (4, 8, 16), 1), (32, 64, (2, 6, 32), 1), (64, 64, (3, 5, 16), 1),
+                                          (64, 32, (2, 4, 48), 1), (16, 32, (4, 8, 32), 2), (32, 64, (6, 6, 64), 2),
+                                          (64, 16, (2, 4, 32), 2), (32, 16, (5, 3, 16), 1)])
+def test_gpu_conv_tc_weight_gradient(gpu_lib, ci, co, dims, s):
+    """The tcgen05 weight gradient (output x extent a multiple of 16)
+    against PyTorch FP64 and the mma.sync engine; dw is accumulated into."""
+    L = gpu_lib.load()
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(ci + 2 * co + dims[2] + s)
+    D, H, W = dims
+    x = _bf(rng.normal(size=(D, H, W, ci)))
+    w = _bf(rng.normal(size=(co, 27, ci)) * 0.2)
+    wt = _to_torch_w(w, co, ci).requires_grad_(True)
+    yt = torch.nn.functional.conv3d(x.permute(3, 0, 1, 2)[None], wt, None, stride=s, padding=1)
+    Do, Ho, Wo = yt.shape[2:]
+    assert Wo % 16 == 0
+    dy = _bf(rng.normal(size=(Do, Ho, Wo, co)))
+    yt.backward(dy.permute(3, 0, 1, 2)[None])
+    dw_ref = wt.grad.permute(0, 2, 3, 4, 1).reshape(-1)  # [co][tz][ty][tx][ci]
+    xd = x.to(torch.bfloat16).to(dev).reshape(-1)
+    wd = w.to(torch.bfloat16).to(dev).reshape(-1)
+    dyd = dy.to(torch.bfloat16).to(dev).reshape(-1)
+    out = {}
+    for name, engine in (("tc", AUTO), ("ms", MMA_SYNC)):
+        dwd = torch.full((wd.numel(),), 0.25, dtype=torch.float32, device=dev)
+        wtd = torch.empty_like(wd)
+        gpu_lib._check(L.lbm_nn_set_conv_engine(engine))
+        try:
+            gpu_lib._check(L.lbm_nn_conv3d_bwd(_p(xd), _d(dims), ci, _p(wd), _p(wtd), co, 3, s, _p(dyd), None,
+                                               _p(dwd), None, None))
+        finally:
+            L.lbm_nn_set_conv_engine(AUTO)
+        torch.cuda.synchronize()
+        out[name] = dwd.cpu().double() - 0.25
+    gpu_lib._check(L.lbm_nn_conv_status())
+    scale = float(dw_ref.abs().max())
+    assert float((out["tc"] - dw_ref).abs().max()) <= 1e-5 * scale + 1e-6
+    assert float((out["tc"] - out["ms"]).abs().max()) <= 1e-5 * scale + 1e-6
