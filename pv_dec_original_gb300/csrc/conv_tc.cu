@@ -5,13 +5,17 @@
 //
 // One CTA (4 warps) computes an output block of 8 (x) x 16 (y) x TZ (z)
 // voxels (TZ = 4 at stride 1, 1 at stride 2) and all co output channels.
-// Per 16-channel chunk of the input it stages, with cp.async, the input
-// voxels the block reads (the block plus its one-voxel halo, 10 x 18 x 6 at
-// stride 1; 17 x 33 x 3 at stride 2) and the chunk of all 27 taps' weights
-// in shared memory, in the canonical no-swizzle K-major layout of the MMA
-// operands: core matrices of 8 rows x 16 bytes (8 channels), rows 16 bytes
-// apart.
-//   input:   [channel half k (2)][z][y][x parity p (S)][x / S][8 channels]
+// Per 16-channel chunk of the input it stages the input voxels the block
+// reads (the block plus its one-voxel halo, 10 x 18 x 6 at stride 1;
+// 17 x 33 x 3 at stride 2) with tensor-memory-access copies
+// (cp.async.bulk.tensor, one per channel half and x parity, zero-filled
+// outside the grid: the padding; at stride 2 an element stride of 2 along x
+// picks one parity) completing on an mbarrier, and the chunk of all 27
+// taps' weights with cp.async, in the canonical no-swizzle K-major layout
+// of the MMA operands: core matrices of 8 rows x 16 bytes (8 channels),
+// rows 16 bytes apart.
+//   input:   [channel half k (2)][x parity p (S)][z][y][x / S][8 channels]
+//            (a parity plane padded to 128 bytes)
 //   weights: [tap][co / 8][channel half k][co % 8][8 channels]
 // The 128 output voxels of one z plane (8 x by 16 y) are the M = 128 rows
 // of one MMA: row m = 8 y + x.  Output x reads input x = S x + tx - 1, so
@@ -33,8 +37,10 @@
 // Bound: the A operand (the staged input, 4 KB per MMA) is read from shared
 // memory by every MMA, 2 co FLOP a byte; at co = 16 that operand traffic,
 // not the tensor pipe, sets the rate (see the convolution profile).
+#include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "lbm_internal.cuh"
@@ -55,10 +61,12 @@ struct Geo {
     static constexpr int ZB = S * (TZ - 1) + 3;
     static constexpr int YB = S * (TY - 1) + 3;
     static constexpr int PAR = S;
-    static constexpr int XH = S == 1 ? TX + 2 : TX + 1;  // stride 2: input x = 2 xh + p, rows 0..16
-    static constexpr int VOX = ZB * YB * PAR * XH;       // staged voxels (1080 / 1782)
-    static constexpr int HALF = VOX * 16;                // bytes of one channel half
+    static constexpr int XH = S == 1 ? TX + 2 : TX + 1;        // stride 2: input x = 2 xh + p, rows 0..16
+    static constexpr int PLANE_RAW = ZB * YB * XH * 16;         // bytes one copy writes (17,280 / 14,256)
+    static constexpr int PLANE = (PLANE_RAW + 127) / 128 * 128;  // copy destinations 128-byte aligned
+    static constexpr int HALF = PAR * PLANE;                     // bytes of one channel half
     static constexpr int TILE = 2 * HALF;
+    static constexpr int TX_BYTES = 2 * PAR * PLANE_RAW;         // bytes the copies of a chunk deliver
 };
 
 // Set when a bounded wait gave up (read and cleared by conv_tc_status).
@@ -102,6 +110,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// 4-D tiled tensor copy global -> shared completing on an mbarrier;
+// coordinates innermost first (channel, x, y, z).
+__device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                          uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
 __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
     asm volatile(
@@ -125,7 +148,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
 
 template <int S, int CO>
 __host__ __device__ constexpr int smem_bytes() {
-    return Geo<S>::TILE + 27 * CO * 32 + 16;  // input, weights, mbarrier + tensor-memory address
+    return Geo<S>::TILE + 27 * CO * 32 + 32;  // input, weights, two mbarriers + tensor-memory address
 }
 
 template <int S, int CO>
@@ -133,19 +156,22 @@ __host__ __device__ constexpr uint32_t tmem_cols() {
     return Geo<S>::TZ * CO < 32 ? 32u : (uint32_t)(Geo<S>::TZ * CO);  // a power of two for CO in {16, 32, 64}
 }
 
-// x [Di][Hi][Wi][ci], w [co][27][ci], y [Do][Ho][Wo][co] with Do = Di / S
-// etc.; Do % TZ == 0, Ho % 16 == 0, Wo % 8 == 0 (the launcher checks).
+// x [Di][Hi][Wi][ci] (read through `map`: the 4-D tensor map of x, box
+// 8 channels x (XH, or 2 XH with element stride 2) x YB x ZB), w [co][27][ci],
+// y [Do][Ho][Wo][co] with Do = Di / S etc.; Do % TZ == 0, Ho % 16 == 0,
+// Wo % 8 == 0 (the launcher checks).
 template <int S, int CO>
-__global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ x, const bf16* __restrict__ w,
-                                                       const float* __restrict__ bias, bf16* __restrict__ y,
-                                                       float* __restrict__ y32, int Di, int Hi, int Wi, int Do,
-                                                       int Ho, int Wo, int ci, int relu) {
+__global__ void __launch_bounds__(kThreads) k_conv3_tc(const __grid_constant__ CUtensorMap map,
+                                                       const bf16* __restrict__ w, const float* __restrict__ bias,
+                                                       bf16* __restrict__ y, float* __restrict__ y32, int Do, int Ho,
+                                                       int Wo, int ci, int relu) {
     using G = Geo<S>;
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char* tile = smem;
     unsigned char* wsm = smem + G::TILE;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(wsm + 27 * CO * 32);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wsm + 27 * CO * 32);  // [0] MMAs done, [1] input copies done
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    volatile int& copy_failed = *reinterpret_cast<volatile int*>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nbx = Wo / TX, nby = Ho / TY;
     const int bx = blockIdx.x % nbx, by = (blockIdx.x / nbx) % nby, bz = blockIdx.x / (nbx * nby);
@@ -160,7 +186,9 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
     }
     if (tid == 0) {
         mbar_init(saddr(bar), 1);
+        mbar_init(saddr(bar + 1), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        copy_failed = 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -169,21 +197,20 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
 
     const uint32_t tile_a = saddr(tile), w_a = saddr(wsm);
     constexpr uint32_t IDESC = idesc_bf16(128, CO);
-    constexpr uint32_t SBO = S * G::PAR * G::XH * 16;  // S input rows per output row
+    constexpr uint32_t SBO = S * G::XH * 16;  // S input rows per output row
     bool ok = true;
     const int chunks = ci / 16;
     int c = 0;
     for (; c < chunks && ok; ++c) {
-        // stage the input voxels (zero outside the grid: the padding) and the weights of this chunk
-        for (int i = tid; i < 2 * G::VOX; i += kThreads) {
-            const int v = i >> 1, k = i & 1;
-            const int xh = v % G::XH, p = (v / G::XH) % G::PAR, yy = (v / (G::XH * G::PAR)) % G::YB,
-                      zz = v / (G::XH * G::PAR * G::YB);
-            const int gx = S * x0 - 1 + S * xh + p, gy = S * y0 - 1 + yy, gz = S * z0 - 1 + zz;
-            const bool in = gx >= 0 && gy >= 0 && gz >= 0 && gx < Wi && gy < Hi && gz < Di;
-            const bf16* src = in ? x + (((int64_t)gz * Hi + gy) * Wi + gx) * ci + c * 16 + k * 8 : x;
-            cp_async16(tile_a + k * G::HALF + v * 16, src, in);
+        // the input voxels of this chunk by tensor copies (zero outside the grid: the padding)
+        if (tid == 0) {
+            mbar_expect_tx(saddr(bar + 1), (uint32_t)G::TX_BYTES);
+            for (int k = 0; k < 2; ++k)
+                for (int p = 0; p < G::PAR; ++p)
+                    tma_load4(tile_a + k * G::HALF + p * G::PLANE, &map, c * 16 + k * 8, S * x0 - 1 + p,
+                              S * y0 - 1, S * z0 - 1, saddr(bar + 1));
         }
+        // the weights of this chunk
         for (int i = tid; i < 27 * CO * 2; i += kThreads) {
             const int k = i & 1, n = (i >> 1) % CO, t = (i >> 1) / CO;
             cp_async16(w_a + t * (CO * 32) + (n >> 3) * 256 + k * 128 + (n & 7) * 16,
@@ -193,20 +220,36 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int z = 0; z < G::TZ; ++z) {
-                for (int t = 0; t < 27; ++t) {
-                    const int tz = t / 9, ty = (t / 3) % 3, tx = t % 3;
-                    const int zz = S * z + tz, p = tx % S, xo = tx / S;
-                    const uint32_t a = tile_a + (((zz * G::YB + ty) * G::PAR + p) * G::XH + xo) * 16;
-                    const uint64_t ad = smem_desc(a, G::HALF, SBO);
-                    const uint64_t bd = smem_desc(w_a + t * (CO * 32), 128, 256);
-                    mma_bf16(tmem + (uint32_t)(z * CO), ad, bd, IDESC, (c > 0 || t > 0) ? 1u : 0u);
+            if (mbar_wait(saddr(bar + 1), (uint32_t)(c & 1))) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                for (int z = 0; z < G::TZ; ++z) {
+                    for (int t = 0; t < 27; ++t) {
+                        const int tz = t / 9, ty = (t / 3) % 3, tx = t % 3;
+                        const int zz = S * z + tz, p = tx % S, xo = tx / S;
+                        const uint32_t a = tile_a + p * G::PLANE + ((zz * G::YB + ty) * G::XH + xo) * 16;
+                        const uint64_t ad = smem_desc(a, G::HALF, SBO);
+                        const uint64_t bd = smem_desc(w_a + t * (CO * 32), 128, 256);
+                        mma_bf16(tmem + (uint32_t)(z * CO), ad, bd, IDESC, (c > 0 || t > 0) ? 1u : 0u);
+                    }
                 }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 saddr(bar))
+                             : "memory");
+            } else {
+                copy_failed = 1;
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             saddr(bar))
-                         : "memory");
+        }
+        __syncthreads();
+        if (copy_failed) {
+            // the copies did not complete in time: record it and wait
+            // (bounded) once more before the shared memory is released
+            if (tid == 0) {
+                atomicOr(&g_conv_tc_flags, 2u);
+                mbar_wait(saddr(bar + 1), (uint32_t)(c & 1));
+            }
+            ok = false;
+            c = -1;  // no MMAs of this chunk to wait for; those of earlier chunks are done
+            break;
         }
         // every thread: the MMAs of this chunk are done (they read the staged block)
         ok = mbar_wait(saddr(bar), (uint32_t)(c & 1));
@@ -242,7 +285,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const bf16* __restrict__ 
                 }
             }
         }
-    } else {
+    } else if (c > 0) {
         // the wait of chunk c - 1 gave up: record it, wait (bounded) once
         // more for that chunk's MMAs, then release the tensor memory
         if (tid == 0) atomicOr(&g_conv_tc_flags, 1u);
@@ -436,17 +479,59 @@ __global__ void k_flip_transpose(const bf16* __restrict__ w, bf16* __restrict__ 
     wt[((int64_t)c * 27 + (26 - t)) * co + o] = w[e];
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library), looked up once.
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled() {
+    static std::atomic<EncodeTiled> fn{nullptr};
+    EncodeTiled f = fn.load(std::memory_order_acquire);
+    if (!f) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        f = reinterpret_cast<EncodeTiled>(p);
+        fn.store(f, std::memory_order_release);
+    }
+    return f;
+}
+
+// The tensor map of x [Di][Hi][Wi][ci] BF16 for stride S: box 8 channels x
+// XH voxels along x (stride 2: 2 XH with element stride 2, one parity) x YB
+// x ZB, zero fill outside the tensor.
+template <int S>
+cudaError_t input_map(CUtensorMap* map, const bf16* x, int Di, int Hi, int Wi, int ci) {
+    using G = Geo<S>;
+    EncodeTiled f = encode_tiled();
+    if (!f) return cudaErrorNotSupported;
+    const cuuint64_t dims[4] = {(cuuint64_t)ci, (cuuint64_t)Wi, (cuuint64_t)Hi, (cuuint64_t)Di};
+    const cuuint64_t strides[3] = {(cuuint64_t)ci * 2, (cuuint64_t)Wi * ci * 2, (cuuint64_t)Hi * Wi * ci * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)(S * G::XH), (cuuint32_t)G::YB, (cuuint32_t)G::ZB};
+    const cuuint32_t estride[4] = {1, (cuuint32_t)S, 1, 1};
+    const CUresult r = f(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(x), dims, strides, box, estride,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 template <int S, int CO>
 cudaError_t launch_co(const bf16* x, const bf16* w, const float* bias, bf16* y, float* y32, int Di, int Hi, int Wi,
                       int ci, int relu, cudaStream_t st) {
     constexpr int bytes = smem_bytes<S, CO>();
     static_assert(bytes <= 227 * 1024, "shared memory");
-    cudaError_t e = cudaFuncSetAttribute(k_conv3_tc<S, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    CUtensorMap map;
+    cudaError_t e = input_map<S>(&map, x, Di, Hi, Wi, ci);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_conv3_tc<S, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
     const int Do = Di / S, Ho = Hi / S, Wo = Wi / S;
     const int64_t blocks = (int64_t)(Wo / TX) * (Ho / TY) * (Do / Geo<S>::TZ);
-    k_conv3_tc<S, CO><<<(unsigned)blocks, kThreads, bytes, st>>>(x, w, bias, y, y32, Di, Hi, Wi, Do, Ho, Wo, ci,
-                                                                 relu);
+    k_conv3_tc<S, CO><<<(unsigned)blocks, kThreads, bytes, st>>>(map, w, bias, y, y32, Do, Ho, Wo, ci, relu);
     return cudaGetLastError();
 }
 

@@ -717,7 +717,7 @@ lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const 
     const Conv g = make_conv(dims_in, ci, co, ksize, stride);
     const int64_t rows = (int64_t)g.Do * g.Ho * g.Wo;
     cudaError_t e;
-    if (use_tc(g))
+    if (use_tc(g) && aligned16(x))
         e = lbm::conv3_tc(x, g.D, g.H, g.W, ci, w, bias, co, relu, y, y_f32, g.stride,
                           static_cast<cudaStream_t>(stream));
     else
@@ -755,7 +755,7 @@ lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const 
     const int taps = ksize * ksize * ksize;
     const int64_t rows_out = (int64_t)g.Do * g.Ho * g.Wo, rows_in = (int64_t)g.D * g.H * g.W;
     cudaError_t e = cudaSuccess;
-    if (dx && use_tc_dx(g)) {
+    if (dx && use_tc_dx(g) && aligned16(dy)) {
         // stride 1: dx is the forward convolution of dy with the flipped, transposed weights
         e = lbm::conv3_flip_transpose(w, w_t, co, ci, st);
         if (e == cudaSuccess) e = lbm::conv3_tc(dy, g.Do, g.Ho, g.Wo, co, w_t, nullptr, ci, 0, dx, nullptr, 1, st);
