@@ -28,8 +28,9 @@ lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const 
  * run on the tcgen05 tensor cores with tensor-memory accumulators
  * (conv_tc.cu) -- the forward pass at stride 1 on input grids with D % 4,
  * H % 16 and W % 8 == 0 and at stride 2 on even grids whose output has
- * H % 16 and W % 8 == 0, and the stride-1 input gradient on the same grids;
- * the others, and the weight gradients, on mma.sync.
+ * H % 16 and W % 8 == 0, the stride-1 input gradient on the same grids,
+ * and the weight gradient wherever the output's W is a multiple of 16
+ * (16-byte aligned activations); the others on mma.sync.
  * LBM_NN_ENGINE_MMA_SYNC: mma.sync everywhere (the comparison path).
  * Process-wide. */
 #define LBM_NN_ENGINE_AUTO 0
@@ -86,6 +87,16 @@ lbm_status lbm_ws_prior(const uint8_t* mask, const int dims[3], double inlet, do
  * FP32 field v (weights renormalised next to solid voxels or the box face,
  * zero on solid); tmp: scratch of v's size. */
 lbm_status lbm_ws_smooth(const uint8_t* mask, const int dims[3], float* v, float* tmp, int rounds, void* stream);
+
+/* The network's BF16 input [nvox][16] for a D x H x W grid (dims) in one
+ * pass: channel 0 clamp(sdf * sdf_scale, -3, 3), 1 the mask (0 / 1), 2
+ * mean_in and 3 period_in (the scaled inlet mean and period, the same for
+ * every voxel), 4 z / D, 5 uz_p / inlet, 6 drho_p / inlet * rho_scale,
+ * 7..15 zero; every value computed in FP32 and rounded to BF16 once.  x
+ * 16-byte aligned. */
+lbm_status lbm_ws_features(const float* sdf, const uint8_t* mask, const float* uz_p, const float* drho_p,
+                           const int dims[3], float sdf_scale, float mean_in, float period_in, float inlet,
+                           float rho_scale, void* x, void* stream);
 
 /* Network output y ([nvox][c] FP32, c >= 4) to fields [4][nvox]: rho - 1 =
  * drho_p + y0 inlet / rho_scale, u = y1..3 inlet / u_scale, u_z += uz_p;

@@ -71,7 +71,7 @@ EXPORTS = [
     "lbm_moment_sums_noalloc",
     "lbm_nn_conv3d_fwd", "lbm_nn_conv3d_bwd", "lbm_nn_set_conv_engine", "lbm_nn_conv_status",
     "lbm_nn_relu_bwd", "lbm_nn_upsample2", "lbm_nn_add", "lbm_nn_mse",
-    "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_output", "lbm_ws_gather",
+    "lbm_nn_adam", "lbm_sdf_from_mask", "lbm_ws_prior", "lbm_ws_smooth", "lbm_ws_features", "lbm_ws_output", "lbm_ws_gather",
     "lbm_init_from_macro_device", "lbm_nearest_next_to_wall", "lbm_set_wall_distances", "lbm_get_wall_distances",
     "lbm_get_macro_async", "lbm_get_wss_async", "lbm_wait_outputs",
 ]
@@ -152,6 +152,7 @@ def load(build_if_missing: bool = True):
     L.lbm_sdf_from_mask.argtypes = [P, I3, P, P, P]
     L.lbm_ws_prior.argtypes = [P, I3, C.c_double, C.c_double, P, P, P, P, P]
     L.lbm_ws_smooth.argtypes = [P, I3, P, P, C.c_int, P]
+    L.lbm_ws_features.argtypes = [P, P, P, P, I3, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, P, P]
     L.lbm_ws_output.argtypes = [P, C.c_int, P, P, P, C.c_int64, C.c_float, C.c_float, C.c_float, P, P]
     L.lbm_ws_gather.argtypes = [P, C.c_int64, P, C.c_int64, P, P, P]
     L.lbm_init_from_macro_device.argtypes = [P, P, P, C.c_int, P]

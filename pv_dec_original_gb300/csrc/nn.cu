@@ -589,6 +589,28 @@ __global__ void k_smooth_axis(const uint8_t* __restrict__ mask, const float* __r
     out[v] = num / den;
 }
 
+// Network input [n][16] BF16, one voxel a thread (two 16-byte stores):
+// channel 0 clamp(sdf sdf_scale, -3, 3), 1 the mask, 2 and 3 the scalar
+// inlet mean and period (scaled), 4 z / D, 5 u_z prior / U, 6 (rho - 1)
+// prior / U rho_scale, 7..15 zero; FP32 values rounded to BF16 once.
+__global__ void k_ws_features(const float* __restrict__ sdf, const uint8_t* __restrict__ mask,
+                              const float* __restrict__ uz_p, const float* __restrict__ drho_p, int64_t n, int64_t hw,
+                              int D, float sdf_scale, float mean_in, float period_in, float inlet, float rho_scale,
+                              uint4* __restrict__ x) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const float f[7] = {fminf(fmaxf(sdf[v] * sdf_scale, -3.f), 3.f), mask[v] ? 1.f : 0.f, mean_in, period_in,
+                        (float)(int)(v / hw) / (float)D, uz_p[v] / inlet, drho_p[v] / inlet * rho_scale};
+    V8 a, b;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        a.h[k] = __float2bfloat16(k < 7 ? f[k] : 0.f);
+        b.h[k] = __float2bfloat16(0.f);
+    }
+    x[2 * v] = a.u;
+    x[2 * v + 1] = b.u;
+}
+
 // Network output [n][c] (FP32) to fields [4][n]: rho - 1 = prior + y0 U /
 // rho_scale, u = y1..3 U / u_scale (+ prior u_z); zero on solid voxels.
 __global__ void k_ws_output(const float* __restrict__ y, int c, const uint8_t* __restrict__ mask,
@@ -900,6 +922,20 @@ lbm_status lbm_ws_smooth(const uint8_t* mask, const int dims[3], float* v, float
     if (src != v) cudaMemcpyAsync(v, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, st);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? LBM_OK : report("lbm_ws_smooth", e);
+}
+
+lbm_status lbm_ws_features(const float* sdf, const uint8_t* mask, const float* uz_p, const float* drho_p,
+                           const int dims[3], float sdf_scale, float mean_in, float period_in, float inlet,
+                           float rho_scale, void* x, void* stream) {
+    if (!sdf || !mask || !uz_p || !drho_p || !dims || !x || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 ||
+        !(inlet != 0.f) || !aligned16(x))
+        return report("lbm_ws_features", cudaSuccess);
+    const int64_t hw = (int64_t)dims[1] * dims[2], n = (int64_t)dims[0] * hw;
+    k_ws_features<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        sdf, mask, uz_p, drho_p, n, hw, dims[0], sdf_scale, mean_in, period_in, inlet, rho_scale,
+        static_cast<uint4*>(x));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LBM_OK : report("lbm_ws_features", e);
 }
 
 lbm_status lbm_ws_output(const float* y, int c, const uint8_t* mask, const float* drho_p, const float* uz_p,

@@ -303,7 +303,24 @@ class Prior:
 
 def features(mask, inlet_mean, period, tau=0.8, device=0):
     """BF16 channels-last network input [D*H*W*C_IN] and the Prior the
-    network's output corrects (every array built on the device)."""
+    network's output corrects, built on the device in one pass
+    (``lbm_ws_features``; ``features_reference`` is the same input from
+    PyTorch element-wise operations)."""
+    torch = _torch()
+    dev = torch.device("cuda", device)
+    sdf = sdf_of_mask(mask, device)
+    prior = Prior(mask, inlet_mean, tau, device)
+    x = torch.empty(mask.size * C_IN, dtype=torch.bfloat16, device=dev)
+    capi._check(capi.load().lbm_ws_features(_ptr(sdf), _ptr(prior.mask), _ptr(prior.uz), _ptr(prior.drho),
+                                            _dims(mask.shape), SDF_SCALE, inlet_mean * MEAN_SCALE,
+                                            period * PERIOD_SCALE, inlet_mean, RHO_SCALE, _ptr(x),
+                                            C.c_void_p(prior.stream.cuda_stream)))
+    return x, prior
+
+
+def features_reference(mask, inlet_mean, period, tau=0.8, device=0):
+    """features() from PyTorch element-wise operations (the test oracle of
+    lbm_ws_features)."""
     torch = _torch()
     dev = torch.device("cuda", device)
     n = mask.size

@@ -317,3 +317,21 @@ def test_gpu_conv_refuses_unbuilt_channel_counts(gpu_lib):
     y = torch.zeros(8 * 8 * 8 * 16, dtype=torch.bfloat16, device=dev)
     rc = L.lbm_nn_conv3d_fwd(_p(x), _d((8, 8, 8)), 48, _p(w), None, 16, 3, 1, 0, _p(y), None, None)
     assert rc == -1  # LBM_ERR_ARG
+
+
+def test_gpu_ws_features_match_reference(gpu_lib):
+    """lbm_ws_features (one pass) against the same network input built from
+    PyTorch element-wise operations: channels 0-3 equal; the scaled position
+    and prior channels within one BF16 rounding (PyTorch divides by a
+    scalar through its reciprocal); padding channels zero."""
+    import torch
+    from pv_dec_original_gb300 import warmstart as WS
+    mask = _vessel_mask()
+    x1, _ = WS.features(mask, 0.025, 3300.0, tau=0.55)
+    x2, _ = WS.features_reference(mask, 0.025, 3300.0, tau=0.55)
+    a = x1.float().reshape(-1, WS.C_IN).cpu()
+    b = x2.float().reshape(-1, WS.C_IN).cpu()
+    assert torch.equal(a[:, :4], b[:, :4])
+    assert torch.all(a[:, 7:] == 0)
+    d = (a[:, 4:7] - b[:, 4:7]).abs()
+    assert torch.all(d <= b[:, 4:7].abs() * 2.0 ** -7 + 1e-30), float(d.max())
