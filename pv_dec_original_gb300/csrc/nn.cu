@@ -789,8 +789,8 @@ lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const 
             e = launch_gemm<1>(ci, static_cast<const bf16*>(dy), static_cast<const bf16*>(w_t), nullptr,
                                static_cast<bf16*>(dx), nullptr, g, rows_in, co, 0, st);
     }
-    if (e == cudaSuccess && dw && g.ks == 3 && g_engine.load() == LBM_NN_ENGINE_AUTO &&
-        lbm::conv3_wgrad_tc_applies(g.D, g.H, g.W, ci, co, g.stride)) {
+    if (e == cudaSuccess && dw && g.ks == 3 && g_engine.load() == LBM_NN_ENGINE_AUTO && aligned16(x) &&
+        aligned16(dy) && lbm::conv3_wgrad_tc_applies(g.D, g.H, g.W, ci, co, g.stride)) {
         e = lbm::conv3_wgrad_tc(x, g.D, g.H, g.W, ci, dy, co, g.stride, dw, st);
     } else if (e == cudaSuccess && dw) {
         const bf16* xb = static_cast<const bf16*>(x);

@@ -354,11 +354,14 @@ def make_target(mask, rho, u, inlet, prior, device=0):
     return t.reshape(-1)
 
 
-def prediction_to_device(y32, prior, smooth=2):
+def prediction_to_device(y32, prior, smooth=1):
     """Per-active-node rho (nact) and u (3 * nact, interleaved) as device
     FP32 tensors from the network output y32 ([voxels][C_OUT] FP32 on the
-    device): prior + correction, smoothed over the fluid, gathered
-    (``lbm_ws_output``, ``lbm_ws_smooth``, ``lbm_ws_gather``)."""
+    device): prior + correction, smoothed over the fluid (`smooth` rounds of
+    the masked [1, 2, 1] filter: one round measured best -- none leaves
+    voxel-scale content that costs a bifurcation's prior thousands of steps,
+    two blur the near-wall profile), gathered (``lbm_ws_output``,
+    ``lbm_ws_smooth``, ``lbm_ws_gather``)."""
     torch = _torch()
     L = capi.load()
     st = C.c_void_p(prior.stream.cuda_stream)
@@ -378,7 +381,7 @@ def prediction_to_device(y32, prior, smooth=2):
     return rho, u
 
 
-def prediction_to_macro(mask, y32, inlet, prior, smooth=2):
+def prediction_to_macro(mask, y32, inlet, prior, smooth=1):
     """prediction_to_device read back to the host: rho (nact) and u
     (nact, 3), FP32."""
     rho, u = prediction_to_device(y32, prior, smooth)

@@ -268,7 +268,7 @@ def test_gpu_ws_output_smooth_gather(gpu_lib):
     for c in range(3):
         np.testing.assert_allclose(uu[:, c], f[1 + c].reshape(-1)[fl], rtol=0, atol=1e-6 * U + 1e-8)
     # the host read-back is the same data
-    r2, u2 = WS.prediction_to_macro(mask, torch.from_numpy(y.reshape(-1)).cuda(), U, pr)
+    r2, u2 = WS.prediction_to_macro(mask, torch.from_numpy(y.reshape(-1)).cuda(), U, pr, smooth=2)
     np.testing.assert_array_equal(r2, rho.cpu().numpy())
     np.testing.assert_array_equal(u2, uu)
 
