@@ -8,7 +8,9 @@
  * (a cudaStream_t, NULL = the default stream) and allocate nothing.
  * Tensors are channels-last ([z][y][x][c]) BF16 with c a multiple of 16
  * (16, 32 or 64); weights are BF16 [co][tap][ci] (tap = (tz*k + ty)*k + tx),
- * FP32 biases [co].  Kernel size 3 (padding 1, stride 1 or 2) or 1. */
+ * FP32 biases [co].  Kernel size 3 (padding 1, stride 1 or 2) or 1.  The
+ * convolutions take 16-byte aligned tensors (activations, weights, FP32
+ * outputs) and return LBM_ERR_ARG for others. */
 #ifndef LBM_NN_H
 #define LBM_NN_H
 

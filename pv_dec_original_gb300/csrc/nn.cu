@@ -734,7 +734,8 @@ extern "C" {
 lbm_status lbm_nn_conv3d_fwd(const void* x, const int dims_in[3], int ci, const void* w, const float* bias, int co,
                              int ksize, int stride, int relu, void* y, float* y_f32, void* stream) {
     if (!x || !dims_in || !w || !y || !padded16(ci) || !padded16(co) || (ksize != 1 && ksize != 3) ||
-        (stride != 1 && stride != 2) || (ksize == 1 && stride != 1))
+        (stride != 1 && stride != 2) || (ksize == 1 && stride != 1) || !aligned16(x) || !aligned16(w) ||
+        !aligned16(y) || (y_f32 && !aligned16(y_f32)))
         return report("lbm_nn_conv3d_fwd", cudaSuccess);
     const Conv g = make_conv(dims_in, ci, co, ksize, stride);
     const int64_t rows = (int64_t)g.Do * g.Ho * g.Wo;
@@ -770,7 +771,8 @@ lbm_status lbm_nn_conv_status(void) {
 lbm_status lbm_nn_conv3d_bwd(const void* x, const int dims_in[3], int ci, const void* w, void* w_t, int co,
                              int ksize, int stride, const void* dy, void* dx, float* dw, float* db, void* stream) {
     if (!x || !dims_in || !w || !dy || !padded16(ci) || !padded16(co) || (ksize != 1 && ksize != 3) ||
-        (stride != 1 && stride != 2) || (ksize == 1 && stride != 1) || (dx && !w_t))
+        (stride != 1 && stride != 2) || (ksize == 1 && stride != 1) || (dx && !w_t) || !aligned16(x) ||
+        !aligned16(w) || !aligned16(dy) || (dx && (!aligned16(dx) || !aligned16(w_t))))
         return report("lbm_nn_conv3d_bwd", cudaSuccess);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const Conv g = make_conv(dims_in, ci, co, ksize, stride);

@@ -53,6 +53,22 @@ def test_errors_are_status_codes_not_crashes(gpu_lib):
     assert L.lbm_destroy(None) == 0
 
 
+def test_convolutions_refuse_misaligned_tensors(gpu_lib):
+    """The convolution entry points check their arguments on the host before
+    any device call: a tensor address that is not 16-byte aligned (the
+    tensor-core kernels copy 16-byte rows and tensor-map boxes) is an
+    argument error, never a launch."""
+    L = gpu_lib.load()
+    dims = (C.c_int * 3)(8, 16, 8)
+    good, odd = C.c_void_p(1 << 20), C.c_void_p((1 << 20) + 8)
+    assert L.lbm_nn_conv3d_fwd(odd, dims, 16, good, None, 16, 3, 1, 0, good, None, None) == -1
+    assert b"invalid argument" in L.lbm_last_global_error()
+    assert L.lbm_nn_conv3d_fwd(good, dims, 16, odd, None, 16, 3, 1, 0, good, None, None) == -1
+    assert L.lbm_nn_conv3d_fwd(good, dims, 16, good, None, 16, 3, 1, 0, good, odd, None) == -1
+    assert L.lbm_nn_conv3d_bwd(good, dims, 16, good, good, 16, 3, 1, odd, None, None, None, None) == -1
+    assert L.lbm_nn_conv3d_bwd(good, dims, 16, good, good, 16, 3, 1, good, odd, None, None, None) == -1
+
+
 def test_stl_reader_matches_python_parser(gpu_lib, tmp_path):
     from pv_dec_original_gb300 import geometry as G
     d = load(fixtures("vox")[0])
