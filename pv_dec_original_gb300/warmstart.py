@@ -259,11 +259,12 @@ class WarmStartNet:
 
 
 # ---------------------------------------------------------------------- data
-def sdf_of_mask(mask, device=0):
-    """Signed distance (device FP32 [D*H*W]) of a [D][H][W] mask."""
+def sdf_of_mask(mask, device=0, mask_dev=None):
+    """Signed distance (device FP32 [D*H*W]) of a [D][H][W] mask (mask_dev:
+    the same mask already on the device, uint8, flat)."""
     torch = _torch()
     dev = torch.device("cuda", device)
-    m = torch.from_numpy(np.ascontiguousarray(mask, np.uint8)).to(dev)
+    m = mask_dev if mask_dev is not None else torch.from_numpy(np.ascontiguousarray(mask, np.uint8)).to(dev)
     out = torch.empty(mask.size, dtype=torch.float32, device=dev)
     scratch = torch.empty(2 * mask.size, dtype=torch.int32, device=dev)
     st = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
@@ -276,13 +277,15 @@ class Prior:
     order = the lattice's active-node order) and the slice-wise
     Hagen-Poiseuille prior (rho - 1, u_z) from ``lbm_ws_prior``."""
 
-    def __init__(self, mask, inlet, tau, device=0):
+    def __init__(self, mask, inlet, tau, device=0, mask_dev=None):
         torch = _torch()
         self.dev = torch.device("cuda", device)
         self.shape = tuple(int(v) for v in mask.shape)
         self.n = int(mask.size)
-        self.mask = torch.from_numpy(np.ascontiguousarray(mask.reshape(-1), np.uint8)).to(self.dev)
-        self.idx = torch.from_numpy(np.flatnonzero(mask.reshape(-1) > 0).astype(np.int64)).to(self.dev)
+        self.mask = (mask_dev if mask_dev is not None else
+                     torch.from_numpy(np.ascontiguousarray(mask.reshape(-1), np.uint8)).to(self.dev))
+        # the fluid voxels in raster order, compacted on the device
+        self.idx = torch.nonzero(self.mask).reshape(-1)
         self.inlet = float(inlet)
         D = self.shape[0]
         f32 = dict(dtype=torch.float32, device=self.dev)
@@ -308,8 +311,9 @@ def features(mask, inlet_mean, period, tau=0.8, device=0):
     PyTorch element-wise operations)."""
     torch = _torch()
     dev = torch.device("cuda", device)
-    sdf = sdf_of_mask(mask, device)
-    prior = Prior(mask, inlet_mean, tau, device)
+    m = torch.from_numpy(np.ascontiguousarray(mask.reshape(-1), np.uint8)).to(dev)  # one upload of the mask
+    prior = Prior(mask, inlet_mean, tau, device, mask_dev=m)
+    sdf = sdf_of_mask(mask, device, mask_dev=m)
     x = torch.empty(mask.size * C_IN, dtype=torch.bfloat16, device=dev)
     capi._check(capi.load().lbm_ws_features(_ptr(sdf), _ptr(prior.mask), _ptr(prior.uz), _ptr(prior.drho),
                                             _dims(mask.shape), SDF_SCALE, inlet_mean * MEAN_SCALE,
