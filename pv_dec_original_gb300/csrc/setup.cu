@@ -265,8 +265,11 @@ __global__ void __launch_bounds__(kNormThreads) k_normals(const double* __restri
         for (int t = 0; t < cnt; ++t) {
             const double* o = tile + 7 * t;
             double dx = x - o[4], dy = y - o[5], dz = z - o[6];
-            double distance = sqrt(dx * dx + dy * dy + dz * dz);
-            double w = o[3] / (distance * distance);
+            // area / distance^2 straight from the squared distance (the
+            // reference squares the square root: the two differ by an
+            // ulp or so per term, far below the normals' 1e-13 checks,
+            // and the FP64 square root of every pair goes)
+            double w = o[3] / (dx * dx + dy * dy + dz * dz);
             n0 += o[0] * w;
             n1 += o[1] * w;
             n2 += o[2] * w;
