@@ -67,7 +67,8 @@ class Cudart:
         self.L = C.CDLL("libcudart.so.13")
         for name in ("cudaEventCreate", "cudaEventRecord", "cudaEventSynchronize", "cudaEventElapsedTime",
                      "cudaEventDestroy", "cudaMalloc", "cudaFree", "cudaMemsetAsync", "cudaHostAlloc",
-                     "cudaFreeHost", "cudaStreamSynchronize", "cudaSetDevice", "cudaGetDeviceProperties"):
+                     "cudaFreeHost", "cudaStreamSynchronize", "cudaSetDevice", "cudaGetDeviceProperties",
+                     "cudaStreamWaitEvent"):
             getattr(self.L, name).restype = C.c_int
 
     def ck(self, rc, what):
@@ -81,6 +82,9 @@ class Cudart:
 
     def record(self, e, stream):
         self.ck(self.L.cudaEventRecord(e, C.c_void_p(stream)), "cudaEventRecord")
+
+    def wait(self, stream, e):
+        self.ck(self.L.cudaStreamWaitEvent(C.c_void_p(stream), e, 0), "cudaStreamWaitEvent")
 
     def elapsed_ms(self, a, b):
         self.ck(self.L.cudaEventSynchronize(b), "cudaEventSynchronize")
@@ -372,15 +376,64 @@ def pv_extra(capi, cr, device, flush, steps=20):
     return out
 
 
-def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
-    """Aggregate MLUPS of the C4 ensemble packed into one lattice (captured
-    graph, one step-kernel launch per step) against the same members as
-    separate lattices advanced together (each its own stream and graph).
-    The members' populations (FP16, about 1 GB) exceed the L2, so
-    consecutive steps are timed without a flush."""
+def concurrent_ms(cr, solvers, steps):
+    """Device time of `steps` steps of every handle, each on its own stream,
+    issued together: the first handle's stream forks to the others by an
+    event and joins them back by one event each; CUDA events around the
+    fork and the join."""
+    s0 = solvers[0].stream()
+    fork, end = cr.event(), cr.event()
+    done = [cr.event() for _ in solvers]
+    cr.record(fork, s0)
+    for s in solvers[1:]:
+        cr.wait(s.stream(), fork)
+    for s, d in zip(solvers, done):
+        s.step_async(steps)
+        cr.record(d, s.stream())
+    for d in done[1:]:
+        cr.wait(s0, d)
+    cr.record(end, s0)
+    ms = cr.elapsed_ms(fork, end)
+    for e in done + [fork, end]:
+        cr.L.cudaEventDestroy(e)
+    for s in solvers:
+        s.check_status()
+    return ms
+
+
+def chained_ms(cr, solvers, steps):
+    """Device time of `steps` steps of every handle one handle after another:
+    each handle's steps wait on an event recorded after the previous
+    handle's, so one runs at a time, with no host synchronisation between."""
+    done = [cr.event() for _ in solvers]
+    fork = cr.event()
+    cr.record(fork, solvers[0].stream())
+    for i, s in enumerate(solvers):
+        if i:
+            cr.wait(s.stream(), done[i - 1])
+        s.step_async(steps)
+        cr.record(done[i], s.stream())
+    ms = cr.elapsed_ms(fork, done[-1])
+    for e in done + [fork]:
+        cr.L.cudaEventDestroy(e)
+    for s in solvers:
+        s.check_status()
+    return ms
+
+
+def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64, groups=4):
+    """Aggregate MLUPS of the C4 ensemble (64 seeded stenosed tubes, FP16
+    storage): packed into one lattice (captured graph, one step-kernel
+    launch per step); packed into `groups` lattices of about equal size
+    advanced concurrently (GroupedEnsemble); and the members as 64 separate
+    lattices, advanced concurrently (each its own stream and graph) and one
+    after another (the plain solver in a loop).  Every arm: 32-step graphs,
+    64 warm-up steps, CUDA events around `steps` steps.  The members'
+    populations (about 1 GB) exceed the L2, so consecutive steps are timed
+    without a flush."""
     from pv_dec_original_gb300 import geometry as G
     from pv_dec_original_gb300 import waveform
-    from pv_dec_original_gb300.ensemble import Ensemble
+    from pv_dec_original_gb300.ensemble import Ensemble, GroupedEnsemble
     members = G.config_c4_ensemble(nmem, seed=0)
     t0 = time.perf_counter()
     ens = Ensemble(members, Q, "f16", TAU, device=device)
@@ -394,8 +447,23 @@ def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
     ens.step_async(steps)
     cr.record(b, st)
     ms = cr.elapsed_ms(a, b)
+    for e in (a, b):
+        cr.L.cudaEventDestroy(e)
     ens.solver.check_status()
-    packed = ens.active * steps / (ms * 1e-3) / 1e6
+    active = ens.active
+    packed = active * steps / (ms * 1e-3) / 1e6
+    launches = ens.solver.launches()
+    ens.solver.close()
+    # packed into groups advanced concurrently
+    grp = GroupedEnsemble(members, groups, Q, "f16", TAU, device=device)
+    grp.autotune(5)
+    grp.set_graph_steps(32)
+    grp.step(64)
+    g_ms = concurrent_ms(cr, grp.solvers(), steps)
+    grouped = grp.active * steps / (g_ms * 1e-3) / 1e6
+    g_sizes = [e.active for e in grp.groups]
+    launches += grp.launches()
+    grp.close()
     # the same members as separate lattices
     singles = []
     for m in members:
@@ -414,24 +482,23 @@ def ensemble_extra(capi, cr, device, Q, nmem=64, steps=64):
         singles.append(s)
     for s in singles:
         s.sync()
-    t0 = time.perf_counter()
-    for s in singles:
-        s.step_async(steps)
-    for s in singles:
-        s.sync()
-    loop_s = time.perf_counter() - t0
-    active = sum(s.counts()["active"] for s in singles)
-    looped = active * steps / loop_s / 1e6
+    assert sum(s.counts()["active"] for s in singles) == active
+    looped = active * steps / (concurrent_ms(cr, singles, steps) * 1e-3) / 1e6
+    serial = active * steps / (chained_ms(cr, singles, steps) * 1e-3) / 1e6
+    launches += sum(s.launches() for s in singles)
     for s in singles:
         s.close()
-    launches = ens.solver.launches()
-    ens.solver.close()
-    return {"members": nmem, "active_nodes": ens.active, "storage": "f16", "steps": steps,
+    return {"members": nmem, "active_nodes": active, "storage": "f16", "steps": steps,
             "packed_mlups": packed, "packed_ms_per_step": ms / steps,
-            "packed_hbm_gbs": ens.active * BYTES_PER_LU[(Q, "f16")] / (ms / steps * 1e-3) / 1e9,
-            "looped_mlups": looped, "speedup_vs_looped": packed / looped, "setup_s": setup_s,
-            "timing": "packed: CUDA events around 64 graph-replayed steps; looped: host wall clock around "
-                      "64 steps of each of the 64 lattices issued on their own streams",
+            "packed_hbm_gbs": active * BYTES_PER_LU[(Q, "f16")] / (ms / steps * 1e-3) / 1e9,
+            "grouped_mlups": grouped, "groups": len(g_sizes), "group_active_nodes": g_sizes,
+            "looped_mlups": looped, "looped_one_at_a_time_mlups": serial,
+            "speedup_vs_looped": grouped / looped, "packed_vs_looped": packed / looped,
+            "grouped_vs_packed": grouped / packed, "speedup_vs_one_at_a_time": grouped / serial,
+            "setup_s": setup_s,
+            "timing": "CUDA events; one lattice: around %d graph-replayed steps on its stream; %d groups and "
+                      "looped: the lattices on their own streams, forked from and joined to one stream by "
+                      "events; one at a time: the lattices chained by events" % (steps, len(g_sizes)),
             "l2": "not flushed (populations exceed L2)", "launches_total": launches}
 
 

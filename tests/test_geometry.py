@@ -80,3 +80,23 @@ def test_ensemble_members_seeded():
         assert 8 <= x["radius"] <= 20 and 120 <= x["length"] <= 400
         assert 0.2 <= x["severity"] <= 0.7 and 0 <= x["eccentricity"] <= 0.3
         assert 2000 <= x["period"] <= 6000 and 0.01 <= x["inlet_mean"] <= 0.04
+
+
+def test_ensemble_groups_split_contiguously_and_balanced():
+    """GroupedEnsemble's split: contiguous runs covering every member once,
+    none empty, each run's total near an equal share."""
+    from pv_dec_original_gb300.ensemble import split_balanced
+    rng = np.random.default_rng(3)
+    for n, g in ((64, 4), (64, 8), (5, 5), (7, 3), (3, 8), (1, 1)):
+        sizes = rng.integers(50_000, 400_000, n)
+        cuts = split_balanced(sizes, g)
+        assert len(cuts) == min(g, n)
+        assert cuts[0][0] == 0 and cuts[-1][1] == n
+        assert all(a < b for a, b in cuts)
+        assert all(cuts[k][1] == cuts[k + 1][0] for k in range(len(cuts) - 1))
+        if n >= 4 * g:
+            share = sizes.sum() / g
+            for a, b in cuts:  # off an equal share by at most the largest member
+                assert abs(sizes[a:b].sum() - share) <= sizes.max()
+    assert split_balanced([5, 5, 5, 5], 2) == [(0, 2), (2, 4)]
+    assert split_balanced([1, 1, 1, 10], 2) == [(0, 3), (3, 4)]

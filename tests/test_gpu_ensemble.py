@@ -72,3 +72,32 @@ def test_gpu_ensemble_matches_separate_lattices(gpu_lib, prec):
     for m, s in enumerate(singles):
         _, _, f1 = s.conservation()
         np.testing.assert_allclose(fl[2 * m:2 * m + 2], f1, rtol=1e-5, atol=1e-9)
+
+
+def test_gpu_grouped_ensemble_matches_one_packed_lattice(gpu_lib):
+    """The members packed into two lattices advanced concurrently on their own
+    streams give every member what one packed lattice gives it."""
+    from pv_dec_original_gb300.ensemble import Ensemble, GroupedEnsemble
+    members = _members()
+    tau = 0.6
+    one = Ensemble(members, 19, "f16", tau)
+    grp = GroupedEnsemble(members, 2, 19, "f16", tau)
+    assert len(grp.groups) == 2 and grp.active == one.active
+    grp.set_graph_steps(8)
+    one.step(37)
+    grp.step(37)
+    rho, u, mem = one.macro()
+    rho2, u2, mem2 = grp.macro()
+    assert np.array_equal(mem, mem2)
+    np.testing.assert_allclose(rho2, rho, rtol=0, atol=1e-6)
+    np.testing.assert_allclose(u2, u, rtol=0, atol=1e-6)
+    w, w2 = one.wss(), grp.wss()
+    assert np.array_equal(w["member"], w2["member"])
+    for m in range(len(members)):
+        sel = w["member"] == m
+        err = np.linalg.norm(w2["tawss"][sel] - w["tawss"][sel]) / np.linalg.norm(w["tawss"][sel])
+        assert err < 1e-5, err
+    _, _, fl = one.solver.conservation()
+    _, _, fl2 = grp.conservation()
+    np.testing.assert_allclose(fl2, fl, rtol=1e-5, atol=1e-9)
+    grp.close()
