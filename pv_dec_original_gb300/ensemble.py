@@ -163,8 +163,8 @@ class GroupedEnsemble:
     One packed lattice advances step by step: every launch waits for the
     whole previous step, so each step ends in a drain where the last blocks
     run alone.  Independent lattices on their own streams fill each other's
-    drains (64 seeded stenosed tubes, FP16: 4 or 8 groups ran 1.05x one
-    packed lattice).  Advancing the groups one after another instead, so
+    drains (64 seeded stenosed tubes, FP16: 4 or 8 groups ran 1.04-1.05x
+    one packed lattice).  Advancing the groups one after another instead, so
     that a group's populations could stay in L2 across its steps, gained
     nothing (groups of 2 to 16 members: 0.91-1.01x one packed lattice).
 
@@ -233,3 +233,40 @@ class GroupedEnsemble:
     def close(self):
         for e in self.groups:
             e.solver.close()
+
+
+def main(argv=None):
+    """python -m pv_dec_original_gb300.ensemble [--members N] [--steps K]
+    [--precision f16] [--groups G] [--variant V]: build the seeded C4
+    ensemble (geometry.config_c4_ensemble, seed 0), advance it K steps (one
+    launch per step, no graph) and print its active nodes and the host-clock
+    MLUPS of those steps.  --variant fixes the launch shape (lbm_set_variant)
+    instead of the default one."""
+    import argparse
+    import time
+
+    from . import geometry as G
+    ap = argparse.ArgumentParser(prog="python -m pv_dec_original_gb300.ensemble")
+    ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--precision", default="f16", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--groups", type=int, default=1)
+    ap.add_argument("--variant", type=int, default=None)
+    ap.add_argument("--tau", type=float, default=0.55)
+    a = ap.parse_args(argv)
+    members = G.config_c4_ensemble(a.members, seed=0)
+    ens = GroupedEnsemble(members, a.groups, 19, a.precision, a.tau)
+    if a.variant is not None:
+        for s in ens.solvers():
+            s.set_variant(a.variant)
+    ens.sync()
+    t0 = time.perf_counter()
+    ens.step(a.steps)
+    dt = time.perf_counter() - t0
+    print(f"members {a.members} groups {len(ens.groups)} active {ens.active} steps {a.steps} "
+          f"host-clock MLUPS {ens.active * a.steps / dt / 1e6:.0f} launches {ens.launches()}")
+    ens.close()
+
+
+if __name__ == "__main__":
+    main()
