@@ -16,7 +16,8 @@
 // rows 16 bytes apart.
 //   input:   [channel half k (2)][x parity p (S)][z][y][x / S][8 channels]
 //            (a parity plane padded to 128 bytes)
-//   weights: [tap][co / 8][channel half k][co % 8][8 channels]
+//   weights: [tap block][co / 8][channel half k][co % 8][8 channels]
+//            (tap block: weight_block)
 // The 128 output voxels of one z plane (8 x by 16 y) are the M = 128 rows
 // of one MMA: row m = 8 y + x.  Output x reads input x = S x + tx - 1, so
 // with the input's x split by parity (stride 2: even and odd columns in
@@ -26,17 +27,21 @@
 // slice are one staged block apart: the leading-dimension offset.  A tap
 // (tx, ty, tz) is just the descriptor's start address (parity tx mod S,
 // column tx / S, row ty, plane S z + tz): the 27 taps reuse the staged block
-// with no copies.  One elected thread issues the TZ planes x 27 taps MMAs of
-// a chunk (M = 128, N = co, K = 16, BF16 x BF16 -> FP32) into TZ
-// accumulators of co tensor-memory columns each and commits them to an
-// mbarrier; every wait is bounded.  The epilogue reads the accumulators with
-// tcgen05.ld (warp w owns tensor-memory lanes 32 w .. 32 w + 31, i.e. rows
-// y = 4 w .. 4 w + 3), adds the bias, applies ReLU and stores BF16 (and
-// FP32 when asked) channels-last.
+// with no copies.  One elected thread issues the MMAs of a chunk (M = 128,
+// K = 16, BF16 x BF16 -> FP32) into TZ accumulators of co tensor-memory
+// columns each and commits them to an mbarrier; every wait is bounded.  At
+// stride 2: TZ x 27 MMAs of N = co.  At stride 1 the accumulators of the
+// TZ planes are adjacent column ranges and one staged plane feeds up to
+// three output planes (through taps tz = 2, 1, 0), so each (ty, tx) takes
+// one MMA per staged plane with N = 1-3 co: 9 x 6 = 54 MMAs instead of
+// 4 x 27, each reading its A operand once.  The epilogue reads the
+// accumulators with tcgen05.ld (warp w owns tensor-memory lanes 32 w ..
+// 32 w + 31, i.e. rows y = 4 w .. 4 w + 3), adds the bias, applies ReLU and
+// stores BF16 (and FP32 when asked) channels-last.
 //
 // Bound: the A operand (the staged input, 4 KB per MMA) is read from shared
-// memory by every MMA, 2 co FLOP a byte; at co = 16 that operand traffic,
-// not the tensor pipe, sets the rate (see the convolution profile).
+// memory by every MMA; at co = 16 that operand traffic, not the tensor
+// pipe, sets the rate (see the convolution profile).
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -156,6 +161,17 @@ __host__ __device__ constexpr uint32_t tmem_cols() {
     return Geo<S>::TZ * CO < 32 ? 32u : (uint32_t)(Geo<S>::TZ * CO);  // a power of two for CO in {16, 32, 64}
 }
 
+// Shared-memory block of tap t = 9 tz + 3 ty + tx in the staged weights.
+// Stride 1 groups the three z taps of each (ty, tx) in the order tz = 2, 1,
+// 0, so that one MMA of N = 3 co takes all three: staged plane zz feeds
+// output planes zz - 2, zz - 1, zz through taps tz = 2, 1, 0, and the
+// accumulators of those planes are the adjacent tensor-memory column
+// ranges (z co .. z co + co - 1 for plane z).  Stride 2 keeps tap order.
+template <int S>
+__host__ __device__ constexpr int weight_block(int t) {
+    return S == 1 ? ((t / 3) % 3 * 3 + t % 3) * 3 + (2 - t / 9) : t;
+}
+
 // x [Di][Hi][Wi][ci] (read through `map`: the 4-D tensor map of x, box
 // 8 channels x (XH, or 2 XH with element stride 2) x YB x ZB), w [co][27][ci],
 // y [Do][Ho][Wo][co] with Do = Di / S etc.; Do % TZ == 0, Ho % 16 == 0,
@@ -213,7 +229,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const __grid_constant__ C
         // the weights of this chunk
         for (int i = tid; i < 27 * CO * 2; i += kThreads) {
             const int k = i & 1, n = (i >> 1) % CO, t = (i >> 1) / CO;
-            cp_async16(w_a + t * (CO * 32) + (n >> 3) * 256 + k * 128 + (n & 7) * 16,
+            cp_async16(w_a + weight_block<S>(t) * (CO * 32) + (n >> 3) * 256 + k * 128 + (n & 7) * 16,
                        w + ((int64_t)n * 27 + t) * ci + c * 16 + k * 8, true);
         }
         asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
@@ -222,14 +238,41 @@ __global__ void __launch_bounds__(kThreads) k_conv3_tc(const __grid_constant__ C
         if (tid == 0) {
             if (mbar_wait(saddr(bar + 1), (uint32_t)(c & 1))) {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                for (int z = 0; z < G::TZ; ++z) {
-                    for (int t = 0; t < 27; ++t) {
-                        const int tz = t / 9, ty = (t / 3) % 3, tx = t % 3;
-                        const int zz = S * z + tz, p = tx % S, xo = tx / S;
-                        const uint32_t a = tile_a + p * G::PLANE + ((zz * G::YB + ty) * G::XH + xo) * 16;
-                        const uint64_t ad = smem_desc(a, G::HALF, SBO);
-                        const uint64_t bd = smem_desc(w_a + t * (CO * 32), 128, 256);
-                        mma_bf16(tmem + (uint32_t)(z * CO), ad, bd, IDESC, (c > 0 || t > 0) ? 1u : 0u);
+                if constexpr (S == 1) {
+                    // per (ty, tx): one MMA per staged plane zz, into output
+                    // planes lo .. hi - 1 (N = (hi - lo) co) with the taps
+                    // tz = zz - lo .. zz - hi + 1 (weight_block); 54 MMAs
+                    // instead of 108, each reading its A operand once.  The
+                    // first (ty, tx) of the first chunk starts with planes 2
+                    // and 5, whose output ranges (0..2 and 3) cover every
+                    // accumulator once: they initialise it.
+                    static_assert(G::TZ == 4 && G::ZB == 6, "merged z taps: 4 output planes, 6 staged");
+                    constexpr int kOrder[6] = {2, 5, 0, 1, 3, 4};
+                    constexpr uint32_t ID1 = idesc_bf16(128, CO), ID2 = idesc_bf16(128, 2 * CO),
+                                       ID3 = idesc_bf16(128, 3 * CO);
+                    for (int u = 0; u < 9; ++u) {
+                        const int ty = u / 3, tx = u % 3;
+                        for (int j = 0; j < 6; ++j) {
+                            const int zz = kOrder[j];
+                            const int lo = zz > 2 ? zz - 2 : 0, hi = zz + 1 < G::TZ ? zz + 1 : G::TZ;
+                            const int np = hi - lo, b0 = 2 - (zz - lo);
+                            const uint32_t a = tile_a + ((zz * G::YB + ty) * G::XH + tx) * 16;
+                            const uint64_t ad = smem_desc(a, G::HALF, SBO);
+                            const uint64_t bd = smem_desc(w_a + (u * 3 + b0) * (CO * 32), 128, 256);
+                            mma_bf16(tmem + (uint32_t)(lo * CO), ad, bd, np == 3 ? ID3 : (np == 2 ? ID2 : ID1),
+                                     (c > 0 || u > 0 || j >= 2) ? 1u : 0u);
+                        }
+                    }
+                } else {
+                    for (int z = 0; z < G::TZ; ++z) {
+                        for (int t = 0; t < 27; ++t) {
+                            const int tz = t / 9, ty = (t / 3) % 3, tx = t % 3;
+                            const int zz = S * z + tz, p = tx % S, xo = tx / S;
+                            const uint32_t a = tile_a + p * G::PLANE + ((zz * G::YB + ty) * G::XH + xo) * 16;
+                            const uint64_t ad = smem_desc(a, G::HALF, SBO);
+                            const uint64_t bd = smem_desc(w_a + weight_block<S>(t) * (CO * 32), 128, 256);
+                            mma_bf16(tmem + (uint32_t)(z * CO), ad, bd, IDESC, (c > 0 || t > 0) ? 1u : 0u);
+                        }
                     }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
