@@ -153,6 +153,9 @@ class Ensemble:
         w["member"] = self.member_of_z(w["pt"] // nxy)
         return w
 
+    def close(self):
+        self.solver.close()
+
 
 class GroupedEnsemble:
     """The members packed into `groups` lattices instead of one: contiguous
@@ -232,7 +235,7 @@ class GroupedEnsemble:
 
     def close(self):
         for e in self.groups:
-            e.solver.close()
+            e.close()
 
 
 def main(argv=None):
