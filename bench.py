@@ -649,7 +649,7 @@ def conv_forward_c5(device, dims=(256, 128, 128), reps=5):
     out = {"grid": list(dims), "gflop": flops / 1e9}
     outputs = {}
     try:
-        for name, engine in (("mma_sync", 1), ("tcgen05", 0)):
+        for name, engine in (("mma_sync", capi.LBM_NN_ENGINE_MMA_SYNC), ("tcgen05", capi.LBM_NN_ENGINE_AUTO)):
             capi._check(L.lbm_nn_set_conv_engine(engine))
             big.forward(xb)
             torch.cuda.synchronize(dev)
@@ -690,7 +690,7 @@ def conv_forward_c5(device, dims=(256, 128, 128), reps=5):
         # sample on each engine
         tgt = torch.rand(nvox * 4, device=dev, generator=g)
         msk = torch.ones(nvox, dtype=torch.uint8, device=dev)
-        for name, engine in (("mma_sync", 1), ("tcgen05", 0)):
+        for name, engine in (("mma_sync", capi.LBM_NN_ENGINE_MMA_SYNC), ("tcgen05", capi.LBM_NN_ENGINE_AUTO)):
             capi._check(L.lbm_nn_set_conv_engine(engine))
 
             def train_step():
@@ -708,7 +708,7 @@ def conv_forward_c5(device, dims=(256, 128, 128), reps=5):
             torch.cuda.synchronize(dev)
             out[name]["train_step_ms"] = ev[0].elapsed_time(ev[1]) / reps
     finally:
-        L.lbm_nn_set_conv_engine(0)
+        L.lbm_nn_set_conv_engine(capi.LBM_NN_ENGINE_AUTO)
     capi._check(L.lbm_nn_conv_status())
     a, b = outputs["tcgen05"], outputs["mma_sync"]
     out["engines_output_max_rel_diff"] = float((a - b).abs().max() / b.abs().max().clamp_min(1e-30))

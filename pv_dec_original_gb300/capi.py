@@ -23,6 +23,7 @@ LBM_COLLISION_BGK = 0
 LBM_COLLISION_REGULARIZED = 1
 MAX_WAVES = 256
 LBM_FLAG_NONFINITE, LBM_FLAG_BOUNDS = 1, 4
+LBM_NN_ENGINE_AUTO, LBM_NN_ENGINE_MMA_SYNC = 0, 1  # lbm_nn_set_conv_engine (include/lbm_nn.h)
 
 ERRORS = {-1: "LBM_ERR_ARG", -2: "LBM_ERR_CUDA", -3: "LBM_ERR_STATE", -4: "LBM_ERR_NONFINITE",
           -5: "LBM_ERR_ALLOC", -6: "LBM_ERR_IO", -7: "LBM_ERR_UNSUPPORTED"}

@@ -27,12 +27,13 @@ def test_python_binding_constants_match_header():
     """The ctypes binding mirrors the header's constants; a stale mirror of
     LBM_NUM_VARIANTS sizes lbm_autotune's output array too small."""
     from pv_dec_original_gb300 import capi
-    txt = open(os.path.join(ROOT, "include", "lbm_gb300.h")).read()
+    txt = "".join(open(os.path.join(ROOT, "include", f)).read() for f in ("lbm_gb300.h", "lbm_nn.h"))
     h = {k: int(v) for k, v in re.findall(r"#define\s+(LBM_\w+)\s+(-?\d+)", txt)}
     mirror = {"LBM_NUM_VARIANTS": capi.NUM_VARIANTS, "LBM_MAX_BC": capi.MAX_BC, "LBM_MAX_WAVES": capi.MAX_WAVES}
     for k in ("LBM_F64", "LBM_F32", "LBM_F16", "LBM_BF16", "LBM_PARITY", "LBM_PHYSICS", "LBM_BC_REF_INLET",
               "LBM_BC_REF_OUTLET_YMAX", "LBM_BC_REF_OUTLET_ZMIN", "LBM_BC_VELOCITY", "LBM_BC_PRESSURE",
-              "LBM_COLLISION_BGK", "LBM_COLLISION_REGULARIZED", "LBM_FLAG_NONFINITE", "LBM_FLAG_BOUNDS"):
+              "LBM_COLLISION_BGK", "LBM_COLLISION_REGULARIZED", "LBM_FLAG_NONFINITE", "LBM_FLAG_BOUNDS",
+              "LBM_NN_ENGINE_AUTO", "LBM_NN_ENGINE_MMA_SYNC"):
         mirror[k] = getattr(capi, k)
     for face, v in capi.FACES.items():
         mirror["LBM_FACE_" + {"x": "X", "y": "Y", "z": "Z"}[face[0]] + ("MIN" if face[1] == "-" else "MAX")] = v
