@@ -100,3 +100,90 @@ def test_ensemble_groups_split_contiguously_and_balanced():
                 assert abs(sizes[a:b].sum() - share) <= sizes.max()
     assert split_balanced([5, 5, 5, 5], 2) == [(0, 2), (2, 4)]
     assert split_balanced([1, 1, 1, 10], 2) == [(0, 3), (3, 4)]
+
+
+def test_grouped_ensemble_bookkeeping_on_the_host(monkeypatch):
+    """GroupedEnsemble's host logic with stand-in groups (no device): the
+    groups are contiguous member runs balanced by fluid voxels, every call
+    reaches every group, and read-outs come back in member order with global
+    member indices."""
+    from pv_dec_original_gb300 import ensemble as E
+    sizes = [5, 9, 4, 7, 6, 8, 3]
+    calls = []
+
+    class FakeSolver:
+        def __init__(self, g):
+            self.g = g
+
+        def stream(self):
+            return 1000 + self.g
+
+        def autotune(self, n):
+            calls.append(("tune", self.g, n))
+            return 6, []
+
+        def set_graph_steps(self, n):
+            calls.append(("graph", self.g, n))
+
+        def sync(self):
+            calls.append(("sync", self.g))
+
+        def check_status(self):
+            calls.append(("status", self.g))
+
+        def launches(self):
+            return 10 + self.g
+
+        def conservation(self):
+            n = len(groups[self.g])
+            return 1.0, np.ones(3), np.arange(2 * n, dtype=float) + 100 * self.g
+
+        def close(self):
+            calls.append(("close", self.g))
+
+    groups = []
+
+    class FakeEnsemble:
+        def __init__(self, members, Q, precision, tau, parts=None, **kw):
+            self.g = len(groups)
+            groups.append(members)
+            self.solver = FakeSolver(self.g)
+            self.n = [int(np.count_nonzero(p[1])) for p in parts]
+            self.active = sum(self.n)
+
+        def step_async(self, n):
+            calls.append(("step", self.g, n))
+
+        def macro(self):
+            mem = np.repeat(np.arange(len(self.n)), self.n)
+            return np.full(self.active, float(self.g)), np.zeros((self.active, 3)), mem
+
+        def wss(self):
+            mem = np.repeat(np.arange(len(self.n)), 2)
+            return {"pt": np.arange(len(mem)), "tawss": np.full(len(mem), float(self.g)), "member": mem}
+
+        def close(self):
+            self.solver.close()
+
+    parts = [(None, np.ones(s, np.uint8), None) for s in sizes]
+    monkeypatch.setattr(E, "voxelize_members", lambda members: parts)
+    monkeypatch.setattr(E, "Ensemble", FakeEnsemble)
+    members = [{"k": k} for k in range(len(sizes))]
+    grp = E.GroupedEnsemble(members, 3, 19, "f16", 0.55)
+    assert [len(m) for m in groups] == [2, 2, 3]  # 14 / 11 / 17 of 42 fluid voxels (targets 14, 28)
+    assert grp.first == [0, 2, 4] and grp.active == sum(sizes)
+    assert [m["k"] for g in groups for m in g] == list(range(len(sizes)))
+    grp.set_graph_steps(32)
+    grp.step(7)
+    assert [c for c in calls if c[0] == "step"] == [("step", g, 7) for g in range(3)]
+    assert {c[1] for c in calls if c[0] == "sync"} == {0, 1, 2}
+    rho, u, mem = grp.macro()
+    assert np.array_equal(mem, np.repeat(np.arange(len(sizes)), sizes))
+    assert np.array_equal(rho, np.repeat([0.0, 1.0, 2.0], [14, 11, 17]))
+    w = grp.wss()
+    assert np.array_equal(w["member"], np.repeat(np.arange(len(sizes)), 2)) and "pt" not in w
+    mass, mom, flux = grp.conservation()
+    assert mass == 3.0 and np.array_equal(mom, np.full(3, 3.0)) and len(flux) == 2 * len(sizes)
+    assert grp.launches() == 33
+    grp.close()
+    assert {c[1] for c in calls if c[0] == "close"} == {0, 1, 2}
